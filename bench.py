@@ -1,0 +1,307 @@
+"""Benchmark: hits/s of the GB300 tracer (FP32 traversal + FP64 recheck) and of the plain FP64 kernel.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload c2|c1]
+
+A step traces one batch of desorptions to absorption on the workload's geometry.
+`value` = hits (Sum nbMCHit, src/MolflowCLI.cpp:61-68) per second of device time
+over K timed steps, max over ranks; `e2e` = the same through the public API with
+the tallies read back to host memory every step.  One JSON line on rank 0.
+Under torchrun each rank traces its own particle range (no data-path collective).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "c1": dict(name="config1_tube_L10cm_R1cm_64gon_tex64x64_maxwell_N2_293K", step=100_000_000, fp64_step=5_000_000),
+    "c2": dict(name="config2_beam_chamber_200k_triangles", step=10_000_000, fp64_step=500_000),
+}
+
+
+def make_model(workload):
+    from molflow_sources_gb300 import workloads
+    if workload == "c1":
+        return workloads.config1_tube()
+    return workloads.config2_beam_chamber()
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def oracle_visit_counts(model, n=2000):
+    """Mean BVH nodes visited and facets tested per ray, counted by the instrumented CPU oracle."""
+    from oracle.oracle import Oracle
+    st, s = Oracle(model).run(n, seed=7, threads=0)
+    return s["node_visits"] / s["rays"], s["prim_tests"] / s["rays"], s
+
+
+def bytes_per_hit(model, nodes, prims):
+    """Algorithmic bytes per hit: node and facet records visited (FP32 layout), the FP64
+    hit-facet record, and the tally read-modify-writes (counters 4x8 B, texture 3x8 B when textured)."""
+    L = model.layout()
+    textured = float(np.mean(L["tex_off"] >= 0))
+    return nodes * 32 + prims * 64 + 160 + 2 * (4 * 8 + textured * 3 * 8)
+
+
+def cpu_baseline(model, target_s=10.0):
+    from oracle.oracle import Oracle
+    orc = Oracle(model)
+    st, s = orc.run(2000, seed=11)
+    rate_des = s["desorbed"] / max(s["seconds"], 1e-6)
+    n = int(max(1000, min(rate_des * target_s, 5e8)))
+    st, s = orc.run(n, seed=12, first_particle=10 ** 12)
+    return {"value": s["hits"] / s["seconds"], "unit": "hits/s", "cores": s["threads"], "kind": "port",
+            "sample": "%d desorptions (%d hits) of the same workload, %.1f s" % (n, s["hits"], s["seconds"]),
+            "seconds": s["seconds"]}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    model = make_model(args.workload)
+    t0 = time.time()
+    steps = []
+    hits_total = 0
+    secs_total = 0.0
+    from oracle.oracle import Oracle
+    orc = Oracle(model)
+    for _ in range(args.warmup):
+        orc.run(500, seed=3)
+    st, s = orc.run(2000, seed=4)
+    rate_des = s["desorbed"] / max(s["seconds"], 1e-6)
+    n = int(max(500, min(rate_des * args.ref_step_s, 5e8)))
+    for k in range(args.steps):
+        st, s = orc.run(n, seed=5, first_particle=k * n)
+        steps.append(s["seconds"])
+        hits_total += s["hits"]
+        secs_total += s["seconds"]
+    v = hits_total / secs_total
+    line = {"metric": "hits/s per GB300 host (CPU reference arm)", "value": v, "unit": "hits/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs_total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": WORKLOADS[args.workload]["name"], "desorptions_per_step": n},
+            "cpu_baseline": {"value": v, "unit": "hits/s", "cores": s["threads"], "kind": "port",
+                             "sample": "%d desorptions per step x %d steps" % (n, args.steps)},
+            "e2e": {"value": v, "unit": "hits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference tracer cannot be built (src_shared submodule absent); the arm runs the FP64 CPU "
+                    "restatement of ParticleTracer in oracle/ on all host cores",
+            "wall_s": time.time() - t0}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=os.environ.get("MFG_BENCH_WORKLOAD", "c2"), choices=list(WORKLOADS))
+    ap.add_argument("--step-desorptions", type=int, default=0)
+    ap.add_argument("--ref-step-s", type=float, default=6.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from molflow_sources_gb300 import _abi as A
+    from molflow_sources_gb300.simulation import GpuSimulation
+
+    W = WORKLOADS[args.workload]
+    n_step = args.step_desorptions or W["step"]
+    model = make_model(args.workload)
+    t0 = time.time()
+    sim = GpuSimulation(model, device=local)
+    load_s = time.time() - t0
+    sim.set_particle_offset(rank * (1 << 48))
+    seed = 0x4D6F6C66
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    # plain FP64 kernel on the same workload (smaller batch; hits/s is a rate)
+    for _ in range(1):
+        sim.SimulationMCStep(W["fp64_step"] // 10, precision=A.PREC_FP64, seed=seed)
+    f64_ms = 0.0
+    f64_hits = 0
+    for _ in range(2):
+        sim.SimulationMCStep(W["fp64_step"], precision=A.PREC_FP64, seed=seed)
+        f64_ms += sim.last_stats["kernel_ms"]
+        f64_hits += sim.last_stats["hits"]
+    fp64_rate = f64_hits / (f64_ms / 1e3)
+
+    for _ in range(args.warmup):
+        sim.SimulationMCStep(n_step, precision=A.PREC_FP32R, seed=seed)
+    sim.ResetSimulation()
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier()
+    kernel_ms = []
+    hits = 0
+    rechecks = 0
+    launches = 0
+    des = 0
+    for k in range(args.steps):
+        flush.fill_(k & 0xFF)   # L2 flush between steps (outside the kernel's event pair)
+        sim.SimulationMCStep(n_step, precision=A.PREC_FP32R, seed=seed)
+        st = sim.last_stats
+        kernel_ms.append(st["kernel_ms"])
+        hits += st["hits"]
+        rechecks += st["rechecks"]
+        launches += st["kernel_launches"]
+        des += st["desorbed"]
+    barrier()
+    # end to end: public API call + tallies copied to host memory every step
+    from molflow_sources_gb300.model import SimuState
+    gstate = SimuState(model)
+    e2e_hits = 0
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for k in range(max(1, args.steps // 2)):
+        sim.SimulationMCStep(n_step, precision=A.PREC_FP32R, seed=seed)
+        e2e_hits += sim.last_stats["hits"]
+        sim.UpdateHitsAndLog(gstate)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t1
+    clocks = sampler.stop()
+    dev_s = sum(kernel_ms) / 1e3
+    rate = hits / dev_s
+    e2e_rate = e2e_hits / e2e_s
+    if dist is not None:
+        t = torch.tensor([dev_s, e2e_s, float(hits), float(e2e_hits)], dtype=torch.float64, device="cuda")
+        mx = t.clone()
+        dist.all_reduce(mx[:2], op=dist.ReduceOp.MAX)
+        tot = t.clone()
+        dist.all_reduce(tot[2:], op=dist.ReduceOp.SUM)
+        rate = float(tot[2]) / float(mx[0])
+        e2e_rate = float(tot[3]) / float(mx[1])
+        dev_s = float(mx[0])
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+    nodes, prims, _ = oracle_visit_counts(model)
+    bph = bytes_per_hit(model, nodes, prims)
+    peak, peak_kind = measured_peaks()
+    mean_launch_s = dev_s / args.steps
+    achieved = (hits / args.steps) * bph / mean_launch_s / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic_%s.json" % args.workload)
+    if os.path.exists(tp):
+        with open(tp) as f:
+            tj = json.load(f)
+        traffic = tj.get("dram_bytes_per_hit", 0) * hits / args.steps
+    cpu = None if args.no_cpu_baseline else cpu_baseline(model)
+    L = model.layout()
+    d2h = 8 * (A.G_N + L["blocks"] * model.n_facets * (A.FC_N + A.FS_N) + L["blocks"] * L["texture_cells"] * 3 +
+               L["blocks"] * L["profile_facets"] * 300 + L["anglemap_cells"])
+    line = {
+        "metric": "hits/s per GB300: FP32+FP64-recheck vs plain FP64 kernel at same 3sigma transmission",
+        "value": rate, "unit": "hits/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": W["name"], "desorptions_per_step": n_step, "facets": model.n_facets,
+                   "precision": "FP32 traversal + FP64 recheck", "l2": "256 MiB write between timed steps",
+                   "parallelism": "particle ranges per rank" if world > 1 else "single GPU"},
+        "fp64_kernel_hits_per_s": fp64_rate, "fp32r_over_fp64": rate / fp64_rate,
+        "desorptions_per_s": des / dev_s * (world if dist is None else 1),
+        "recheck_fraction": rechecks / max(hits + des, 1),
+        "e2e": {"value": e2e_rate, "unit": "hits/s", "h2d_bytes_per_step": int(A.RunOptions.__basicsize__ if hasattr(A.RunOptions, "__basicsize__") else 48),
+                "d2h_bytes_per_step": int(d2h), "api": "SimulationMCStep + UpdateHitsAndLog (C ABI mfg_run + mfg_fetch)"},
+        "gpu_launches": launches,
+        "model_load_s": load_s,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "bytes_per_hit": bph, "nodes_per_ray": nodes, "facets_per_ray": prims,
+                     "peak_kind": peak_kind},
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

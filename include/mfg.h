@@ -1,0 +1,275 @@
+/*
+ * mfg.h — C ABI of the GB300 test-particle Monte Carlo tracer.
+ *
+ * This library replaces the CPU worker threads that run MolFlow+'s
+ * `MFSim::ParticleTracer::SimulationMCStep` (src/Simulation/Particle.cpp:207-396)
+ * and the BVH `Intersect` it calls (src/Simulation/Particle.cpp:245).  The caller
+ * hands over a `MolflowSimulationModel`-equivalent flat descriptor and reads back
+ * a `GlobalSimuState`-shaped result (src/Simulation/MolflowSimGeom.h:106-154).
+ *
+ * Conventions
+ *   - Plain C: pointers, sizes, int status codes.  No exception crosses the ABI.
+ *   - Every `const` pointer in a descriptor is read during the call that takes it
+ *     and copied; the caller keeps ownership.
+ *   - Units follow the reference: lengths in cm, time in s, speeds in m/s,
+ *     outgassing in Pa*m^3/s, temperature in K, gas mass in g/mol.
+ *   - One handle is used by one host thread at a time (the library serialises
+ *     calls on a handle with a mutex); different handles are independent.
+ */
+#ifndef MFG_H
+#define MFG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MFG_ABI_VERSION 1u
+
+/* ---- status codes (replace the reference's exceptions / MCStepResult,
+ *      src/Simulation/Particle.h:24-28, src/Simulation/MolflowSimGeom.cpp:219-247) ---- */
+#define MFG_OK                       0
+#define MFG_ERR_INVALID_MODEL        1  /* model descriptor rejected (SanityCheck, MolflowSimGeom.cpp:337-404) */
+#define MFG_ERR_NO_SOURCE            2  /* no desorbing facet (MCStepResult::DesorptionError, Particle.cpp:228-231,466-469) */
+#define MFG_ERR_TIMEOUT              3  /* wait or kernel time limit reached (GetHitLock timeout, MolflowSimGeom.cpp:1239-1248) */
+#define MFG_ERR_ABORTED              4  /* mfg_abort() was called while running */
+#define MFG_ERR_CUDA                 5  /* CUDA runtime error; text in mfg_last_error */
+#define MFG_ERR_UNSUPPORTED_FEATURE  6  /* model uses a feature this build does not trace */
+#define MFG_ERR_INVALID_ARGUMENT     7
+#define MFG_ERR_BUSY                 8  /* a run is still in flight on this handle */
+#define MFG_ERR_NO_DEVICE            9
+#define MFG_ERR_LIMIT               10  /* a size exceeds a documented limit */
+
+/* desorption types, src/MolflowTypes.h:17-21 */
+#define MFG_DES_NONE      0
+#define MFG_DES_UNIFORM   1
+#define MFG_DES_COSINE    2
+#define MFG_DES_COSINE_N  3
+#define MFG_DES_ANGLEMAP  4
+
+/* profile types, src/MolflowTypes.h:29-35 */
+#define MFG_PROFILE_NONE          0
+#define MFG_PROFILE_U             1
+#define MFG_PROFILE_V             2
+#define MFG_PROFILE_ANGULAR       3
+#define MFG_PROFILE_VELOCITY      4
+#define MFG_PROFILE_ORT_VELOCITY  5
+#define MFG_PROFILE_TAN_VELOCITY  6
+#define MFG_PROFILE_SIZE        100   /* bins per profile (value stored by the reference's fixtures) */
+
+/* texture recording flags (facet sh.countDes/countAbs/countRefl/countTrans/countDirection) */
+#define MFG_COUNT_DES    1u
+#define MFG_COUNT_ABS    2u
+#define MFG_COUNT_REFL   4u
+#define MFG_COUNT_TRANS  8u
+#define MFG_COUNT_DIR   16u
+
+/* fields of one FacetHitBuffer in a state view (fields named at Particle.cpp:1200-1207) */
+#define MFG_FC_NBMCHIT    0   /* facet_counts: u64 */
+#define MFG_FC_NBDESORBED 1
+#define MFG_FC_NBABSORBED 2
+#define MFG_FC_N          3
+#define MFG_FS_NBHITEQUIV          0   /* facet_sums: double */
+#define MFG_FS_NBABSEQUIV          1
+#define MFG_FS_SUM_1_PER_ORT_VEL   2
+#define MFG_FS_SUM_V_ORT           3
+#define MFG_FS_SUM_1_PER_VELOCITY  4
+#define MFG_FS_N                   5
+/* global counters (GlobalHitBuffer, Particle.cpp:36-45) */
+#define MFG_G_NBMCHIT      0
+#define MFG_G_NBHITEQUIV   1
+#define MFG_G_NBDESORBED   2
+#define MFG_G_NBABSEQUIV   3
+#define MFG_G_NBLEAK       4
+#define MFG_G_DIST_TOTAL   5
+#define MFG_G_DIST_FULLHITS 6
+#define MFG_G_N            8
+
+/*
+ * Model descriptor: the fields of MolflowSimulationModel that the tracer reads
+ * (src/Simulation/MolflowSimGeom.h:158-232, facet fields used in Particle.cpp).
+ * Per-facet arrays have n_facets entries.  Optional arrays may be NULL and then
+ * take the reference's defaults (given in brackets).
+ */
+typedef struct mfg_model_desc {
+    uint32_t abi_version;              /* MFG_ABI_VERSION */
+    int32_t  n_vertices;
+    const double*  vertices;           /* [n_vertices*3] (x,y,z) cm — vertices3 */
+    int32_t  n_facets;
+    const int32_t* facet_vertex_start; /* [n_facets+1] offsets into facet_vertex_index */
+    const int32_t* facet_vertex_index; /* polygon vertex indices (facet->indices), right-hand rule gives N */
+
+    const double*  sticking;           /* sh.sticking                     [0] */
+    const double*  opacity;            /* sh.opacity                      [1] */
+    const double*  outgassing;         /* sh.outgassing Pa*m3/s           [0] */
+    const double*  temperature;        /* sh.temperature K                [293.15] */
+    const double*  accommodation;      /* sh.accomodationFactor           [1] */
+    const int32_t* desorb_type;        /* sh.desorbType                   [DES_NONE] */
+    const double*  desorb_exponent;    /* sh.desorbTypeN                  [0] */
+    const double*  refl_diffuse;       /* sh.reflection.diffusePart       [1] */
+    const double*  refl_specular;      /* sh.reflection.specularPart      [0] */
+    const double*  refl_cos_exponent;  /* sh.reflection.cosineExponent    [0] */
+    const uint8_t* is_2sided;          /* sh.is2sided                     [0] */
+    const int32_t* structure;          /* sh.superIdx (-1: all structures) [0] */
+    const int32_t* link_dest;          /* sh.superDest (0: none)          [0] */
+    const int32_t* teleport_dest;      /* sh.teleportDest (0: none)       [0] */
+    const double*  tex_width;          /* sh.texWidth_precise (0: no texture)  [0] */
+    const double*  tex_height;         /* sh.texHeight_precise            [0] */
+    const uint32_t* count_flags;       /* MFG_COUNT_* bits                [0] */
+    const int32_t* profile_type;       /* sh.profileType                  [PROFILE_NONE] */
+    const double*  max_speed;          /* sh.maxSpeed for velocity profiles [0] */
+    const int32_t* anglemap_phi_width;       /* anglemapParams.phiWidth (record when >0 and record flag) [0] */
+    const double*  anglemap_theta_limit;     /* anglemapParams.thetaLimit  [1.570796326] */
+    const int32_t* anglemap_theta_lower_res; /* anglemapParams.thetaLowerRes [0] */
+    const int32_t* anglemap_theta_higher_res;/* anglemapParams.thetaHigherRes [0] */
+    const uint8_t* anglemap_record;          /* anglemapParams.record [0] */
+    const int32_t* sticking_param;     /* index into params (-1: constant) [-1] */
+    const int32_t* opacity_param;      /* [-1] */
+    const int32_t* outgassing_param;   /* [-1] */
+    const int32_t* temperature_param;  /* [-1] */
+    const uint8_t* enable_sojourn;     /* sh.enableSojournTime [0] */
+    const double*  sojourn_freq;       /* sh.sojournFreq [0] */
+    const double*  sojourn_e;          /* sh.sojournE J/mol [0] */
+    const uint8_t* is_moving;          /* sh.isMoving [0] */
+
+    /* simulation parameters (MolflowSimulationModel::sp, otfParams) */
+    double   gas_mass;                 /* sp.gasMass g/mol */
+    int32_t  use_maxwell;              /* sp.useMaxwellDistribution */
+    int32_t  constant_flow;            /* sp.calcConstantFlow */
+    double   time_window;              /* sp.timeWindowSize s (latestMoment when no moments) */
+    int32_t  enable_decay;             /* sp.enableDecay */
+    double   half_life;                /* sp.halfLife s */
+    int32_t  low_flux_mode;            /* otfParams.lowFluxMode */
+    double   low_flux_cutoff;          /* otfParams.lowFluxCutoff */
+    int32_t  n_structures;             /* sh.nbSuper (>=1) */
+
+    /* time moments (tdParams.moments): centre and window, sorted by centre */
+    int32_t  n_moments;
+    const double* moment_time;
+    const double* moment_window;
+
+    /* time-dependent parameters (tdParams.parameters): piecewise (t, value) tables */
+    int32_t  n_params;
+    const int32_t* param_start;        /* [n_params+1] offsets into param_t/param_v */
+    const double*  param_t;
+    const double*  param_v;
+    const uint8_t* param_log_x;        /* logXinterp [0] */
+    const uint8_t* param_log_y;        /* logYinterp [0] */
+} mfg_model_desc;
+
+/*
+ * Result view: caller-owned buffers laid out like GlobalSimuState
+ * (src/Simulation/MolflowSimGeom.h:56-154).  Sizes come from mfg_state_layout().
+ * Moment block 0 is constant flow, blocks 1..n_moments the time moments.
+ * Any pointer may be NULL (that part is skipped).
+ */
+typedef struct mfg_state_layout {
+    int64_t n_facets;
+    int64_t n_moments;             /* blocks per facet = 1 + n_moments */
+    int64_t texture_cells;         /* sum over textured facets of texWidth*texHeight */
+    int64_t profile_facets;        /* facets with a profile */
+    int64_t direction_cells;       /* sum over facets with countDirection of texWidth*texHeight */
+    int64_t anglemap_cells;        /* sum over recording facets of phiWidth*(lowerRes+higherRes) */
+    /* element counts of each view array */
+    int64_t n_global;              /* MFG_G_N */
+    int64_t n_facet_counts;        /* (1+M)*F*MFG_FC_N */
+    int64_t n_facet_sums;          /* (1+M)*F*MFG_FS_N */
+    int64_t n_texture;             /* (1+M)*texture_cells*3  (countEquiv, sum_v_ort_per_area, sum_1_per_ort_velocity) */
+    int64_t n_profile;             /* (1+M)*profile_facets*PROFILE_SIZE*3 (countEquiv, sum_v_ort, sum_1_per_ort_velocity) */
+    int64_t n_direction;           /* (1+M)*direction_cells*4 (dir.x, dir.y, dir.z, count) */
+    int64_t n_anglemap;            /* anglemap_cells */
+} mfg_state_layout;
+
+typedef struct mfg_state_view {
+    double*   global;        /* [n_global] */
+    uint64_t* facet_counts;  /* [n_facet_counts] */
+    double*   facet_sums;    /* [n_facet_sums] */
+    double*   texture;       /* [n_texture] */
+    double*   profile;       /* [n_profile] */
+    double*   direction;     /* [n_direction] */
+    uint64_t* anglemap;      /* [n_anglemap] */
+} mfg_state_view;
+
+/* Run options (precision, RNG, launch shape). */
+#define MFG_PREC_FP64    0   /* plain FP64 traversal, polygon tests and physics */
+#define MFG_PREC_FP32R   1   /* FP32 traversal/tests + FP64 recheck and FP64 new origin */
+
+typedef struct mfg_run_options {
+    int32_t  precision;          /* MFG_PREC_* */
+    uint64_t seed;               /* Philox key; replaces MersenneTwister seeding (MolflowSimulation.cpp:44-55) */
+    int32_t  block_size;         /* threads per block, 0 = autotuned default */
+    int32_t  blocks_per_sm;      /* 0 = occupancy maximum */
+    int32_t  smem_bvh_nodes;     /* BVH nodes staged in shared memory, -1 = auto */
+    double   time_limit_s;       /* kernel self-stops after this wall time (status MFG_ERR_TIMEOUT), 0 = 600 s */
+    uint64_t max_steps_per_particle; /* a particle that exceeds this many bounces is dropped and counted, 0 = 2^40 */
+} mfg_run_options;
+
+/* Run statistics of the last run (filled by mfg_run / mfg_wait). */
+typedef struct mfg_run_stats {
+    uint64_t desorbed;           /* particles started in this run */
+    uint64_t hits;               /* nbMCHit added in this run */
+    uint64_t leaks;
+    uint64_t rechecks;           /* FP32R: rays re-intersected in FP64 */
+    uint64_t dropped;            /* particles dropped at max_steps_per_particle */
+    double   kernel_ms;          /* tracing kernel time, CUDA events on the launch stream */
+    double   total_ms;           /* whole call incl. set-up and flushes */
+    int32_t  status;
+    int32_t  kernel_launches;    /* kernels this library launched for the run */
+} mfg_run_stats;
+
+typedef struct mfg_model mfg_model;
+typedef struct mfg_sim mfg_sim;
+
+/* ---- library ---- */
+uint32_t mfg_abi_version(void);
+/* Last error text of the calling thread (copied into buf, NUL terminated). Returns its length. */
+size_t   mfg_last_error(char* buf, size_t buflen);
+
+/* ---- model: replaces MolflowSimulationModel construction + PrepareToRun +
+ *      BuildAccelStructure (MolflowSimGeom.cpp:124-253) ---- */
+int mfg_model_create(const mfg_model_desc* desc, mfg_model** out);
+void mfg_model_destroy(mfg_model* model);
+int mfg_state_layout_of(const mfg_model* model, mfg_state_layout* out);
+/* Derived per-facet geometry as computed by the library (O,U,V,N,nU,nV as 18 doubles per facet, area) for checks. */
+int mfg_model_facet_geometry(const mfg_model* model, double* out18, double* area);
+/* BVH statistics: node count, depth, leaf count. */
+int mfg_model_bvh_info(const mfg_model* model, int64_t* nodes, int64_t* depth, int64_t* leaves);
+
+/* ---- simulation: replaces MolflowSimulation (MolflowSimulation.h:22-45) and the
+ *      ParticleTracer worker threads (Particle.h:40-129) ---- */
+int mfg_sim_create(const mfg_model* model, int device, mfg_sim** out);
+void mfg_sim_destroy(mfg_sim* sim);
+/* Zero all tallies (GlobalSimuState::Reset, MolflowSimGeom.cpp:527-548).  The particle
+ * counter keeps running, as the reference's random generators do across a reset. */
+int mfg_reset(mfg_sim* sim);
+/* Philox counter of the next particle to desorb (0 after mfg_sim_create).  Ranks or
+ * replicas that split one run use disjoint ranges. */
+int mfg_set_particle_offset(mfg_sim* sim, uint64_t first_particle);
+uint64_t mfg_particle_offset(const mfg_sim* sim);
+/* Desorb and trace n_desorptions particles to absorption or leak; blocking.
+ * Replaces SimulationMCStep(nbStep, threadNum, remainingDes) over all threads
+ * (Particle.cpp:207-396) with the desorption limit as the work unit. */
+int mfg_run(mfg_sim* sim, uint64_t n_desorptions, const mfg_run_options* opt, mfg_run_stats* stats);
+/* Asynchronous form: mfg_run_async returns at once; mfg_wait blocks up to timeout_ms. */
+int mfg_run_async(mfg_sim* sim, uint64_t n_desorptions, const mfg_run_options* opt);
+int mfg_poll(mfg_sim* sim);                      /* MFG_OK when done, MFG_ERR_BUSY while running */
+int mfg_wait(mfg_sim* sim, int64_t timeout_ms, mfg_run_stats* stats);
+int mfg_abort(mfg_sim* sim);                     /* sets the host-mapped abort word read by the kernel */
+/* Copy accumulated tallies into the caller's view (overwrites). Replaces
+ * UpdateMCHits / GlobalSimuState::operator+= (Particle.cpp:21-73, MolflowSimGeom.cpp:452-458). */
+int mfg_fetch(mfg_sim* sim, mfg_state_view* view);
+
+/* Replay mode: intersect caller-given rays (no physics).  For ray i:
+ * origin[3i..], direction[3i..], last_facet[i] (facet to skip, -1 none).
+ * Out: hit_facet[i] (-1 = no hit), hit_t[i] (distance in |direction| units).
+ * Replaces one `Intersect(ray)` call per ray (Particle.cpp:245). Host buffers. */
+int mfg_replay(mfg_sim* sim, int32_t precision, int64_t n_rays,
+               const double* origin, const double* direction, const int32_t* last_facet,
+               int32_t* hit_facet, double* hit_t, uint64_t* n_rechecks);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MFG_H */

@@ -1,0 +1,539 @@
+// api.cu — the extern "C" boundary declared in include/mfg.h.
+//
+// Owns the CUDA side: device copies of a model, tally buffers, the launch of the
+// persistent tracer on a private stream, host-side waits with time limits, and
+// the conversion of fixed-point tallies to the GlobalSimuState field layout.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/mfg.h"
+#include "model_build.h"
+#include "trace_kernels.cuh"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+int cuda_fail(cudaError_t e, const char* what) {
+    g_err = std::string(what) + ": " + cudaGetErrorString(e);
+    return MFG_ERR_CUDA;
+}
+#define CK(call)                                         \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+template <class T>
+int upload(std::vector<void*>& owned, const std::vector<T>& v, const T** out) {
+    if (v.empty()) { *out = nullptr; return MFG_OK; }
+    void* p = nullptr;
+    CK(cudaMalloc(&p, sizeof(T) * v.size()));
+    owned.push_back(p);
+    CK(cudaMemcpy(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+    *out = static_cast<const T*>(p);
+    return MFG_OK;
+}
+
+inline double u128(const unsigned long long* p) {
+    return double(p[1]) * 18446744073709551616.0 + double(p[0]);
+}
+
+}  // namespace
+
+struct mfg_model {
+    mfg::HostModel h;
+};
+
+struct mfg_sim {
+    const mfg_model* model = nullptr;
+    int device = 0;
+    int sm_count = 0;
+    std::vector<void*> owned;
+    DevModel dm{};
+    DevTally dt{};
+    unsigned long long* d_counter = nullptr;
+    int* h_abort = nullptr;      // host-mapped
+    int* d_abort = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    size_t n_global = TG_N, n_facet = 0, n_texture = 0, n_profile = 0, n_anglemap = 0;
+    uint64_t particles_started = 0;
+    bool running = false;
+    mfg_run_stats pending{};
+    std::vector<unsigned long long> g_before;
+    std::chrono::steady_clock::time_point t_start;
+    std::mutex mu;
+    int launches = 0;
+};
+
+extern "C" {
+
+uint32_t mfg_abi_version(void) { return MFG_ABI_VERSION; }
+
+size_t mfg_last_error(char* buf, size_t buflen) {
+    if (buf && buflen) {
+        size_t n = std::min(buflen - 1, g_err.size());
+        std::memcpy(buf, g_err.data(), n);
+        buf[n] = 0;
+    }
+    return g_err.size();
+}
+
+int mfg_model_create(const mfg_model_desc* desc, mfg_model** out) {
+    if (!out) return fail(MFG_ERR_INVALID_ARGUMENT, "out is null");
+    *out = nullptr;
+    auto* m = new mfg_model();
+    std::string err;
+    int rc = mfg::build_host_model(desc, m->h, err);
+    if (rc != MFG_OK) {
+        delete m;
+        return fail(rc, err);
+    }
+    if (m->h.bvh_depth >= mfgk::kStack - 2) {
+        delete m;
+        return fail(MFG_ERR_LIMIT, "BVH deeper than the traversal stack");
+    }
+    *out = m;
+    return MFG_OK;
+}
+
+void mfg_model_destroy(mfg_model* model) { delete model; }
+
+int mfg_state_layout_of(const mfg_model* model, mfg_state_layout* out) {
+    if (!model || !out) return fail(MFG_ERR_INVALID_ARGUMENT, "null argument");
+    *out = model->h.layout;
+    return MFG_OK;
+}
+
+int mfg_model_facet_geometry(const mfg_model* model, double* out18, double* area) {
+    if (!model) return fail(MFG_ERR_INVALID_ARGUMENT, "null model");
+    for (int i = 0; i < model->h.nf; ++i) {
+        const auto& F = model->h.facets[i];
+        if (out18) {
+            double* o = out18 + 18 * size_t(i);
+            for (int a = 0; a < 3; ++a) {
+                o[a] = F.O[a]; o[3 + a] = F.U[a]; o[6 + a] = F.V[a];
+                o[9 + a] = F.N[a]; o[12 + a] = F.nU[a]; o[15 + a] = F.nV[a];
+            }
+        }
+        if (area) area[i] = F.area;
+    }
+    return MFG_OK;
+}
+
+int mfg_model_bvh_info(const mfg_model* model, int64_t* nodes, int64_t* depth, int64_t* leaves) {
+    if (!model) return fail(MFG_ERR_INVALID_ARGUMENT, "null model");
+    if (nodes) *nodes = int64_t(model->h.nodes_d.size());
+    if (depth) *depth = model->h.bvh_depth;
+    if (leaves) *leaves = model->h.bvh_leaves;
+    return MFG_OK;
+}
+
+static int sim_upload(mfg_sim* s) {
+    const mfg::HostModel& h = s->model->h;
+    DevModel& M = s->dm;
+    std::memset(&M, 0, sizeof M);
+    M.nf = h.nf;
+    M.nstruct = h.nstruct;
+    M.n_src = int32_t(h.src_facet.size());
+    M.nm = h.nm;
+    int rc;
+#define UP(vec, field) if ((rc = upload(s->owned, vec, &M.field)) != MFG_OK) return rc
+    UP(h.nodes_d, nodes_d);
+    UP(h.nodes_f, nodes_f);
+    UP(h.roots, roots);
+    UP(h.prims, prims);
+    UP(h.isect_d, isect_d);
+    UP(h.isect_f, isect_f);
+    UP(h.poly_d, poly_d);
+    UP(h.poly_f, poly_f);
+    UP(h.v2_d, v2_d);
+    UP(h.v2_f, v2_f);
+    UP(h.phys_d, phys_d);
+    UP(h.phys_f, phys_f);
+    UP(h.info, info);
+    UP(h.info2, info2);
+    UP(h.centers, center);
+    UP(h.src_cdf, src_cdf);
+    UP(h.src_facet, src_facet);
+    UP(h.src_id, src_id);
+    UP(h.mstart, mstart);
+    UP(h.mend, mend);
+    UP(h.id_start, id_start);
+    UP(h.id_t, id_t);
+    UP(h.id_cum, id_cum);
+    UP(h.par_start, par_start);
+    UP(h.par_t, par_t);
+    UP(h.par_v, par_v);
+    UP(h.par_logx, par_logx);
+    UP(h.par_logy, par_logy);
+#undef UP
+    M.src_total = h.src_total;
+    M.latest = h.latest;
+    M.maxwin = h.maxwin;
+    for (int i = 0; i < MFG_MAXWELL_N; ++i) { M.cdf_v[i] = h.cdf_v[i]; M.cdf_p[i] = h.cdf_p[i]; }
+    M.gas_mass = h.gas_mass;
+    M.ort_factor = h.use_maxwell ? 1.0 : 1.1781;
+    M.half_life = h.half_life;
+    M.use_maxwell = h.use_maxwell;
+    M.constant_flow = h.constant_flow;
+    M.enable_decay = h.enable_decay;
+    M.texture_cells = h.layout.texture_cells;
+    M.profile_facets = h.layout.profile_facets;
+    M.anglemap_cells = h.layout.anglemap_cells;
+    M.scene_scale = h.scene_scale;
+    // tallies
+    const size_t B = 1 + size_t(h.nm);
+    s->n_facet = B * size_t(h.nf) * TF_N;
+    s->n_texture = B * size_t(h.layout.texture_cells) * TT_N;
+    s->n_profile = B * size_t(h.layout.profile_facets) * MFG_PROFILE_SIZE * TT_N;
+    s->n_anglemap = size_t(h.layout.anglemap_cells);
+    auto alloc = [&](unsigned long long** p, size_t n) -> int {
+        *p = nullptr;
+        if (!n) return MFG_OK;
+        void* q = nullptr;
+        CK(cudaMalloc(&q, n * sizeof(unsigned long long)));
+        s->owned.push_back(q);
+        *p = static_cast<unsigned long long*>(q);
+        return MFG_OK;
+    };
+    if ((rc = alloc(&s->dt.global, TG_N))) return rc;
+    if ((rc = alloc(&s->dt.facet, s->n_facet))) return rc;
+    if ((rc = alloc(&s->dt.texture, s->n_texture))) return rc;
+    if ((rc = alloc(&s->dt.profile, s->n_profile))) return rc;
+    if ((rc = alloc(&s->dt.anglemap, s->n_anglemap))) return rc;
+    if ((rc = alloc(&s->d_counter, 1))) return rc;
+    return MFG_OK;
+}
+
+int mfg_reset(mfg_sim* s) {
+    if (!s) return fail(MFG_ERR_INVALID_ARGUMENT, "null sim");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
+    CK(cudaSetDevice(s->device));
+    CK(cudaMemsetAsync(s->dt.global, 0, TG_N * 8, s->stream));
+    if (s->n_facet) CK(cudaMemsetAsync(s->dt.facet, 0, s->n_facet * 8, s->stream));
+    if (s->n_texture) CK(cudaMemsetAsync(s->dt.texture, 0, s->n_texture * 8, s->stream));
+    if (s->n_profile) CK(cudaMemsetAsync(s->dt.profile, 0, s->n_profile * 8, s->stream));
+    if (s->n_anglemap) CK(cudaMemsetAsync(s->dt.anglemap, 0, s->n_anglemap * 8, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return MFG_OK;
+}
+
+int mfg_set_particle_offset(mfg_sim* s, uint64_t first_particle) {
+    if (!s) return fail(MFG_ERR_INVALID_ARGUMENT, "null sim");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
+    s->particles_started = first_particle;
+    return MFG_OK;
+}
+
+uint64_t mfg_particle_offset(const mfg_sim* s) { return s ? s->particles_started : 0; }
+
+int mfg_sim_create(const mfg_model* model, int device, mfg_sim** out) {
+    if (!model || !out) return fail(MFG_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) return fail(MFG_ERR_NO_DEVICE, "no CUDA device available");
+    if (device < 0 || device >= ndev) return fail(MFG_ERR_NO_DEVICE, "device index out of range");
+    auto* s = new mfg_sim();
+    s->model = model;
+    s->device = device;
+    auto bail = [&](int rc) {
+        mfg_sim_destroy(s);
+        return rc;
+    };
+    if ((e = cudaSetDevice(device)) != cudaSuccess) return bail(cuda_fail(e, "cudaSetDevice"));
+    cudaDeviceProp prop;
+    if ((e = cudaGetDeviceProperties(&prop, device)) != cudaSuccess) return bail(cuda_fail(e, "cudaGetDeviceProperties"));
+    s->sm_count = prop.multiProcessorCount;
+    if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(cuda_fail(e, "stream"));
+    if ((e = cudaEventCreate(&s->ev0)) != cudaSuccess) return bail(cuda_fail(e, "event"));
+    if ((e = cudaEventCreate(&s->ev1)) != cudaSuccess) return bail(cuda_fail(e, "event"));
+    if ((e = cudaHostAlloc(&s->h_abort, sizeof(int), cudaHostAllocMapped)) != cudaSuccess) return bail(cuda_fail(e, "cudaHostAlloc"));
+    *s->h_abort = 0;
+    if ((e = cudaHostGetDevicePointer(&s->d_abort, s->h_abort, 0)) != cudaSuccess) return bail(cuda_fail(e, "mapped pointer"));
+    int rc = sim_upload(s);
+    if (rc != MFG_OK) return bail(rc);
+    rc = mfg_reset(s);
+    if (rc != MFG_OK) return bail(rc);
+    *out = s;
+    return MFG_OK;
+}
+
+void mfg_sim_destroy(mfg_sim* s) {
+    if (!s) return;
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (void* p : s->owned) cudaFree(p);
+    if (s->h_abort) cudaFreeHost(s->h_abort);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+static int read_global(mfg_sim* s, std::vector<unsigned long long>& g) {
+    g.assign(TG_N, 0);
+    CK(cudaMemcpyAsync(g.data(), s->dt.global, TG_N * 8, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return MFG_OK;
+}
+
+int mfg_run_async(mfg_sim* s, uint64_t n, const mfg_run_options* opt) {
+    if (!s) return fail(MFG_ERR_INVALID_ARGUMENT, "null sim");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
+    const mfg::HostModel& h = s->model->h;
+    if (!h.gpu_supported) return fail(MFG_ERR_UNSUPPORTED_FEATURE, "not traced on the GPU: " + h.gpu_unsupported_reason);
+    if (h.src_facet.empty()) return fail(MFG_ERR_NO_SOURCE, "no desorbing facet (total outgassing is zero)");
+    mfg_run_options o{};
+    if (opt) o = *opt;
+    if (o.precision != MFG_PREC_FP64 && o.precision != MFG_PREC_FP32R) return fail(MFG_ERR_INVALID_ARGUMENT, "unknown precision");
+    CK(cudaSetDevice(s->device));
+    int rc = read_global(s, s->g_before);
+    if (rc) return rc;
+    *s->h_abort = 0;
+    CK(cudaMemsetAsync(s->d_counter, 0, 8, s->stream));
+    LaunchCtl C{};
+    C.next_particle = s->d_counter;
+    C.first_particle = s->particles_started;
+    C.n_particles = n;
+    C.max_steps = o.max_steps_per_particle ? o.max_steps_per_particle : (1ull << 40);
+    double lim = o.time_limit_s > 0 ? o.time_limit_s : 600.0;
+    C.time_limit_ns = (unsigned long long)(lim * 1e9);
+    C.key0 = uint32_t(o.seed);
+    C.key1 = uint32_t(o.seed >> 32);
+    C.abort_flag = s->d_abort;
+    size_t fac_bytes = size_t(h.nf) * SF_N * 8;
+    C.smem_facets = fac_bytes <= 64 * 1024 ? 1 : 0;
+    size_t dyn = (TG_N + (C.smem_facets ? size_t(h.nf) * SF_N : 0)) * 8;
+    int block = o.block_size > 0 ? o.block_size : 256;
+    if (block % 32 || block > 256) return fail(MFG_ERR_INVALID_ARGUMENT, "block_size must be a multiple of 32, at most 256");
+    const void* fn = o.precision == MFG_PREC_FP32R ? (const void*)mfgk::trace_kernel<true> : (const void*)mfgk::trace_kernel<false>;
+    CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn)));
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, dyn));
+    if (per_sm < 1) return fail(MFG_ERR_LIMIT, "kernel does not fit on an SM with this block size");
+    if (o.blocks_per_sm > 0) per_sm = std::min(per_sm, int(o.blocks_per_sm));
+    long long grid = (long long)per_sm * s->sm_count;
+    long long need = (long long)((n + block - 1) / block);
+    grid = std::max(1LL, std::min(grid, need));
+    s->t_start = std::chrono::steady_clock::now();
+    CK(cudaEventRecord(s->ev0, s->stream));
+    if (o.precision == MFG_PREC_FP32R)
+        mfgk::trace_kernel<true><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
+    else
+        mfgk::trace_kernel<false><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(s->ev1, s->stream));
+    s->launches = 1;
+    s->running = true;
+    s->pending = mfg_run_stats{};
+    s->pending.desorbed = n;
+    s->particles_started += n;
+    return MFG_OK;
+}
+
+int mfg_poll(mfg_sim* s) {
+    if (!s) return fail(MFG_ERR_INVALID_ARGUMENT, "null sim");
+    if (!s->running) return MFG_OK;
+    cudaError_t e = cudaEventQuery(s->ev1);
+    if (e == cudaErrorNotReady) return MFG_ERR_BUSY;
+    if (e != cudaSuccess) return cuda_fail(e, "kernel");
+    return MFG_OK;
+}
+
+int mfg_wait(mfg_sim* s, int64_t timeout_ms, mfg_run_stats* stats) {
+    if (!s) return fail(MFG_ERR_INVALID_ARGUMENT, "null sim");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (!s->running) {
+        if (stats) *stats = s->pending;
+        return s->pending.status;
+    }
+    CK(cudaSetDevice(s->device));
+    auto t0 = std::chrono::steady_clock::now();
+    while (true) {
+        cudaError_t e = cudaEventQuery(s->ev1);
+        if (e == cudaSuccess) break;
+        if (e != cudaErrorNotReady) { s->running = false; return cuda_fail(e, "tracer kernel"); }
+        if (timeout_ms >= 0 &&
+            std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count() > timeout_ms)
+            return fail(MFG_ERR_TIMEOUT, "run still in flight after the wait limit");
+        std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
+    s->running = false;
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    std::vector<unsigned long long> g;
+    int rc = read_global(s, g);
+    if (rc) return rc;
+    mfg_run_stats& st = s->pending;
+    st.hits = g[TG_HITS] - s->g_before[TG_HITS];
+    st.leaks = g[TG_LEAK] - s->g_before[TG_LEAK];
+    st.rechecks = g[TG_RECHECK] - s->g_before[TG_RECHECK];
+    st.dropped = g[TG_DROPPED] - s->g_before[TG_DROPPED];
+    st.kernel_ms = ms;
+    st.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - s->t_start).count();
+    st.kernel_launches = s->launches;
+    unsigned long long status = g[TG_STATUS];
+    st.status = MFG_OK;
+    if (status & KS_STACK) st.status = MFG_ERR_LIMIT;
+    if (status & KS_TIMEOUT) st.status = MFG_ERR_TIMEOUT;
+    if (status & KS_ABORTED) st.status = MFG_ERR_ABORTED;
+    if (status) {
+        unsigned long long zero = 0;
+        CK(cudaMemcpyAsync(s->dt.global + TG_STATUS, &zero, 8, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        g_err = st.status == MFG_ERR_TIMEOUT ? "kernel time limit reached; particles in flight were dropped"
+              : st.status == MFG_ERR_ABORTED ? "run aborted" : "BVH traversal stack overflow";
+    }
+    if (stats) *stats = st;
+    return st.status;
+}
+
+int mfg_run(mfg_sim* s, uint64_t n, const mfg_run_options* opt, mfg_run_stats* stats) {
+    int rc = mfg_run_async(s, n, opt);
+    if (rc != MFG_OK) return rc;
+    return mfg_wait(s, -1, stats);
+}
+
+int mfg_abort(mfg_sim* s) {
+    if (!s) return fail(MFG_ERR_INVALID_ARGUMENT, "null sim");
+    *(volatile int*)s->h_abort = 1;
+    return MFG_OK;
+}
+
+int mfg_fetch(mfg_sim* s, mfg_state_view* v) {
+    if (!s || !v) return fail(MFG_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
+    CK(cudaSetDevice(s->device));
+    const mfg::HostModel& h = s->model->h;
+    const double f = h.use_maxwell ? 1.0 : 1.1781;
+    std::vector<unsigned long long> g, fa, tx, pr, am;
+    g.resize(TG_N);
+    fa.resize(s->n_facet);
+    tx.resize(s->n_texture);
+    pr.resize(s->n_profile);
+    am.resize(s->n_anglemap);
+    CK(cudaMemcpyAsync(g.data(), s->dt.global, TG_N * 8, cudaMemcpyDeviceToHost, s->stream));
+    if (s->n_facet) CK(cudaMemcpyAsync(fa.data(), s->dt.facet, s->n_facet * 8, cudaMemcpyDeviceToHost, s->stream));
+    if (s->n_texture && v->texture) CK(cudaMemcpyAsync(tx.data(), s->dt.texture, s->n_texture * 8, cudaMemcpyDeviceToHost, s->stream));
+    if (s->n_profile && v->profile) CK(cudaMemcpyAsync(pr.data(), s->dt.profile, s->n_profile * 8, cudaMemcpyDeviceToHost, s->stream));
+    if (s->n_anglemap && v->anglemap) CK(cudaMemcpyAsync(am.data(), s->dt.anglemap, s->n_anglemap * 8, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if (v->global) {
+        std::fill(v->global, v->global + MFG_G_N, 0.0);
+        v->global[MFG_G_NBMCHIT] = double(g[TG_HITS]);
+        v->global[MFG_G_NBHITEQUIV] = double(g[TG_HITS]);
+        v->global[MFG_G_NBDESORBED] = double(g[TG_DES]);
+        v->global[MFG_G_NBABSEQUIV] = double(g[TG_ABS]);
+        v->global[MFG_G_NBLEAK] = double(g[TG_LEAK]);
+        v->global[MFG_G_DIST_TOTAL] = u128(&g[TG_DIST_LO]) / MFG_SCALE_DIST;
+        v->global[MFG_G_DIST_FULLHITS] = u128(&g[TG_DISTF_LO]) / MFG_SCALE_DIST;
+    }
+    const size_t B = 1 + size_t(h.nm);
+    for (size_t m = 0; m < B; ++m)
+        for (int i = 0; i < h.nf; ++i) {
+            const unsigned long long* t = &fa[(m * h.nf + i) * TF_N];
+            size_t k = m * h.nf + i;
+            if (v->facet_counts) {
+                v->facet_counts[k * MFG_FC_N + MFG_FC_NBMCHIT] = t[TF_HITS];
+                v->facet_counts[k * MFG_FC_N + MFG_FC_NBDESORBED] = t[TF_DES];
+                v->facet_counts[k * MFG_FC_N + MFG_FC_NBABSORBED] = t[TF_ABS];
+            }
+            if (v->facet_sums) {
+                double* o = v->facet_sums + k * MFG_FS_N;
+                o[MFG_FS_NBHITEQUIV] = double(t[TF_HITS]);
+                o[MFG_FS_NBABSEQUIV] = double(t[TF_ABS]);
+                o[MFG_FS_SUM_1_PER_ORT_VEL] = u128(t + TF_S1OV) / MFG_SCALE_INV;
+                o[MFG_FS_SUM_V_ORT] = u128(t + TF_SVORT) / MFG_SCALE_V * f;
+                o[MFG_FS_SUM_1_PER_VELOCITY] = u128(t + TF_S1V) / MFG_SCALE_INV;
+            }
+        }
+    if (v->texture) {
+        const size_t C = size_t(h.layout.texture_cells);
+        for (size_t m = 0; m < B; ++m)
+            for (size_t c = 0; c < C; ++c) {
+                const unsigned long long* t = &tx[(m * C + c) * TT_N];
+                double* o = v->texture + (m * C + c) * 3;
+                o[0] = double(t[TT_COUNT]);
+                o[1] = u128(t + TT_SVORT) / MFG_SCALE_V * f * h.tex_inc[c];
+                o[2] = u128(t + TT_S1OV) / MFG_SCALE_INV / f;
+            }
+    }
+    if (v->profile) {
+        const size_t P = size_t(h.layout.profile_facets) * MFG_PROFILE_SIZE;
+        for (size_t m = 0; m < B; ++m)
+            for (size_t c = 0; c < P; ++c) {
+                const unsigned long long* t = &pr[(m * P + c) * TT_N];
+                double* o = v->profile + (m * P + c) * 3;
+                o[0] = double(t[TT_COUNT]);
+                o[1] = u128(t + TT_SVORT) / MFG_SCALE_V * f;
+                o[2] = u128(t + TT_S1OV) / MFG_SCALE_INV;
+            }
+    }
+    if (v->anglemap)
+        for (size_t c = 0; c < s->n_anglemap; ++c) v->anglemap[c] = am[c];
+    if (v->direction) std::fill(v->direction, v->direction + h.layout.n_direction, 0.0);
+    return MFG_OK;
+}
+
+int mfg_replay(mfg_sim* s, int32_t precision, int64_t n, const double* origin, const double* direction,
+               const int32_t* last_facet, int32_t* hit_facet, double* hit_t, uint64_t* n_rechecks) {
+    if (!s || n < 0 || (n > 0 && (!origin || !direction || !last_facet || !hit_facet || !hit_t)))
+        return fail(MFG_ERR_INVALID_ARGUMENT, "null argument");
+    if (n == 0) { if (n_rechecks) *n_rechecks = 0; return MFG_OK; }
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
+    CK(cudaSetDevice(s->device));
+    double *d_o = nullptr, *d_d = nullptr, *d_t = nullptr;
+    int *d_l = nullptr, *d_f = nullptr;
+    unsigned long long* d_r = nullptr;
+    auto cleanup = [&]() { cudaFree(d_o); cudaFree(d_d); cudaFree(d_t); cudaFree(d_l); cudaFree(d_f); cudaFree(d_r); };
+    cudaError_t e = cudaSuccess;
+    if ((e = cudaMalloc(&d_o, 24 * n)) || (e = cudaMalloc(&d_d, 24 * n)) || (e = cudaMalloc(&d_t, 8 * n)) ||
+        (e = cudaMalloc(&d_l, 4 * n)) || (e = cudaMalloc(&d_f, 4 * n)) || (e = cudaMalloc(&d_r, 16))) {
+        cleanup();
+        return cuda_fail(e, "cudaMalloc (replay)");
+    }
+    cudaMemcpyAsync(d_o, origin, 24 * n, cudaMemcpyHostToDevice, s->stream);
+    cudaMemcpyAsync(d_d, direction, 24 * n, cudaMemcpyHostToDevice, s->stream);
+    cudaMemcpyAsync(d_l, last_facet, 4 * n, cudaMemcpyHostToDevice, s->stream);
+    cudaMemsetAsync(d_r, 0, 16, s->stream);
+    int block = 128;
+    long long grid = (n + block - 1) / block;
+    mfgk::replay_kernel<<<unsigned(grid), block, 0, s->stream>>>(s->dm, precision, n, d_o, d_d, d_l, d_f, d_t, d_r,
+                                                                d_r + 1);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) {
+        unsigned long long r[2] = {0, 0};
+        cudaMemcpyAsync(hit_facet, d_f, 4 * n, cudaMemcpyDeviceToHost, s->stream);
+        cudaMemcpyAsync(hit_t, d_t, 8 * n, cudaMemcpyDeviceToHost, s->stream);
+        cudaMemcpyAsync(r, d_r, 16, cudaMemcpyDeviceToHost, s->stream);
+        e = cudaStreamSynchronize(s->stream);
+        if (n_rechecks) *n_rechecks = r[0];
+        if (e == cudaSuccess && (r[1] & KS_STACK)) { cleanup(); return fail(MFG_ERR_LIMIT, "BVH traversal stack overflow"); }
+    }
+    cleanup();
+    if (e != cudaSuccess) return cuda_fail(e, "replay kernel");
+    return MFG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,195 @@
+// device_model.h — data layout of a model in GPU memory, shared by host and kernels.
+//
+// One model = facets (planar polygons), a BVH per structure and the tables the
+// tracer samples from.  Records are AoS and 16-byte aligned so a thread fetches
+// one facet with a few vector loads; the FP32 copies are half the size for the
+// FP32 traversal.
+#pragma once
+#include <stdint.h>
+
+#define MFG_MAX_TRANSPARENT 0   // transparent passes are not traced on the GPU yet
+#define MFG_MAXWELL_N 100
+
+// BVH nodes are stored breadth-first, so the two children of an internal node
+// are adjacent.  Internal node: a = index of the left child (right = a+1),
+// b = split axis (0..2).  Leaf: a = first index into the prim list, b = -1 - count.
+// FP64 bounds (64 B):
+struct __align__(16) NodeD {
+    double lo[3];
+    double hi[3];
+    int32_t a, b;
+    int32_t pad0, pad1;
+};
+// FP32 bounds rounded outward and padded by a scene-relative margin (32 B).
+struct __align__(16) NodeF {
+    float lo[3];
+    float hi[3];
+    int32_t a, b;
+};
+
+// Facet intersection record FP64 (128 B):
+//  [0..2] N, [3] D = N.O, [4..6] O, [7] pad, [8..10] U/|U|^2, [11] pad, [12..14] V/|V|^2, [15] pad
+struct __align__(16) FacetIsectD { double v[16]; };
+// FP32 copy (64 B), same order
+struct __align__(16) FacetIsectF { float v[16]; };
+
+// Polygon record: circle shortcut + vertex range (64 B / 32 B).
+//  cu, cv: centre in normalised (u,v); su = |U|, sv = |V|; rin2/rout2: squared radii (cm^2)
+//  of a disk certainly inside / a disk containing the polygon; vstart, nv.
+struct __align__(16) PolyD { double cu, cv, su, sv, rin2, rout2; int32_t vstart, nv; };
+struct __align__(16) PolyF { float cu, cv, su, sv, rin2, rout2; int32_t vstart, nv; };
+
+// Facet flags
+#define FF_TWO_SIDED   1u
+#define FF_TEXTURED    2u
+#define FF_STICK_PARAM 4u
+#define FF_TEMP_PARAM  8u
+#define FF_SOJOURN     16u
+#define FF_ANGLEMAP    32u
+#define FF_PROFILE     64u
+#define FF_DIFFUSE_ONLY 128u
+
+// Per-facet physics record (FP64, 128 B).
+struct __align__(16) FacetPhysD {
+    double nU[3], nV[3];
+    double sticking, sqrtT, accommodation, diffuse, specular, cos_exp;
+    double texw_p, texh_p;
+    double soj_freq, soj_e;
+};
+struct __align__(16) FacetPhysF {
+    float nU[3], nV[3];
+    float N[3];
+    float sticking, sqrtT, accommodation, diffuse, specular, cos_exp;
+    float texw_p, texh_p;
+    float pad;
+};
+// Per-facet integer info (32 B).
+struct __align__(16) FacetInfo {
+    uint32_t flags, count;      // FF_*, MFG_COUNT_*
+    int32_t tex_off, tex_w;     // texture cell offset in one moment block, width in cells
+    int32_t tex_h, prof_idx;
+    int32_t ang_off, profile_type;
+};
+struct __align__(16) FacetInfo2 {
+    int32_t structure, desorb_type, stick_param, temp_param;
+    int32_t am_phi, am_lo, am_hi, pad;
+    double am_limit, max_speed, desorb_exp, temperature;
+};
+
+// Device-resident tallies.  Fixed-point scales: velocities (m/s) * 2^20,
+// inverse velocities (s/m) * 2^32, distances (cm) * 2^20.
+#define MFG_SCALE_V    1048576.0              /* 2^20 */
+#define MFG_SCALE_INV  4294967296.0           /* 2^32 */
+#define MFG_SCALE_DIST 1048576.0              /* 2^20 */
+#define MFG_Q_MAX      1125899906842624.0     /* 2^50: per-sample clamp */
+#define MFG_SMEM_FLUSH (1ull << 60)           /* shared partial sums move to global above this */
+
+// global (u64 pairs = 128-bit fixed point where noted)
+#define TG_HITS 0
+#define TG_DES 1
+#define TG_ABS 2
+#define TG_LEAK 3
+#define TG_DIST_LO 4   // 128-bit: distTraveled_total
+#define TG_DIST_HI 5
+#define TG_DISTF_LO 6  // 128-bit: distTraveledTotal_fullHitsOnly
+#define TG_DISTF_HI 7
+#define TG_DROPPED 8
+#define TG_RECHECK 9
+#define TG_STATUS 10
+#define TG_N 16
+// per facet per moment block (u64): counts then 128-bit sums
+#define TF_HITS 0
+#define TF_DES 1
+#define TF_ABS 2
+#define TF_S1OV 3   // lo, hi
+#define TF_SVORT 5  // lo, hi
+#define TF_S1V 7    // lo, hi
+#define TF_N 9
+// per texture cell / profile bin per moment block (u64)
+#define TT_COUNT 0
+#define TT_S1OV 1   // lo, hi
+#define TT_SVORT 3  // lo, hi
+#define TT_N 5
+// shared-memory partial layouts (u64)
+#define SF_HITS 0
+#define SF_DES 1
+#define SF_ABS 2
+#define SF_S1OV 3
+#define SF_SVORT 4
+#define SF_S1V 5
+#define SF_N 6
+#define ST_N 3
+
+// kernel status bits (TG_STATUS)
+#define KS_TIMEOUT 1ull
+#define KS_ABORTED 2ull
+#define KS_NO_SOURCE 4ull
+#define KS_STACK 8ull
+
+struct DevModel {
+    int32_t nf, nstruct;
+    int32_t n_src, nm;
+    const NodeD* nodes_d;
+    const NodeF* nodes_f;
+    const int32_t* roots;        // root node per structure
+    const int32_t* prims;        // facet ids in leaf order
+    const FacetIsectD* isect_d;
+    const FacetIsectF* isect_f;
+    const PolyD* poly_d;
+    const PolyF* poly_f;
+    const double2* v2_d;
+    const float2* v2_f;
+    const FacetPhysD* phys_d;
+    const FacetPhysF* phys_f;
+    const FacetInfo* info;
+    const FacetInfo2* info2;
+    const double* center;        // 3 per facet (start point fallback)
+    const double* src_cdf;       // prefix sums of source weights
+    const int32_t* src_facet;
+    const int32_t* src_id;       // integrated-desorption table index per source (-1 none)
+    double src_total;
+    double latest;               // latestMoment
+    const double* mstart;        // moment window starts (sorted)
+    const double* mend;
+    double maxwin;
+    // integrated desorption tables (concatenated)
+    const int32_t* id_start;
+    const double* id_t;
+    const double* id_cum;
+    // time-dependent parameters (concatenated)
+    const int32_t* par_start;
+    const double* par_t;
+    const double* par_v;
+    const uint8_t* par_logx;
+    const uint8_t* par_logy;
+    double cdf_v[MFG_MAXWELL_N];
+    double cdf_p[MFG_MAXWELL_N];
+    double gas_mass;
+    double ort_factor;           // 1.0 with Maxwell speeds, 1.1781 without (Particle.cpp:673)
+    double half_life;
+    int32_t use_maxwell, constant_flow, enable_decay, pad0;
+    int64_t texture_cells;       // per moment block
+    int64_t profile_facets;
+    int64_t anglemap_cells;
+    double scene_scale;          // max |coordinate| of the scene (for FP32 tolerances)
+};
+
+struct DevTally {
+    unsigned long long* global;      // TG_N
+    unsigned long long* facet;       // (1+M) * nf * TF_N
+    unsigned long long* texture;     // (1+M) * texture_cells * TT_N
+    unsigned long long* profile;     // (1+M) * profile_facets * 100 * TT_N
+    unsigned long long* anglemap;    // anglemap_cells
+};
+
+struct LaunchCtl {
+    unsigned long long* next_particle;   // work counter (particles handed out)
+    unsigned long long first_particle;   // Philox counter of particle 0 of this run
+    unsigned long long n_particles;
+    unsigned long long max_steps;
+    unsigned long long time_limit_ns;    // a warp stops this long after it started
+    uint32_t key0, key1;
+    const volatile int* abort_flag;      // host-mapped
+    int smem_textures;                   // 1: moment-0 texture partials in shared memory
+    int smem_facets;                     // 1: moment-0 facet partials in shared memory
+};

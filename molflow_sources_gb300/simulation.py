@@ -1,0 +1,250 @@
+"""Host-side mirror of the reference simulation interface over the C ABI (libmfg.so).
+
+`GpuSimulation` stands where `MolflowSimulation` (src/Simulation/MolflowSimulation.h:22-45)
+and its `MFSim::ParticleTracer` worker threads (src/Simulation/Particle.h:40-129)
+stand in molflowCLI: the model goes in once, `SimulationMCStep` advances the
+simulation by a number of desorptions, and `UpdateHitsAndLog` adds the tallies
+into a `GlobalSimuState`-shaped `SimuState` (src/Simulation/Particle.cpp:21-73,
+1294-1312).  All work runs in the CUDA library; this module never computes
+tallies itself and raises when the library is missing.
+"""
+import ctypes as C
+import enum
+import os
+import threading
+
+import numpy as np
+
+from . import _abi as A
+from .model import Model, SimuState
+
+_LIB = None
+_LIB_LOCK = threading.Lock()
+
+
+class MfgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (A.STATUS_NAMES.get(code, code), msg))
+        self.code = code
+
+
+class MCStepResult(enum.IntEnum):
+    """MFSim::MCStepResult (src/Simulation/Particle.h:24-28)."""
+    Success = 0
+    DesorptionError = 1
+    MaxReached = 2
+
+
+def library_path():
+    from .build import LIB
+    return LIB
+
+
+def load_library(build_if_missing=True):
+    """Load libmfg.so (building it when sources are newer).  Raises if unavailable."""
+    global _LIB
+    with _LIB_LOCK:
+        if _LIB is not None:
+            return _LIB
+        from . import build as B
+        if build_if_missing:
+            B.build()
+        if not os.path.exists(B.LIB):
+            raise MfgError(A.MFG_ERR_NO_DEVICE, "libmfg.so is not built (run molflow_sources_gb300.build.build())")
+        L = C.CDLL(B.LIB)
+        vp = C.c_void_p
+        L.mfg_abi_version.restype = C.c_uint32
+        L.mfg_last_error.argtypes = [C.c_char_p, C.c_size_t]
+        L.mfg_last_error.restype = C.c_size_t
+        L.mfg_model_create.argtypes = [C.POINTER(A.ModelDesc), C.POINTER(vp)]
+        L.mfg_model_destroy.argtypes = [vp]
+        L.mfg_model_destroy.restype = None
+        L.mfg_state_layout_of.argtypes = [vp, C.POINTER(A.StateLayout)]
+        L.mfg_model_facet_geometry.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.mfg_model_bvh_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        L.mfg_sim_create.argtypes = [vp, C.c_int, C.POINTER(vp)]
+        L.mfg_sim_destroy.argtypes = [vp]
+        L.mfg_sim_destroy.restype = None
+        L.mfg_reset.argtypes = [vp]
+        L.mfg_set_particle_offset.argtypes = [vp, C.c_uint64]
+        L.mfg_particle_offset.argtypes = [vp]
+        L.mfg_particle_offset.restype = C.c_uint64
+        L.mfg_run.argtypes = [vp, C.c_uint64, C.POINTER(A.RunOptions), C.POINTER(A.RunStats)]
+        L.mfg_run_async.argtypes = [vp, C.c_uint64, C.POINTER(A.RunOptions)]
+        L.mfg_poll.argtypes = [vp]
+        L.mfg_wait.argtypes = [vp, C.c_int64, C.POINTER(A.RunStats)]
+        L.mfg_abort.argtypes = [vp]
+        L.mfg_fetch.argtypes = [vp, C.POINTER(A.StateView)]
+        L.mfg_replay.argtypes = [vp, C.c_int32, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                 C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_double),
+                                 C.POINTER(C.c_uint64)]
+        if L.mfg_abi_version() != A.MFG_ABI_VERSION:
+            raise MfgError(A.MFG_ERR_INVALID_MODEL, "libmfg ABI version mismatch")
+        _LIB = L
+        return L
+
+
+def last_error():
+    L = load_library()
+    buf = C.create_string_buffer(1024)
+    L.mfg_last_error(buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def _check(rc):
+    if rc != A.MFG_OK:
+        raise MfgError(rc, last_error())
+    return rc
+
+
+class GpuModel:
+    """Device-independent prepared model (facet basis, BVH, tables) — mfg_model."""
+
+    def __init__(self, model: Model):
+        self.model = model
+        L = load_library()
+        self._desc = model.desc()
+        h = C.c_void_p()
+        _check(L.mfg_model_create(C.byref(self._desc), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            load_library().mfg_model_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def layout(self):
+        Lo = A.StateLayout()
+        _check(load_library().mfg_state_layout_of(self.h, C.byref(Lo)))
+        return {f: getattr(Lo, f) for f, _ in A.StateLayout._fields_}
+
+    def facet_geometry(self):
+        o = np.zeros((self.model.n_facets, 18))
+        area = np.zeros(self.model.n_facets)
+        _check(load_library().mfg_model_facet_geometry(self.h, A.ptr(o, C.c_double), A.ptr(area, C.c_double)))
+        return o, area
+
+    def bvh_info(self):
+        n, d, l = C.c_int64(), C.c_int64(), C.c_int64()
+        _check(load_library().mfg_model_bvh_info(self.h, C.byref(n), C.byref(d), C.byref(l)))
+        return {"nodes": n.value, "depth": d.value, "leaves": l.value}
+
+
+class GpuSimulation:
+    """GPU replacement of MolflowSimulation + its ParticleTracer threads."""
+
+    def __init__(self, model: Model = None, device: int = 0):
+        self.device = device
+        self.h = None
+        self.gmodel = None
+        self.last_stats = None
+        if model is not None:
+            self.LoadSimulation(model)
+
+    # --- MolflowSimulation surface (MolflowSimulation.h:22-45) ---
+    def LoadSimulation(self, model: Model):
+        """Prepare the model (geometry, BVH, tables) and upload it (MolflowSimulation.cpp:92-154)."""
+        self.close()
+        self.model = model
+        self.gmodel = GpuModel(model)
+        h = C.c_void_p()
+        _check(load_library().mfg_sim_create(self.gmodel.h, self.device, C.byref(h)))
+        self.h = h
+        return 0
+
+    def ResetSimulation(self):
+        _check(load_library().mfg_reset(self.h))
+
+    def GetHitsSize(self):
+        L = self.gmodel.layout()
+        return 8 * (L["n_global"] + L["n_facet_counts"] + L["n_facet_sums"] + L["n_texture"] + L["n_profile"] +
+                    L["n_direction"] + L["n_anglemap"])
+
+    def set_particle_offset(self, first_particle):
+        _check(load_library().mfg_set_particle_offset(self.h, int(first_particle)))
+
+    def particle_offset(self):
+        return int(load_library().mfg_particle_offset(self.h))
+
+    # --- ParticleTracer surface (Particle.h:45,86) ---
+    def SimulationMCStep(self, n_desorptions, precision=A.PREC_FP64, seed=0x4D6F6C66, block_size=0,
+                         blocks_per_sm=0, time_limit_s=0.0, max_steps=0):
+        """Desorb and trace n_desorptions particles on the GPU (blocking)."""
+        if not time_limit_s:
+            time_limit_s = float(os.environ.get("MFG_TIME_LIMIT_S", "0"))
+        o = A.RunOptions(precision=precision, seed=seed, block_size=block_size, blocks_per_sm=blocks_per_sm,
+                         smem_bvh_nodes=-1, time_limit_s=time_limit_s, max_steps_per_particle=max_steps)
+        st = A.RunStats()
+        rc = load_library().mfg_run(self.h, int(n_desorptions), C.byref(o), C.byref(st))
+        self.last_stats = {f: getattr(st, f) for f, _ in A.RunStats._fields_}
+        if rc == A.MFG_ERR_NO_SOURCE:
+            return MCStepResult.DesorptionError
+        _check(rc)
+        return MCStepResult.Success
+
+    def run_async(self, n_desorptions, precision=A.PREC_FP64, seed=0x4D6F6C66, time_limit_s=0.0):
+        o = A.RunOptions(precision=precision, seed=seed, smem_bvh_nodes=-1, time_limit_s=time_limit_s)
+        _check(load_library().mfg_run_async(self.h, int(n_desorptions), C.byref(o)))
+
+    def poll(self):
+        return load_library().mfg_poll(self.h)
+
+    def wait(self, timeout_ms=-1):
+        st = A.RunStats()
+        rc = load_library().mfg_wait(self.h, int(timeout_ms), C.byref(st))
+        self.last_stats = {f: getattr(st, f) for f, _ in A.RunStats._fields_}
+        return rc
+
+    def abort(self):
+        _check(load_library().mfg_abort(self.h))
+
+    def fetch(self, state: SimuState = None):
+        """Accumulated tallies since the last reset, as a new (or given) SimuState."""
+        st = state if state is not None else SimuState(self.model)
+        v = st.view()
+        _check(load_library().mfg_fetch(self.h, C.byref(v)))
+        return st
+
+    def UpdateHitsAndLog(self, global_state: SimuState, lock: threading.Lock = None, timeout_ms=10000):
+        """Add this simulation's tallies into global_state and clear them (Particle.cpp:21-73,1294-1312)."""
+        local = self.fetch()
+        if lock is not None:
+            if not lock.acquire(timeout=timeout_ms / 1000.0):
+                return False
+        try:
+            global_state += local
+        finally:
+            if lock is not None:
+                lock.release()
+        self.ResetSimulation()
+        return True
+
+    def replay(self, origin, direction, last, precision=A.PREC_FP64):
+        """Intersect given rays (replay mode); returns (hit_facet, hit_t, n_rechecks)."""
+        origin = np.ascontiguousarray(origin, np.float64)
+        direction = np.ascontiguousarray(direction, np.float64)
+        last = np.ascontiguousarray(last, np.int32)
+        n = len(last)
+        hf = np.zeros(n, np.int32)
+        ht = np.zeros(n, np.float64)
+        nr = C.c_uint64()
+        _check(load_library().mfg_replay(self.h, precision, n, A.ptr(origin, C.c_double), A.ptr(direction, C.c_double),
+                                         A.ptr(last, C.c_int32), A.ptr(hf, C.c_int32), A.ptr(ht, C.c_double),
+                                         C.byref(nr)))
+        return hf, ht, nr.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            load_library().mfg_sim_destroy(self.h)
+            self.h = None
+        if getattr(self, "gmodel", None) is not None:
+            self.gmodel.close()
+            self.gmodel = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

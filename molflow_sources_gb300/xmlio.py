@@ -1,0 +1,235 @@
+"""MolFlow+ XML reader: geometry, simulation settings and stored results.
+
+Reads the `<SimulationEnvironment type="molflow">` files the reference writes
+(src/IO/WriterXML.cpp:72-903) and reads (src/IO/LoaderXML.cpp:31-1130), plain
+or inside a .zip, with the standard library only.  Produces a `Model` (the
+facet fields used by the tracer, LoaderXML.cpp:831-1120) and a `SimuState`
+with the stored GlobalSimuState (LoaderXML.cpp:366-760).
+"""
+import io
+import zipfile
+import xml.etree.ElementTree as ET
+
+import numpy as np
+
+from . import _abi as A
+from .model import Model, SimuState
+
+
+def _root(path_or_bytes):
+    if isinstance(path_or_bytes, (bytes, bytearray)):
+        data = bytes(path_or_bytes)
+    elif str(path_or_bytes).lower().endswith(".zip"):
+        with zipfile.ZipFile(path_or_bytes) as z:
+            names = [n for n in z.namelist() if n.lower().endswith(".xml")]
+            data = z.read(names[0])
+    else:
+        with open(path_or_bytes, "rb") as f:
+            data = f.read()
+    return ET.parse(io.BytesIO(data)).getroot()
+
+
+def _f(node, attr, default=0.0):
+    if node is None or node.get(attr) is None:
+        return default
+    return float(node.get(attr))
+
+
+def _i(node, attr, default=0):
+    if node is None or node.get(attr) is None:
+        return default
+    v = node.get(attr)
+    if v in ("true", "false"):
+        return int(v == "true")
+    return int(float(v))
+
+
+def _parse_user_moments(um_node):
+    """UserMoments entries: 'begin,spacing,end' ranges or single times (TimeMoments.cpp:58-83)."""
+    times, windows = [], []
+    if um_node is None:
+        return times, windows
+    for u in um_node.findall("UserEntry"):
+        content = u.get("content", "")
+        win = float(u.get("window", "0"))
+        parts = [p for p in content.replace(" ", "").split(",") if p]
+        if len(parts) == 3:
+            b, s, e = map(float, parts)
+            k = 0
+            while b + k * s <= e * (1 + 1e-12) and s > 0:
+                times.append(b + k * s)
+                windows.append(win)
+                k += 1
+        elif len(parts) == 1:
+            times.append(float(parts[0]))
+            windows.append(win)
+    return times, windows
+
+
+def load(path_or_bytes, with_state=True):
+    """Return (model, state or None, info dict)."""
+    r = _root(path_or_bytes)
+    g = r.find("Geometry")
+    vnode = g.find("Vertices")
+    verts = np.array([[float(v.get("x")), float(v.get("y")), float(v.get("z"))] for v in vnode.findall("Vertex")])
+    fnodes = g.find("Facets").findall("Facet")
+    facets = [[int(i.get("vertex")) for i in f.find("Indices").findall("Indice")] for f in fnodes]
+    m = Model(verts, facets)
+    sims = r.find("MolflowSimuSettings")
+    # time-dependent parameters (LoaderXML.cpp:69-100)
+    names = []
+    pnode = sims.find("Parameters") if sims is not None else None
+    if pnode is not None:
+        for p in pnode.findall("Parameter"):
+            t = [float(x.get("t")) for x in p.findall("Moment")]
+            v = [float(x.get("value")) for x in p.findall("Moment")]
+            m.add_param(t, v, logx=_i(p, "logXinterp"), logy=_i(p, "logYinterp"))
+            names.append(p.get("name"))
+
+    def param_ref(node, name_attr):
+        if node is None:
+            return -1
+        if node.get(name_attr):
+            nm = node.get(name_attr)
+            return names.index(nm) if nm in names else -1
+        return _i(node, "parameterId", -1)
+
+    for k, f in enumerate(fnodes):
+        st = f.find("Sticking")
+        op = f.find("Opacity")
+        og = f.find("Outgassing")
+        te = f.find("Temperature")
+        rf = f.find("Reflection")
+        su = f.find("Structure")
+        rec = f.find("Recordings")
+        tx = rec.find("Texture") if rec is not None else None
+        m.sticking[k] = _f(st, "constValue")
+        m.sticking_param[k] = param_ref(st, "stickingParam")
+        m.opacity[k] = _f(op, "constValue", 1.0)
+        m.opacity_param[k] = param_ref(op, "opacityParam")
+        m.is_2sided[k] = _i(op, "is2sided")
+        m.outgassing[k] = _f(og, "constValue")
+        m.outgassing_param[k] = param_ref(og, "OutgassingParam")
+        m.desorb_type[k] = _i(og, "desType")
+        m.desorb_exponent[k] = _f(og, "desExponent")
+        m.temperature[k] = _f(te, "value", 293.15)
+        m.temperature_param[k] = param_ref(te, "tempParam")
+        m.accommodation[k] = _f(te, "accFactor", 1.0)
+        if rf is not None and rf.get("diffusePart") is not None:
+            m.refl_diffuse[k] = _f(rf, "diffusePart", 1.0)
+            m.refl_specular[k] = _f(rf, "specularPart", 0.0)
+            m.refl_cos_exponent[k] = _f(rf, "cosineExponent", 0.0)
+        elif rf is not None:
+            t = _i(rf, "type")
+            m.refl_diffuse[k], m.refl_specular[k] = (1.0, 0.0) if t == 0 else ((0.0, 1.0) if t == 1 else (0.0, 0.0))
+        m.enable_sojourn[k] = _i(rf, "enableSojournTime")
+        m.sojourn_freq[k] = _f(rf, "sojournFreq")
+        m.sojourn_e[k] = _f(rf, "sojournE")
+        m.structure[k] = _i(su, "inStructure")
+        m.link_dest[k] = _i(su, "linksTo")
+        m.teleport_dest[k] = _i(f.find("Teleport"), "target")
+        m.is_moving[k] = _i(f.find("Motion"), "isMoving")
+        if rec is not None:
+            m.profile_type[k] = _i(rec.find("Profile"), "type")
+            am = rec.find("IncidentAngleMap")
+            if am is not None:
+                m.anglemap_record[k] = _i(am, "record")
+                m.anglemap_phi_width[k] = _i(am, "phiWidth")
+                m.anglemap_theta_limit[k] = _f(am, "thetaLimit", 1.570796326)
+                m.anglemap_theta_lower_res[k] = _i(am, "thetaLowerRes")
+                m.anglemap_theta_higher_res[k] = _i(am, "thetaHigherRes")
+        if tx is not None:
+            m.tex_width[k] = _f(tx, "texDimX")
+            m.tex_height[k] = _f(tx, "texDimY")
+            flags = 0
+            for bit, attr in ((A.COUNT_DES, "countDes"), (A.COUNT_ABS, "countAbs"), (A.COUNT_REFL, "countRefl"),
+                              (A.COUNT_TRANS, "countTrans"), (A.COUNT_DIR, "countDir")):
+                if _i(tx, attr):
+                    flags |= bit
+            m.count_flags[k] = flags
+    structs = g.find("Structures")
+    m.n_structures = max(1, _i(structs, "nb", 1))
+    if sims is not None:
+        gas = sims.find("Gas")
+        m.gas_mass = _f(gas, "mass", 28.0)
+        m.enable_decay = _i(gas, "enableDecay")
+        m.half_life = _f(gas, "halfLife", 1.0)
+        lf = sims.find("LowFluxMode")
+        m.low_flux_mode = _i(lf, "enabled")
+        m.low_flux_cutoff = _f(lf, "cutoff", 1e-7)
+        ts = sims.find("TimeSettings")
+        m.time_window = _f(ts, "timeWindow", 1e-10)
+        m.use_maxwell = _i(ts, "useMaxwellDistr", 1)
+        m.constant_flow = _i(ts, "calcConstFlow", 1)
+        t, w = _parse_user_moments(ts.find("UserMoments") if ts is not None else None)
+        if t:
+            m.set_moments(t, w)
+    info = {"n_structures": m.n_structures, "param_names": names}
+    state = load_state(r, m) if with_state else None
+    return m, state, info
+
+
+def load_state(r, m):
+    """Stored results (LoaderXML.cpp:366-760) into a SimuState; None if absent."""
+    res = r.find("MolflowResults")
+    if res is None:
+        return None
+    st = SimuState(m)
+    L = st.L
+    moments = res.find("Moments").findall("Moment")
+    for mi, mom in enumerate(moments):
+        if mi >= L["blocks"]:
+            break
+        if mi == 0:
+            gh = mom.find("Global/Hits")
+            st.global_[A.G_NBMCHIT] = _f(gh, "totalHit")
+            st.global_[A.G_NBHITEQUIV] = _f(gh, "totalHitEquiv")
+            st.global_[A.G_NBDESORBED] = _f(gh, "totalDes")
+            st.global_[A.G_NBABSEQUIV] = _f(gh, "totalAbsEquiv")
+            st.global_[A.G_NBLEAK] = _f(gh, "totalLeak")
+            st.global_[A.G_DIST_TOTAL] = _f(gh, "totalDist_total")
+            st.global_[A.G_DIST_FULLHITS] = _f(gh, "totalDist_fullHitsOnly")
+        for fr in mom.find("FacetResults").findall("Facet"):
+            k = int(fr.get("id"))
+            h = fr.find("Hits")
+            st.facet_counts[mi, k, A.FC_NBMCHIT] = int(float(h.get("nbHit")))
+            st.facet_counts[mi, k, A.FC_NBDESORBED] = int(float(h.get("nbDes")))
+            st.facet_counts[mi, k, A.FC_NBABSORBED] = int(round(float(h.get("nbAbsEquiv"))))
+            st.facet_sums[mi, k, A.FS_NBHITEQUIV] = _f(h, "nbHitEquiv")
+            st.facet_sums[mi, k, A.FS_NBABSEQUIV] = _f(h, "nbAbsEquiv")
+            st.facet_sums[mi, k, A.FS_SUM_V_ORT] = _f(h, "sum_v_ort")
+            st.facet_sums[mi, k, A.FS_SUM_1_PER_ORT_VEL] = _f(h, "sum_1_per_v")
+            st.facet_sums[mi, k, A.FS_SUM_1_PER_VELOCITY] = _f(h, "sum_v")
+            pr = fr.find("Profile")
+            if pr is not None and L["prof_idx"][k] >= 0:
+                p = st.profile[mi, L["prof_idx"][k]]
+                for s in pr.findall("Slice"):
+                    j = int(s.get("id"))
+                    if j < A.PROFILE_SIZE:
+                        p[j, 0] = _f(s, "countEquiv")
+                        p[j, 1] = _f(s, "sum_v_ort")
+                        p[j, 2] = _f(s, "sum_1_per_v")
+            tx = fr.find("Texture")
+            if tx is not None and L["tex_off"][k] >= 0:
+                w, hh = int(L["tex_w"][k]), int(L["tex_h"][k])
+                fw, fh = int(tx.get("width")), int(tx.get("height"))
+                blocks = {}
+                for c in tx:
+                    vals = np.array(c.text.split(), dtype=np.float64) if c.text and c.text.strip() else np.zeros(0)
+                    blocks[c.tag] = vals
+                o = L["tex_off"][k]
+                for field, tag in ((0, "count"), (1, "sum_v_ort"), (2, "sum_1_per_v")):
+                    vals = blocks.get(tag)
+                    if vals is None or vals.size < fw * fh:
+                        continue
+                    grid = vals[:fw * fh].reshape(fh, fw)[:hh, :w]
+                    sub = np.zeros((hh, w))
+                    sub[:grid.shape[0], :grid.shape[1]] = grid
+                    st.texture[mi, o:o + w * hh, field] = sub.reshape(-1)
+            am = fr.find("IncidentAngleMap")
+            if am is not None and L["ang_off"][k] >= 0 and mi == 0:
+                vals = np.array(am.text.split(), dtype=np.float64) if am.text else np.zeros(0)
+                o = L["ang_off"][k]
+                n = min(vals.size, st.anglemap.size - o)
+                st.anglemap[o:o + n] = vals[:n].astype(np.uint64)
+    return st

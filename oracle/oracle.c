@@ -1,0 +1,1279 @@
+/*
+ * oracle.c — CPU FP64 restatement of MolFlow+'s test-particle Monte Carlo tracer.
+ *
+ * TEST INFRASTRUCTURE ONLY (see oracle.h).  Written from the reference's
+ * algorithm; each function names the reference lines it follows.  Compiled with
+ * -ffp-contract=off so x86 and Arm builds give identical numbers.
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define PI_D 3.14159265358979323846
+#define KB_MOLFLOW 1.38E-23
+#define MAXWELL_CDF_N 100
+#define MAX_TRANSP 256
+
+/* ------------------------------------------------------------------ RNG -- */
+
+/* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11). */
+void orc_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        c0 = hi1 ^ c1 ^ k0;
+        c1 = lo1;
+        c2 = hi0 ^ c3 ^ k1;
+        c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+static inline double u01_from(uint32_t a, uint32_t b) {
+    /* uniform double in [0,1): 52 random mantissa bits of (a:b) in [1,2), minus 1 (exact) */
+    uint64_t m = (((uint64_t)a << 32) | b) >> 12;
+    uint64_t bits = 0x3FF0000000000000ull | m;
+    double x;
+    memcpy(&x, &bits, sizeof x);
+    return x - 1.0;
+}
+
+/* MT19937 (Matsumoto & Nishimura 1998) */
+typedef struct { uint32_t mt[624]; int mti; } mt19937;
+static void mt_seed(mt19937* g, uint32_t s) {
+    g->mt[0] = s;
+    for (int i = 1; i < 624; ++i)
+        g->mt[i] = 1812433253u * (g->mt[i - 1] ^ (g->mt[i - 1] >> 30)) + (uint32_t)i;
+    g->mti = 624;
+}
+static uint32_t mt_next(mt19937* g) {
+    uint32_t y;
+    if (g->mti >= 624) {
+        for (int k = 0; k < 624; ++k) {
+            y = (g->mt[k] & 0x80000000u) | (g->mt[(k + 1) % 624] & 0x7fffffffu);
+            g->mt[k] = g->mt[(k + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+        }
+        g->mti = 0;
+    }
+    y = g->mt[g->mti++];
+    y ^= (y >> 11);
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= (y >> 18);
+    return y;
+}
+
+typedef struct {
+    int mode;
+    uint32_t key[2];
+    uint64_t pid;
+    uint32_t ctr;
+    int have;
+    double cache;
+    mt19937 mt;
+} rng_t;
+
+static void rng_start_particle(rng_t* r, uint64_t pid) {
+    r->pid = pid; r->ctr = 0; r->have = 0;
+}
+static double rnd(rng_t* r) {
+    if (r->mode == ORC_RNG_MT) {
+        uint32_t a = mt_next(&r->mt), b = mt_next(&r->mt);
+        return u01_from(a, b);
+    }
+    if (r->have) { r->have = 0; return r->cache; }
+    uint32_t c[4] = {(uint32_t)r->pid, (uint32_t)(r->pid >> 32), r->ctr++, 0u}, o[4];
+    orc_philox4x32(c, r->key, o);
+    r->cache = u01_from(o[2], o[3]);
+    r->have = 1;
+    return u01_from(o[0], o[1]);
+}
+/* order-independent draw for the opacity decision of facet f at trace step s */
+static double rnd_opacity(rng_t* r, uint64_t step, int f) {
+    if (r->mode == ORC_RNG_MT) return rnd(r);
+    uint32_t c[4] = {(uint32_t)r->pid, (uint32_t)(r->pid >> 32), (uint32_t)step, (uint32_t)f + 1u}, o[4];
+    orc_philox4x32(c, r->key, o);
+    return u01_from(o[0], o[1]);
+}
+
+/* -------------------------------------------------------------- vectors -- */
+static inline double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static inline void cross3(const double* a, const double* b, double* c) {
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+}
+static inline double norm3(const double* a) { return sqrt(dot3(a, a)); }
+
+/* ------------------------------------------------------- interpolation -- */
+/* index of the last table entry <= key, -1 if key is below the first (MathTools lower_index contract,
+ * described at Particle.cpp:435-437) */
+static int lower_index(double key, const double* tab, int n) {
+    int lo = 0, hi = n;  /* first index with tab[i] > key */
+    while (lo < hi) { int mid = (lo + hi) >> 1; if (tab[mid] <= key) lo = mid + 1; else hi = mid; }
+    return lo - 1;
+}
+static double weigh(double a, double b, double w) { return a + (b - a) * w; }
+/* InterpolateY(x, table, logX, logY, allowExtrapolate): y at x (SimulationMC.cpp:20) */
+static double interp_y(double x, const double* xs, const double* ys, int n, int logx, int logy, int extrap) {
+    if (n == 1) return ys[0];
+    int i = lower_index(x, xs, n);
+    if (i == -1) { if (!extrap) return ys[0]; i = 0; }
+    else if (i == n - 1) { if (!extrap) return ys[n - 1]; i = n - 2; }
+    double x0 = xs[i], x1 = xs[i + 1], y0 = ys[i], y1 = ys[i + 1];
+    double w = logx ? (log10(x) - log10(x0)) / (log10(x1) - log10(x0)) : (x - x0) / (x1 - x0);
+    if (logy) return pow(10.0, weigh(log10(y0), log10(y1), w));
+    return weigh(y0, y1, w);
+}
+/* InterpolateX(y, table, ...): x where the table reaches y (Physics.cpp:7) */
+static double interp_x(double y, const double* xs, const double* ys, int n, int logx, int logy, int extrap) {
+    if (n == 1) return xs[0];
+    int i = lower_index(y, ys, n);
+    if (i == -1) { if (!extrap) return xs[0]; i = 0; }
+    else if (i == n - 1) { if (!extrap) return xs[n - 1]; i = n - 2; }
+    double y0 = ys[i], y1 = ys[i + 1];
+    double w = logy ? (log10(y) - log10(y0)) / (log10(y1) - log10(y0)) : (y - y0) / (y1 - y0);
+    if (logx) return pow(10.0, weigh(log10(xs[i]), log10(xs[i + 1]), w));
+    return weigh(xs[i], xs[i + 1], w);
+}
+
+/* Generate_CDF(1 K, gasMass): flux-weighted Maxwell CDF on 100 points (CDFGeneration.cpp:54-83) */
+void orc_maxwell_cdf(double gas_mass, double* speed, double* cumul) {
+    const double kb = 1.38E-23, R = 8.3144621;
+    double T = 1.0;
+    double a = sqrt(kb * T / (gas_mass * 1.67E-27));
+    double vprob = sqrt(2.0 * R * T / (gas_mass / 1000.0));
+    double bin = 4.0 * vprob / (double)MAXWELL_CDF_N;
+    for (int i = 0; i < MAXWELL_CDF_N; ++i) {
+        double x = (double)i * bin;
+        double y = (x * x) / (2.0 * a * a);
+        speed[i] = x;
+        cumul[i] = 1.0 - exp(-y) * (y + 1.0);
+    }
+}
+
+/* -------------------------------------------------------------- model -- */
+typedef struct {
+    double O[3], U[3], V[3], N[3], nU[3], nV[3];
+    double center[3];
+    double bbmin[3], bbmax[3];
+    double area;
+    double invU2, invV2;   /* 1/|U|^2, 1/|V|^2 */
+    double planeD;         /* N.O */
+    int vstart, nv;        /* into model->v2 (u,v pairs) */
+    /* parameters */
+    double sticking, opacity, outgassing, temperature, sqrtT, accommodation;
+    int desorb_type; double desorb_exp;
+    double diffuse, specular, cos_exp;
+    int two_sided, structure, link, teleport;
+    double texw_p, texh_p; int texw, texh; uint32_t count;
+    int profile_type; double max_speed;
+    int am_record, am_phi, am_lo, am_hi; double am_limit;
+    int p_stick, p_opac, p_outg, p_temp;
+    int sojourn; double soj_freq, soj_e;
+    /* layout */
+    long tex_off, dir_off, ang_off; int prof_idx;
+    /* desorption */
+    int id_idx;            /* integrated desorption table index, -1 none */
+} ofacet;
+
+typedef struct { double bmin[3], bmax[3]; int left, right, first, count; } onode;
+
+typedef struct { int n; double* t; double* v; int logx, logy; } oparam;
+typedef struct { int n; double* t; double* cum; } oid;
+
+struct orc_model {
+    int nf, nstruct;
+    ofacet* f;
+    double* v2;            /* vertices2, 2 doubles per vertex */
+    double* texinc;        /* per texture cell increment (1/area) */
+    /* per-structure BVH over facet ids */
+    int* nnodes; onode** nodes; int** prims;
+    /* moments */
+    int nm; double* mstart; double* mend; double maxwin;
+    double latest;
+    int constant_flow, use_maxwell, low_flux, decay;
+    double low_flux_cutoff, half_life, gas_mass;
+    double cdf_v[MAXWELL_CDF_N], cdf_p[MAXWELL_CDF_N];
+    int nparams; oparam* params;
+    int nid; oid* ids;
+    double* src_prefix; int* src_facet; int nsrc; double src_total;
+    mfg_state_layout L;
+};
+
+static void set_err(char* err, size_t n, const char* msg) {
+    if (err && n) { strncpy(err, msg, n - 1); err[n - 1] = 0; }
+}
+
+/* Facet basis (O,U,V,N,nU,nV) and normalised polygon vertices, restating the
+ * src_shared geometry initialisation contract used by the tracer:
+ * N from the first non-degenerate pair of consecutive edges (right-hand rule),
+ * nU along the first edge, nV = N x nU, (u,v) of every vertex rescaled to the
+ * polygon's bounding rectangle, N and nV flipped when the signed area is negative.
+ * Texture dims in the fixtures confirm U runs along indices[0]->indices[1]. */
+static int facet_basis(ofacet* F, const double* vert, const int32_t* idx, double* v2) {
+    int n = F->nv;
+    const double* p0 = vert + 3 * idx[0];
+    double N[3] = {0, 0, 0};
+    int ok = 0;
+    for (int k = 0; k + 2 < n + 0 && !ok; ++k) {
+        const double* a = vert + 3 * idx[k];
+        const double* b = vert + 3 * idx[k + 1];
+        const double* c = vert + 3 * idx[k + 2];
+        double e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+        double e2[3] = {c[0] - b[0], c[1] - b[1], c[2] - b[2]};
+        cross3(e1, e2, N);
+        if (norm3(N) >= 1e-11) ok = 1;
+    }
+    if (!ok) return -1;
+    double nn = norm3(N);
+    for (int i = 0; i < 3; ++i) N[i] /= nn;
+    const double* p1 = vert + 3 * idx[1];
+    double U[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+    double ul = norm3(U);
+    if (ul <= 0) return -1;
+    for (int i = 0; i < 3; ++i) U[i] /= ul;
+    double V[3];
+    cross3(N, U, V);
+    double umin = 0, umax = 0, vmin = 0, vmax = 0;
+    for (int j = 0; j < n; ++j) {
+        const double* p = vert + 3 * idx[j];
+        double d[3] = {p[0] - p0[0], p[1] - p0[1], p[2] - p0[2]};
+        double u = (j == 0) ? 0.0 : dot3(U, d);
+        double v = (j == 0) ? 0.0 : dot3(V, d);
+        v2[2 * j] = u; v2[2 * j + 1] = v;
+        if (u < umin) umin = u; if (u > umax) umax = u;
+        if (v < vmin) vmin = v; if (v > vmax) vmax = v;
+    }
+    double area2 = 0;
+    for (int j = 0; j < n; ++j) {
+        int jn = (j + 1) % n;
+        area2 += v2[2 * j] * v2[2 * jn + 1] - v2[2 * jn] * v2[2 * j + 1];
+    }
+    if (area2 < 0) {
+        for (int i = 0; i < 3; ++i) { N[i] = -N[i]; V[i] = -V[i]; }
+        vmin = 0; vmax = 0;
+        for (int j = 0; j < n; ++j) {
+            v2[2 * j + 1] = -v2[2 * j + 1];
+            if (v2[2 * j + 1] < vmin) vmin = v2[2 * j + 1];
+            if (v2[2 * j + 1] > vmax) vmax = v2[2 * j + 1];
+        }
+    }
+    F->area = fabs(0.5 * area2);
+    double uD = umax - umin, vD = vmax - vmin;
+    if (uD <= 0 || vD <= 0) return -1;
+    for (int i = 0; i < 3; ++i) {
+        F->N[i] = N[i]; F->nU[i] = U[i]; F->nV[i] = V[i];
+        F->O[i] = p0[i] + umin * U[i] + vmin * V[i];
+        F->U[i] = U[i] * uD; F->V[i] = V[i] * vD;
+    }
+    for (int j = 0; j < n; ++j) {
+        v2[2 * j] = (v2[2 * j] - umin) / uD;
+        v2[2 * j + 1] = (v2[2 * j + 1] - vmin) / vD;
+    }
+    F->invU2 = 1.0 / dot3(F->U, F->U);
+    F->invV2 = 1.0 / dot3(F->V, F->V);
+    F->planeD = dot3(F->N, F->O);
+    for (int i = 0; i < 3; ++i) { F->bbmin[i] = 1e300; F->bbmax[i] = -1e300; }
+    for (int j = 0; j < n; ++j) {
+        const double* p = vert + 3 * idx[j];
+        for (int i = 0; i < 3; ++i) {
+            if (p[i] < F->bbmin[i]) F->bbmin[i] = p[i];
+            if (p[i] > F->bbmax[i]) F->bbmax[i] = p[i];
+        }
+    }
+    for (int i = 0; i < 3; ++i) F->center[i] = 0.5 * (F->bbmin[i] + F->bbmax[i]);
+    return 0;
+}
+
+/* Crossing-number point-in-polygon in (u,v) space (IsInFacet contract, Particle.cpp:148,540). */
+static int in_polygon(const double* v2, int n, double u, double v) {
+    int inside = 0;
+    for (int i = 0, j = n - 1; i < n; j = i++) {
+        double ui = v2[2 * i], vi = v2[2 * i + 1], uj = v2[2 * j], vj = v2[2 * j + 1];
+        if ((vi > v) != (vj > v)) {
+            double cr = (uj - ui) * (v - vi) - (u - ui) * (vj - vi);
+            if ((cr > 0) == (vj > vi)) inside = !inside;
+        }
+    }
+    return inside;
+}
+
+/* area of polygon (u,v in cm) clipped to an axis-aligned rectangle, Sutherland-Hodgman */
+static double clip_area(const double* poly, int n, double x0, double y0, double x1, double y1) {
+    double bufA[2 * 4096], bufB[2 * 4096];
+    if (n > 1000) return -1;
+    int m = n;
+    memcpy(bufA, poly, sizeof(double) * 2 * n);
+    double* in = bufA; double* out = bufB;
+    for (int edge = 0; edge < 4; ++edge) {
+        int k = 0;
+        for (int i = 0; i < m; ++i) {
+            double* P = in + 2 * i; double* Q = in + 2 * ((i + 1) % m);
+            double dp, dq;
+            switch (edge) {
+                case 0: dp = P[0] - x0; dq = Q[0] - x0; break;
+                case 1: dp = x1 - P[0]; dq = x1 - Q[0]; break;
+                case 2: dp = P[1] - y0; dq = Q[1] - y0; break;
+                default: dp = y1 - P[1]; dq = y1 - Q[1]; break;
+            }
+            if (dp >= 0) { out[2 * k] = P[0]; out[2 * k + 1] = P[1]; ++k; }
+            if ((dp >= 0) != (dq >= 0)) {
+                double t = dp / (dp - dq);
+                out[2 * k] = P[0] + t * (Q[0] - P[0]);
+                out[2 * k + 1] = P[1] + t * (Q[1] - P[1]);
+                ++k;
+            }
+        }
+        m = k;
+        double* tmp = in; in = out; out = tmp;
+        if (m == 0) return 0.0;
+    }
+    double a = 0;
+    for (int i = 0; i < m; ++i) {
+        int j = (i + 1) % m;
+        a += in[2 * i] * in[2 * j + 1] - in[2 * j] * in[2 * i + 1];
+    }
+    return fabs(0.5 * a);
+}
+
+/* ---------------------------------------------------------------- BVH -- */
+typedef struct { int* ids; double* cen; const ofacet* f; onode* nodes; int nn, cap; int* prims; int np; } bvh_build;
+
+static int bvh_rec(bvh_build* B, int* ids, int n) {
+    if (B->nn >= B->cap) { B->cap *= 2; B->nodes = (onode*)realloc(B->nodes, sizeof(onode) * B->cap); }
+    int me = B->nn++;
+    onode nd;
+    for (int i = 0; i < 3; ++i) { nd.bmin[i] = 1e300; nd.bmax[i] = -1e300; }
+    for (int k = 0; k < n; ++k) {
+        const ofacet* F = &B->f[ids[k]];
+        for (int i = 0; i < 3; ++i) {
+            if (F->bbmin[i] < nd.bmin[i]) nd.bmin[i] = F->bbmin[i];
+            if (F->bbmax[i] > nd.bmax[i]) nd.bmax[i] = F->bbmax[i];
+        }
+    }
+    nd.left = nd.right = -1;
+    if (n <= 2) {   /* 2 facets per leaf (MolflowSimulation.cpp:79) */
+        nd.first = B->np; nd.count = n;
+        for (int k = 0; k < n; ++k) B->prims[B->np++] = ids[k];
+        B->nodes[me] = nd;
+        return me;
+    }
+    /* binned SAH on centroids, 16 bins per axis */
+    double cmin[3] = {1e300, 1e300, 1e300}, cmax[3] = {-1e300, -1e300, -1e300};
+    for (int k = 0; k < n; ++k)
+        for (int i = 0; i < 3; ++i) {
+            double c = B->f[ids[k]].center[i];
+            if (c < cmin[i]) cmin[i] = c; if (c > cmax[i]) cmax[i] = c;
+        }
+    enum { NB = 16 };
+    double best = 1e300; int bax = -1; double bsplit = 0;
+    for (int ax = 0; ax < 3; ++ax) {
+        double ext = cmax[ax] - cmin[ax];
+        if (ext <= 0) continue;
+        int cnt[NB] = {0}; double bmn[NB][3], bmx[NB][3];
+        for (int b = 0; b < NB; ++b) for (int i = 0; i < 3; ++i) { bmn[b][i] = 1e300; bmx[b][i] = -1e300; }
+        for (int k = 0; k < n; ++k) {
+            const ofacet* F = &B->f[ids[k]];
+            int b = (int)((F->center[ax] - cmin[ax]) / ext * NB); if (b >= NB) b = NB - 1; if (b < 0) b = 0;
+            cnt[b]++;
+            for (int i = 0; i < 3; ++i) {
+                if (F->bbmin[i] < bmn[b][i]) bmn[b][i] = F->bbmin[i];
+                if (F->bbmax[i] > bmx[b][i]) bmx[b][i] = F->bbmax[i];
+            }
+        }
+        for (int s = 1; s < NB; ++s) {
+            double lmn[3] = {1e300, 1e300, 1e300}, lmx[3] = {-1e300, -1e300, -1e300};
+            double rmn[3] = {1e300, 1e300, 1e300}, rmx[3] = {-1e300, -1e300, -1e300};
+            int lc = 0, rc = 0;
+            for (int b = 0; b < s; ++b) { lc += cnt[b]; for (int i = 0; i < 3; ++i) { if (bmn[b][i] < lmn[i]) lmn[i] = bmn[b][i]; if (bmx[b][i] > lmx[i]) lmx[i] = bmx[b][i]; } }
+            for (int b = s; b < NB; ++b) { rc += cnt[b]; for (int i = 0; i < 3; ++i) { if (bmn[b][i] < rmn[i]) rmn[i] = bmn[b][i]; if (bmx[b][i] > rmx[i]) rmx[i] = bmx[b][i]; } }
+            if (!lc || !rc) continue;
+            double dl[3] = {lmx[0] - lmn[0], lmx[1] - lmn[1], lmx[2] - lmn[2]};
+            double dr[3] = {rmx[0] - rmn[0], rmx[1] - rmn[1], rmx[2] - rmn[2]};
+            double sal = dl[0] * dl[1] + dl[1] * dl[2] + dl[2] * dl[0];
+            double sar = dr[0] * dr[1] + dr[1] * dr[2] + dr[2] * dr[0];
+            double cost = sal * lc + sar * rc;
+            if (cost < best) { best = cost; bax = ax; bsplit = cmin[ax] + ext * (double)s / NB; }
+        }
+    }
+    int mid;
+    if (bax < 0) {
+        mid = n / 2;   /* all centroids equal: split the list */
+    } else {
+        int i = 0, j = n - 1;
+        while (i <= j) {
+            if (B->f[ids[i]].center[bax] < bsplit) ++i;
+            else { int t = ids[i]; ids[i] = ids[j]; ids[j] = t; --j; }
+        }
+        mid = i;
+        if (mid == 0 || mid == n) mid = n / 2;
+    }
+    nd.first = -1; nd.count = 0;
+    B->nodes[me] = nd;
+    int l = bvh_rec(B, ids, mid);
+    int r = bvh_rec(B, ids + mid, n - mid);
+    B->nodes[me].left = l; B->nodes[me].right = r;
+    return me;
+}
+
+static void build_structure_bvh(orc_model* M, int s) {
+    int* ids = (int*)malloc(sizeof(int) * (M->nf + 1));
+    int n = 0;
+    for (int i = 0; i < M->nf; ++i)
+        if (M->f[i].structure == -1 || M->f[i].structure == s) ids[n++] = i;
+    bvh_build B;
+    B.f = M->f; B.cap = 2 * n + 2; B.nodes = (onode*)malloc(sizeof(onode) * B.cap); B.nn = 0;
+    B.prims = (int*)malloc(sizeof(int) * (n + 1)); B.np = 0;
+    if (n > 0) bvh_rec(&B, ids, n);
+    M->nodes[s] = B.nodes; M->nnodes[s] = B.nn; M->prims[s] = B.prims;
+    free(ids);
+}
+
+/* ---------------------------------------------------- Generate_ID -------- */
+/* Integrated desorption for a time-dependent outgassing parameter (IDGeneration.cpp:45-207). */
+static void generate_id(const oparam* P, double latest, oid* out) {
+    int cap = 16 + 12 * (P->n + 2);
+    double* ot = (double*)malloc(sizeof(double) * (P->n + 3));
+    double* ov = (double*)malloc(sizeof(double) * (P->n + 3));
+    int no = 0;
+    out->t = (double*)malloc(sizeof(double) * cap);
+    out->cum = (double*)malloc(sizeof(double) * cap);
+    int n = 0;
+    int ia;
+    for (ia = 0; ia < P->n && P->t[ia] < latest; ++ia) {}
+    int last_before = 0;
+    if (ia >= P->n) { ia = P->n - 1; last_before = 1; }
+    out->t[n] = 0.0; out->cum[n] = 0.0; ++n;
+    if (P->t[0] > 0.0) { ot[no] = 0.0; ov[no] = P->v[0]; ++no; }
+    if (last_before) {
+        for (int i = 0; i < P->n; ++i) { ot[no] = P->t[i]; ov[no] = P->v[i]; ++no; }
+        ot[no] = latest; ov[no] = ov[no - 1]; ++no;
+    } else {
+        for (int i = 0; i < ia; ++i) { ot[no] = P->t[i]; ov[no] = P->v[i]; ++no; }
+        if (!(fabs(ot[no - 1] - latest) < 1e-10)) {
+            ot[no] = latest;
+            ov[no] = interp_y(latest, P->t, P->v, P->n, P->logx, P->logy, 1);
+            ++no;
+        }
+    }
+    for (int i = 1; i < no; ++i) {
+        if (fabs(ov[i] - ov[i - 1]) < 1e-10) {
+            out->t[n] = ot[i];
+            out->cum[n] = out->cum[n - 1] + (ot[i] - ot[i - 1]) * ov[i] * 0.1;  /* MBARLS_TO_PAM3S */
+            ++n;
+        } else {
+            const int steps = 10;
+            double t0 = ot[i - 1], t1 = ot[i], dt = t1 - t0, delta = 1.0 / steps;
+            double lt0 = 0, lt1 = 0, ldt = 0, sub_dt = 0, sub_ldt = 0;
+            if (P->logx) {
+                lt0 = (t0 == 0) ? -99 : log10(t0); lt1 = log10(t1); ldt = lt1 - lt0; sub_ldt = ldt * delta;
+            } else sub_dt = dt * delta;
+            double pv = ov[i - 1], pt = t0;
+            double frac = delta;
+            while (frac < 1.0001) {
+                double et = P->logx ? pow(10.0, lt0 + frac * ldt) : t0 + frac * dt;
+                double ev = interp_y(et, ot, ov, no, P->logx, P->logy, 1);
+                double g;
+                if (!P->logx && !P->logy) g = sub_dt * 0.5 * (pv + ev);
+                else if (P->logx && !P->logy) g = (ev - pv) * (pt - et) / log(et / pt) - pt * pv + et * ev;
+                else if (!P->logx && P->logy) {
+                    double le = (ev > 0) ? log10(ev) : -99, lp = (pt > 0) ? log10(pv) : -99;
+                    g = sub_dt * (ev - pv) * log10(exp(1.0)) / (le - lp);
+                } else {
+                    double le = (ev > 0) ? log10(ev) : -99, lp = (pt > 0) ? log10(pv) : -99;
+                    double m = (le - lp) / sub_ldt;
+                    if (m != -1.0) g = pv / pow(pt, m) / (m + 1.0) * (pow(et, m + 1.0) - pow(pt, m + 1.0));
+                    else g = pt * pv * sub_ldt;
+                }
+                if (n >= cap) { cap *= 2; out->t = (double*)realloc(out->t, sizeof(double) * cap); out->cum = (double*)realloc(out->cum, sizeof(double) * cap); }
+                out->t[n] = et; out->cum[n] = out->cum[n - 1] + g * 0.1; ++n;
+                pv = ev; pt = et;
+                frac += delta;
+            }
+        }
+    }
+    out->n = n;
+    free(ot); free(ov);
+}
+
+/* ------------------------------------------------------- model create -- */
+#define OPT(ptr, i, def) ((ptr) ? (ptr)[i] : (def))
+
+int orc_model_create(const mfg_model_desc* d, orc_model** out, char* err, size_t errlen) {
+    *out = NULL;
+    if (!d || d->abi_version != MFG_ABI_VERSION) { set_err(err, errlen, "bad descriptor version"); return MFG_ERR_INVALID_MODEL; }
+    if (d->n_facets <= 0 || d->n_vertices <= 0 || !d->vertices || !d->facet_vertex_start || !d->facet_vertex_index) {
+        set_err(err, errlen, "empty geometry"); return MFG_ERR_INVALID_MODEL;
+    }
+    orc_model* M = (orc_model*)calloc(1, sizeof(orc_model));
+    M->nf = d->n_facets;
+    M->nstruct = d->n_structures > 0 ? d->n_structures : 1;
+    M->f = (ofacet*)calloc(M->nf, sizeof(ofacet));
+    int nvt = d->facet_vertex_start[M->nf];
+    M->v2 = (double*)malloc(sizeof(double) * 2 * (nvt + 1));
+    M->constant_flow = d->constant_flow; M->use_maxwell = d->use_maxwell;
+    M->low_flux = d->low_flux_mode; M->low_flux_cutoff = d->low_flux_cutoff;
+    M->decay = d->enable_decay; M->half_life = d->half_life; M->gas_mass = d->gas_mass;
+    char msg[256];
+    for (int i = 0; i < M->nf; ++i) {
+        ofacet* F = &M->f[i];
+        F->vstart = d->facet_vertex_start[i];
+        F->nv = d->facet_vertex_start[i + 1] - F->vstart;
+        if (F->nv < 3) { snprintf(msg, sizeof msg, "facet %d has fewer than 3 vertices", i + 1); set_err(err, errlen, msg); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL; }
+        for (int k = 0; k < F->nv; ++k) {
+            int vi = d->facet_vertex_index[F->vstart + k];
+            if (vi < 0 || vi >= d->n_vertices) { set_err(err, errlen, "vertex index out of range"); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL; }
+        }
+        if (facet_basis(F, d->vertices, d->facet_vertex_index + F->vstart, M->v2 + 2 * F->vstart) != 0) {
+            snprintf(msg, sizeof msg, "facet %d is degenerate", i + 1); set_err(err, errlen, msg); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL;
+        }
+        F->sticking = OPT(d->sticking, i, 0.0);
+        F->opacity = OPT(d->opacity, i, 1.0);
+        if (F->opacity < 0) F->opacity = 0; if (F->opacity > 1) F->opacity = 1;   /* clamp (MolflowSimGeom.cpp:148-150) */
+        F->outgassing = OPT(d->outgassing, i, 0.0);
+        F->temperature = OPT(d->temperature, i, 293.15);
+        F->sqrtT = sqrt(F->temperature);
+        F->accommodation = OPT(d->accommodation, i, 1.0);
+        F->desorb_type = OPT(d->desorb_type, i, MFG_DES_NONE);
+        F->desorb_exp = OPT(d->desorb_exponent, i, 0.0);
+        F->diffuse = OPT(d->refl_diffuse, i, 1.0);
+        F->specular = OPT(d->refl_specular, i, 0.0);
+        F->cos_exp = OPT(d->refl_cos_exponent, i, 0.0);
+        F->two_sided = OPT(d->is_2sided, i, 0);
+        F->structure = OPT(d->structure, i, 0);
+        F->link = OPT(d->link_dest, i, 0);
+        F->teleport = OPT(d->teleport_dest, i, 0);
+        F->texw_p = OPT(d->tex_width, i, 0.0);
+        F->texh_p = OPT(d->tex_height, i, 0.0);
+        F->count = OPT(d->count_flags, i, 0u);
+        F->profile_type = OPT(d->profile_type, i, MFG_PROFILE_NONE);
+        F->max_speed = OPT(d->max_speed, i, 0.0);
+        F->am_record = OPT(d->anglemap_record, i, 0);
+        F->am_phi = OPT(d->anglemap_phi_width, i, 0);
+        F->am_limit = OPT(d->anglemap_theta_limit, i, 1.570796326);
+        F->am_lo = OPT(d->anglemap_theta_lower_res, i, 0);
+        F->am_hi = OPT(d->anglemap_theta_higher_res, i, 0);
+        F->p_stick = OPT(d->sticking_param, i, -1);
+        F->p_opac = OPT(d->opacity_param, i, -1);
+        F->p_outg = OPT(d->outgassing_param, i, -1);
+        F->p_temp = OPT(d->temperature_param, i, -1);
+        F->sojourn = OPT(d->enable_sojourn, i, 0);
+        F->soj_freq = OPT(d->sojourn_freq, i, 0.0);
+        F->soj_e = OPT(d->sojourn_e, i, 0.0);
+        if (F->link || F->teleport || OPT(d->is_moving, i, 0) || F->desorb_type == MFG_DES_ANGLEMAP) {
+            snprintf(msg, sizeof msg, "facet %d: link/teleport/moving/angle-map desorption not traced by the oracle", i + 1);
+            set_err(err, errlen, msg); orc_model_destroy(M); return MFG_ERR_UNSUPPORTED_FEATURE;
+        }
+        if (F->structure < -1 || F->structure >= M->nstruct) { set_err(err, errlen, "structure index out of range"); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL; }
+        int textured = (F->texw_p * F->texh_p) > 0;   /* isTextured (LoaderXML.cpp:1111) */
+        if (textured) {
+            F->texw = (int)ceil(F->texw_p - 1e-9); F->texh = (int)ceil(F->texh_p - 1e-9);
+            if (F->texw < 1) F->texw = 1; if (F->texh < 1) F->texh = 1;
+        } else { F->texw = F->texh = 0; F->count = 0; }
+    }
+    /* time-dependent parameters */
+    M->nparams = d->n_params;
+    if (M->nparams > 0) {
+        M->params = (oparam*)calloc(M->nparams, sizeof(oparam));
+        for (int p = 0; p < M->nparams; ++p) {
+            int s = d->param_start[p], e = d->param_start[p + 1];
+            M->params[p].n = e - s;
+            M->params[p].t = (double*)malloc(sizeof(double) * (e - s + 1));
+            M->params[p].v = (double*)malloc(sizeof(double) * (e - s + 1));
+            memcpy(M->params[p].t, d->param_t + s, sizeof(double) * (e - s));
+            memcpy(M->params[p].v, d->param_v + s, sizeof(double) * (e - s));
+            M->params[p].logx = OPT(d->param_log_x, p, 0);
+            M->params[p].logy = OPT(d->param_log_y, p, 0);
+            if (M->params[p].n < 1) { set_err(err, errlen, "empty parameter"); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL; }
+        }
+    }
+    for (int i = 0; i < M->nf; ++i) {
+        ofacet* F = &M->f[i];
+        if (F->p_stick >= M->nparams || F->p_opac >= M->nparams || F->p_outg >= M->nparams || F->p_temp >= M->nparams) {
+            set_err(err, errlen, "facet refers to a missing time-dependent parameter"); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL;
+        }
+    }
+    /* moments and latest moment (PrepareToRun, MolflowSimGeom.cpp:202-206; CalcIntervalCache :255-261) */
+    M->nm = d->n_moments;
+    if (M->nm > 0) {
+        M->mstart = (double*)malloc(sizeof(double) * M->nm);
+        M->mend = (double*)malloc(sizeof(double) * M->nm);
+        M->maxwin = 0;
+        for (int k = 0; k < M->nm; ++k) {
+            M->mstart[k] = d->moment_time[k] - 0.5 * d->moment_window[k];
+            M->mend[k] = d->moment_time[k] + 0.5 * d->moment_window[k];
+            if (d->moment_window[k] > M->maxwin) M->maxwin = d->moment_window[k];
+            if (k > 0 && d->moment_time[k] < d->moment_time[k - 1]) { set_err(err, errlen, "moments must be sorted"); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL; }
+        }
+        M->latest = d->moment_time[M->nm - 1] + 0.5 * d->moment_window[M->nm - 1];
+    } else {
+        M->latest = d->time_window * 0.5;
+    }
+    orc_maxwell_cdf(M->gas_mass, M->cdf_v, M->cdf_p);
+    /* integrated desorption per outgassing parameter */
+    M->ids = (oid*)calloc(M->nparams + 1, sizeof(oid));
+    M->nid = 0;
+    int* pid2id = (int*)malloc(sizeof(int) * (M->nparams + 1));
+    for (int p = 0; p < M->nparams; ++p) pid2id[p] = -1;
+    for (int i = 0; i < M->nf; ++i) {
+        ofacet* F = &M->f[i];
+        F->id_idx = -1;
+        if (F->p_outg >= 0) {
+            if (pid2id[F->p_outg] < 0) { generate_id(&M->params[F->p_outg], M->latest, &M->ids[M->nid]); pid2id[F->p_outg] = M->nid++; }
+            F->id_idx = pid2id[F->p_outg];
+        }
+    }
+    free(pid2id);
+    /* source table: StartFromSource facet weights (Particle.cpp:421-464) */
+    M->src_prefix = (double*)malloc(sizeof(double) * (M->nf + 1));
+    M->src_facet = (int*)malloc(sizeof(int) * (M->nf + 1));
+    M->nsrc = 0;
+    double sum = 0;
+    for (int i = 0; i < M->nf; ++i) {
+        ofacet* F = &M->f[i];
+        if (F->desorb_type == MFG_DES_NONE) continue;
+        double w = (F->id_idx >= 0 ? M->ids[F->id_idx].cum[M->ids[F->id_idx].n - 1] : M->latest * F->outgassing)
+                   / (KB_MOLFLOW * F->temperature);
+        if (!(w > 0)) continue;
+        if (F->structure == -1) { set_err(err, errlen, "a facet in all structures cannot desorb"); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL; }
+        sum += w;
+        M->src_prefix[M->nsrc] = sum; M->src_facet[M->nsrc] = i; M->nsrc++;
+    }
+    M->src_total = sum;
+    /* layout + texture increments (Initializer.cpp:433-456) */
+    mfg_state_layout* L = &M->L;
+    memset(L, 0, sizeof *L);
+    L->n_facets = M->nf; L->n_moments = M->nm;
+    for (int i = 0; i < M->nf; ++i) {
+        ofacet* F = &M->f[i];
+        F->tex_off = -1; F->dir_off = -1; F->ang_off = -1; F->prof_idx = -1;
+        if (F->texw > 0) { F->tex_off = L->texture_cells; L->texture_cells += (long)F->texw * F->texh; }
+        if ((F->count & MFG_COUNT_DIR) && F->texw > 0) { F->dir_off = L->direction_cells; L->direction_cells += (long)F->texw * F->texh; }
+        if (F->profile_type != MFG_PROFILE_NONE) F->prof_idx = (int)L->profile_facets++;
+        if (F->am_record && F->am_phi > 0 && F->am_lo >= 0 && F->am_hi >= 0 && F->am_lo + F->am_hi > 0) { F->ang_off = L->anglemap_cells; L->anglemap_cells += (long)F->am_phi * (F->am_lo + F->am_hi); }
+    }
+    int64_t B = 1 + M->nm;
+    L->n_global = MFG_G_N;
+    L->n_facet_counts = B * M->nf * MFG_FC_N;
+    L->n_facet_sums = B * M->nf * MFG_FS_N;
+    L->n_texture = B * L->texture_cells * 3;
+    L->n_profile = B * L->profile_facets * MFG_PROFILE_SIZE * 3;
+    L->n_direction = B * L->direction_cells * 4;
+    L->n_anglemap = L->anglemap_cells;
+    M->texinc = (double*)calloc(L->texture_cells + 1, sizeof(double));
+    for (int i = 0; i < M->nf; ++i) {
+        ofacet* F = &M->f[i];
+        if (F->texw <= 0) continue;
+        double lu = norm3(F->U), lv = norm3(F->V);
+        double rw = lu / F->texw_p, rh = lv / F->texh_p;
+        double sides = F->two_sided ? 2.0 : 1.0;
+        double* poly = (double*)malloc(sizeof(double) * 2 * F->nv);
+        for (int k = 0; k < F->nv; ++k) { poly[2 * k] = M->v2[2 * (F->vstart + k)] * lu; poly[2 * k + 1] = M->v2[2 * (F->vstart + k) + 1] * lv; }
+        for (int y = 0; y < F->texh; ++y)
+            for (int x = 0; x < F->texw; ++x) {
+                double a = clip_area(poly, F->nv, x * rw, y * rh, (x + 1) * rw, (y + 1) * rh);
+                if (a < 0) a = rw * rh;
+                M->texinc[F->tex_off + (long)y * F->texw + x] = (a > 1e-12 * rw * rh) ? 1.0 / (a * sides) : 0.0;
+            }
+        free(poly);
+    }
+    M->nnodes = (int*)calloc(M->nstruct, sizeof(int));
+    M->nodes = (onode**)calloc(M->nstruct, sizeof(onode*));
+    M->prims = (int**)calloc(M->nstruct, sizeof(int*));
+    for (int s = 0; s < M->nstruct; ++s) build_structure_bvh(M, s);
+    *out = M;
+    return MFG_OK;
+}
+
+void orc_model_destroy(orc_model* M) {
+    if (!M) return;
+    free(M->f); free(M->v2); free(M->texinc);
+    if (M->nodes) for (int s = 0; s < M->nstruct; ++s) { free(M->nodes[s]); free(M->prims[s]); }
+    free(M->nodes); free(M->prims); free(M->nnodes);
+    free(M->mstart); free(M->mend);
+    for (int p = 0; p < M->nparams; ++p) { free(M->params[p].t); free(M->params[p].v); }
+    free(M->params);
+    if (M->ids) for (int k = 0; k < M->nid; ++k) { free(M->ids[k].t); free(M->ids[k].cum); }
+    free(M->ids);
+    free(M->src_prefix); free(M->src_facet);
+    free(M);
+}
+
+int orc_layout(const orc_model* M, mfg_state_layout* out) { *out = M->L; return MFG_OK; }
+
+int orc_facet_geometry(const orc_model* M, double* o18, double* area) {
+    for (int i = 0; i < M->nf; ++i) {
+        const ofacet* F = &M->f[i];
+        double* o = o18 + 18 * i;
+        for (int k = 0; k < 3; ++k) { o[k] = F->O[k]; o[3 + k] = F->U[k]; o[6 + k] = F->V[k]; o[9 + k] = F->N[k]; o[12 + k] = F->nU[k]; o[15 + k] = F->nV[k]; }
+        if (area) area[i] = F->area;
+    }
+    return MFG_OK;
+}
+
+/* ---------------------------------------------------------- intersect -- */
+typedef struct { int facet; double t, u, v; } ohit;
+typedef struct {
+    int hard; double t, u, v;
+    int ntr; ohit tr[MAX_TRANSP];
+    uint64_t nodes, prims;
+} oisect;
+
+static double param_at(const orc_model* M, int p, double t) {
+    const oparam* P = &M->params[p];
+    return interp_y(t, P->t, P->v, P->n, P->logx, P->logy, 0);
+}
+
+/* Ray/facet test: plane hit in front of the ray, (u,v) inside the bounding rectangle,
+ * inside the polygon; back faces of one-sided facets are invisible. */
+static int facet_hit(const orc_model* M, const ofacet* F, const double* o, const double* d, double* t, double* u, double* v) {
+    double den = dot3(F->N, d);
+    if (!F->two_sided && den >= 0.0) return 0;
+    if (den == 0.0) return 0;
+    double tt = (F->planeD - dot3(F->N, o)) / den;
+    if (!(tt > 0.0)) return 0;
+    double p[3] = {o[0] + tt * d[0] - F->O[0], o[1] + tt * d[1] - F->O[1], o[2] + tt * d[2] - F->O[2]};
+    double uu = dot3(p, F->U) * F->invU2;
+    if (uu < 0.0 || uu > 1.0) return 0;
+    double vv = dot3(p, F->V) * F->invV2;
+    if (vv < 0.0 || vv > 1.0) return 0;
+    if (!in_polygon(M->v2 + 2 * F->vstart, F->nv, uu, vv)) return 0;
+    *t = tt; *u = uu; *v = vv;
+    return 1;
+}
+
+static inline int box_hit(const onode* n, const double* o, const double* inv, double tmax) {
+    double t0 = 0.0, t1 = tmax;
+    for (int a = 0; a < 3; ++a) {
+        double ta = (n->bmin[a] - o[a]) * inv[a];
+        double tb = (n->bmax[a] - o[a]) * inv[a];
+        if (ta > tb) { double x = ta; ta = tb; tb = x; }
+        if (ta != ta) ta = -1e300;   /* 0*inf */
+        if (tb != tb) tb = 1e300;
+        if (ta > t0) t0 = ta;
+        if (tb < t1) t1 = tb;
+        if (t0 > t1) return 0;
+    }
+    return 1;
+}
+
+static void intersect(const orc_model* M, int s, const double* o, const double* d, int last, double time,
+                      rng_t* r, uint64_t step, oisect* H) {
+    H->hard = -1; H->t = 1e99; H->ntr = 0;
+    if (M->nnodes[s] == 0) return;
+    double inv[3] = {1.0 / d[0], 1.0 / d[1], 1.0 / d[2]};
+    const onode* nodes = M->nodes[s];
+    const int* prims = M->prims[s];
+    int stack[128], sp = 0;
+    stack[sp++] = 0;
+    while (sp) {
+        const onode* n = &nodes[stack[--sp]];
+        H->nodes++;
+        if (!box_hit(n, o, inv, H->t)) continue;
+        if (n->left < 0) {
+            for (int k = 0; k < n->count; ++k) {
+                int fi = prims[n->first + k];
+                if (fi == last) continue;
+                const ofacet* F = &M->f[fi];
+                H->prims++;
+                double t, u, v;
+                if (!facet_hit(M, F, o, d, &t, &u, &v)) continue;
+                double op = (F->p_opac >= 0) ? param_at(M, F->p_opac, time) : F->opacity;
+                int hard = (op >= 1.0) ? 1 : (op <= 0.0 ? 0 : (rnd_opacity(r, step, fi) < op));
+                if (hard) {
+                    if (t < H->t || (t == H->t && fi < H->hard)) { H->t = t; H->hard = fi; H->u = u; H->v = v; }
+                } else if (H->ntr < MAX_TRANSP) {
+                    H->tr[H->ntr].facet = fi; H->tr[H->ntr].t = t; H->tr[H->ntr].u = u; H->tr[H->ntr].v = v; H->ntr++;
+                }
+            }
+        } else {
+            /* visit the child on the ray's near side first */
+            const onode* L = &nodes[n->left];
+            const onode* R = &nodes[n->right];
+            int ax = 0; double best = -1;
+            for (int a = 0; a < 3; ++a) {
+                double sep = fabs((L->bmin[a] + L->bmax[a]) - (R->bmin[a] + R->bmax[a]));
+                if (sep > best) { best = sep; ax = a; }
+            }
+            int l_first = ((L->bmin[ax] + L->bmax[ax]) < (R->bmin[ax] + R->bmax[ax])) == (d[ax] > 0);
+            if (sp + 2 > 128) continue;
+            if (l_first) { stack[sp++] = n->right; stack[sp++] = n->left; }
+            else { stack[sp++] = n->left; stack[sp++] = n->right; }
+        }
+    }
+}
+
+/* ------------------------------------------------------------- tracer -- */
+typedef struct {
+    double* global;
+    uint64_t* fc;
+    double* fs;
+    double* tex;
+    double* prof;
+    double* dir;
+    uint64_t* ang;
+} otally;
+
+typedef struct {
+    double o[3], d[3];
+    double time, velocity, ori, dist, gen_time, decay_at;
+    int last, structure;
+    uint64_t bounces;
+    double u, v;   /* facetHitDetails of the current facet */
+} opart;
+
+/* moment blocks of time t: all moments whose [start,end) window contains t
+ * (LookupMomentIndex, Particle.cpp:1364-1379, which returns the single window
+ * when windows are disjoint) */
+static int moments_of(const orc_model* M, double t, int* out, int maxn) {
+    if (M->nm == 0) return 0;
+    int hi = lower_index(t, M->mstart, M->nm);   /* last start <= t */
+    int n = 0;
+    for (int k = hi; k >= 0 && M->mstart[k] > t - M->maxwin - 1e-300; --k) {
+        if (M->mstart[k] <= t && t < M->mend[k]) { if (n < maxn) out[n++] = k + 1; }
+    }
+    return n;
+}
+
+static void polar_to_cart(const ofacet* F, double theta, double phi, int reverse, double* out) {
+    double st = sin(theta), ct = cos(theta), sp = sin(phi), cp = cos(phi);
+    double u = st * cp, v = st * sp, n = ct;
+    if (reverse) n = -n;
+    for (int k = 0; k < 3; ++k) out[k] = u * F->nU[k] + v * F->nV[k] + n * F->N[k];
+}
+static void cart_to_polar(const ofacet* F, const double* d, double* theta, double* phi) {
+    double u = dot3(d, F->nU), v = dot3(d, F->nV), n = dot3(d, F->N);
+    if (n > 1) n = 1; if (n < -1) n = -1;
+    *theta = acos(n);
+    *phi = atan2(v, u);
+}
+
+static void add_moment_block(const orc_model* M, otally* T, int m, int fi, double hit, double des, double absn,
+                             double s1v, double svort, const opart* P) {
+    uint64_t* fc = T->fc + ((size_t)m * M->nf + fi) * MFG_FC_N;
+    double* fs = T->fs + ((size_t)m * M->nf + fi) * MFG_FS_N;
+    double he = hit * P->ori;
+    fc[MFG_FC_NBMCHIT] += (uint64_t)hit;
+    fc[MFG_FC_NBDESORBED] += (uint64_t)des;
+    fc[MFG_FC_NBABSORBED] += (uint64_t)absn;
+    fs[MFG_FS_NBHITEQUIV] += he;
+    fs[MFG_FS_NBABSEQUIV] += absn * P->ori;
+    fs[MFG_FS_SUM_1_PER_ORT_VEL] += P->ori * s1v;
+    fs[MFG_FS_SUM_V_ORT] += P->ori * svort;
+    fs[MFG_FS_SUM_1_PER_VELOCITY] += (he + des) / P->velocity;
+}
+/* IncreaseFacetCounter (Particle.cpp:1194-1230) */
+static void facet_counter(const orc_model* M, otally* T, const int* ms, int nms, int fi, double hit, double des,
+                          double absn, double s1v, double svort, const opart* P) {
+    add_moment_block(M, T, 0, fi, hit, des, absn, s1v, svort, P);
+    for (int k = 0; k < nms; ++k) add_moment_block(M, T, ms[k], fi, hit, des, absn, s1v, svort, P);
+}
+/* RecordHitOnTexture (Particle.cpp:978-1004) */
+static void texture_hit(const orc_model* M, otally* T, const int* ms, int nms, const ofacet* F, const opart* P,
+                        int count_hit, double vel_factor, double ort_factor) {
+    long tu = (long)(P->u * F->texw_p), tv = (long)(P->v * F->texh_p);
+    if (tu >= F->texw) tu = F->texw - 1; if (tv >= F->texh) tv = F->texh - 1;
+    if (tu < 0) tu = 0; if (tv < 0) tv = 0;
+    long add = tu + tv * F->texw;
+    double ort = (M->use_maxwell ? 1.0 : 1.1781) * P->velocity * fabs(dot3(P->d, F->N));
+    double inc = M->texinc[F->tex_off + add];
+    for (int k = -1; k < nms; ++k) {
+        int m = (k < 0) ? 0 : ms[k];
+        double* c = T->tex + ((size_t)m * M->L.texture_cells + F->tex_off + add) * 3;
+        if (count_hit) c[0] += P->ori;
+        c[1] += P->ori * ort_factor * ort * inc;
+        c[2] += P->ori * vel_factor / ort;
+    }
+}
+/* RecordDirectionVector (Particle.cpp:1006-1023) */
+static void direction_hit(const orc_model* M, otally* T, const int* ms, int nms, const ofacet* F, const opart* P) {
+    long tu = (long)(P->u * F->texw_p), tv = (long)(P->v * F->texh_p);
+    if (tu >= F->texw) tu = F->texw - 1; if (tv >= F->texh) tv = F->texh - 1;
+    long add = tu + tv * F->texw;
+    for (int k = -1; k < nms; ++k) {
+        int m = (k < 0) ? 0 : ms[k];
+        double* c = T->dir + ((size_t)m * M->L.direction_cells + F->dir_off + add) * 4;
+        for (int a = 0; a < 3; ++a) c[a] += P->ori * P->d[a] * P->velocity;
+        c[3] += 1.0;
+    }
+}
+/* ProfileFacet (Particle.cpp:1026-1085) */
+static void profile_hit(const orc_model* M, otally* T, const int* ms, int nms, const ofacet* F, const opart* P,
+                        int count_hit, double vel_factor, double ort_factor) {
+    if (F->prof_idx < 0) return;
+    int pt = F->profile_type;
+    long pos = -1;
+    int slices = 0;   /* 1: count only; 2: full slice */
+    double dotn = dot3(F->N, P->d);
+    if (count_hit && pt == MFG_PROFILE_ANGULAR) {
+        double theta = acos(fabs(dotn));
+        pos = (long)(theta / (PI_D / 2) * (double)MFG_PROFILE_SIZE);
+        if (pos < 0) pos = 0; if (pos > MFG_PROFILE_SIZE - 1) pos = MFG_PROFILE_SIZE - 1;
+        slices = 1;
+    } else if (pt == MFG_PROFILE_U || pt == MFG_PROFILE_V) {
+        double x = (pt == MFG_PROFILE_U) ? P->u : P->v;
+        pos = (long)(x * (double)MFG_PROFILE_SIZE);
+        if (pos < 0 || pos >= MFG_PROFILE_SIZE) return;
+        slices = 2;
+    } else if (count_hit && (pt == MFG_PROFILE_VELOCITY || pt == MFG_PROFILE_ORT_VELOCITY || pt == MFG_PROFILE_TAN_VELOCITY)) {
+        double dd;
+        if (pt == MFG_PROFILE_VELOCITY) dd = 1.0;
+        else if (pt == MFG_PROFILE_ORT_VELOCITY) dd = fabs(dotn);
+        else dd = sqrt(1 - dotn * dotn);
+        double x = dd * P->velocity / F->max_speed * (double)MFG_PROFILE_SIZE;
+        if (!(x >= 0) || x >= MFG_PROFILE_SIZE) return;
+        pos = (long)x;
+        slices = 1;
+    } else return;
+    double ort = P->velocity * fabs(dotn);
+    for (int k = -1; k < nms; ++k) {
+        int m = (k < 0) ? 0 : ms[k];
+        double* c = T->prof + (((size_t)m * M->L.profile_facets + F->prof_idx) * MFG_PROFILE_SIZE + pos) * 3;
+        if (slices == 1) { c[0] += P->ori; continue; }
+        if (count_hit) c[0] += P->ori;
+        c[2] += P->ori * vel_factor / ort;
+        c[1] += P->ori * ort_factor * (M->use_maxwell ? 1.0 : 1.1781) * ort;
+    }
+}
+/* RecordAngleMap (Particle.cpp:1104-1136) */
+static void anglemap_hit(const orc_model* M, otally* T, const ofacet* F, const opart* P) {
+    if (F->ang_off < 0) return;
+    double th, ph;
+    cart_to_polar(F, P->d, &th, &ph);
+    if (th > PI_D / 2.0) th = fabs(PI_D - th);
+    long ti;
+    if (th < F->am_limit) {
+        if (F->am_lo <= 0) return;
+        ti = (long)(th / F->am_limit * (double)F->am_lo);
+    } else {
+        if (F->am_hi <= 0) return;
+        ti = F->am_lo + (long)((th - F->am_limit) / (PI_D / 2.0 - F->am_limit) * (double)F->am_hi);
+    }
+    long pi = (long)((ph + 3.1415926) / (2.0 * PI_D) * (double)F->am_phi);
+    if (ti >= F->am_lo + F->am_hi) ti = F->am_lo + F->am_hi - 1;
+    if (pi >= F->am_phi) pi = F->am_phi - 1; if (pi < 0) pi = 0;
+    T->ang[F->ang_off + ti * F->am_phi + pi] += 1;
+}
+
+static double maxwell_speed(const orc_model* M, double sqrtT, double r) {
+    return sqrtT * interp_x(r, M->cdf_v, M->cdf_p, MAXWELL_CDF_N, 0, 0, 1);
+}
+static double temperature_at(const orc_model* M, const ofacet* F, double t) {
+    return (F->p_temp >= 0) ? param_at(M, F->p_temp, t) : F->temperature;
+}
+
+/* StartFromSource (Particle.cpp:407-685) for facets without outgassing maps. */
+static int start_from_source(const orc_model* M, otally* T, rng_t* r, opart* P) {
+    double sr = rnd(r) * M->src_total;
+    int lo = 0, hi = M->nsrc;   /* first k with prefix[k] > sr */
+    while (lo < hi) { int mid = (lo + hi) >> 1; if (M->src_prefix[mid] > sr) hi = mid; else lo = mid + 1; }
+    if (lo >= M->nsrc) return 0;
+    int fi = M->src_facet[lo];
+    const ofacet* F = &M->f[fi];
+    int reverse = F->two_sided ? (rnd(r) > 0.5) : 0;
+    P->last = fi;
+    if (F->id_idx >= 0) {
+        const oid* I = &M->ids[F->id_idx];
+        P->time = interp_x(rnd(r) * I->cum[I->n - 1], I->t, I->cum, I->n, 0, 0, 1);
+    } else P->time = rnd(r) * M->latest;
+    P->gen_time = P->time;
+    if (M->use_maxwell) P->velocity = maxwell_speed(M, F->sqrtT, rnd(r));
+    else P->velocity = 145.469 * sqrt(F->temperature / M->gas_mass);
+    P->ori = 1.0;
+    if (M->decay) {
+        double tau = 1.44269 * M->half_life;
+        P->decay_at = P->time - tau * log(1.0 - rnd(r));
+    } else P->decay_at = 1e100;
+    P->bounces = 0; P->dist = 0;
+    int found = 0;
+    for (int tries = 0; tries < 1000 && !found; ++tries) {
+        double u = rnd(r), v = rnd(r);
+        if (in_polygon(M->v2 + 2 * F->vstart, F->nv, u, v)) {
+            for (int k = 0; k < 3; ++k) P->o[k] = F->O[k] + u * F->U[k] + v * F->V[k];
+            P->u = u; P->v = v; found = 1;
+        }
+    }
+    if (!found) { P->u = 0.5; P->v = 0.5; for (int k = 0; k < 3; ++k) P->o[k] = F->center[k]; }
+    double th, ph;
+    switch (F->desorb_type) {
+        case MFG_DES_UNIFORM: th = acos(rnd(r)); ph = rnd(r) * 2.0 * PI_D; break;
+        case MFG_DES_COSINE_N: th = acos(pow(rnd(r), 1.0 / (F->desorb_exp + 1.0))); ph = rnd(r) * 2.0 * PI_D; break;
+        default: th = acos(sqrt(rnd(r))); ph = rnd(r) * 2.0 * PI_D; break;
+    }
+    polar_to_cart(F, th, ph, reverse, P->d);
+    P->structure = F->structure;
+    T->global[MFG_G_NBDESORBED] += 1.0;
+    double ort = P->velocity * fabs(dot3(P->d, F->N));
+    int ms[256]; int nms = moments_of(M, P->time, ms, 256);
+    facet_counter(M, T, ms, nms, fi, 0, 1, 0, 2.0 / ort, (M->use_maxwell ? 1.0 : 1.1781) * ort, P);
+    profile_hit(M, T, ms, nms, F, P, 0, 2.0, 1.0);
+    if (F->count & MFG_COUNT_DES) texture_hit(M, T, ms, nms, F, P, 1, 2.0, 1.0);
+    return 1;
+}
+
+/* RegisterTransparentPass (Particle.cpp:1232-1257) */
+static void transparent_pass(const orc_model* M, otally* T, int fi, const ohit* h, opart* P) {
+    const ofacet* F = &M->f[fi];
+    double df = fabs(dot3(P->d, F->N));
+    int ms[256]; int nms = moments_of(M, P->time + h->t / 100.0 / P->velocity, ms, 256);
+    double su = P->u, sv = P->v;
+    P->u = h->u; P->v = h->v;
+    facet_counter(M, T, ms, nms, fi, 1, 0, 0, 2.0 / (P->velocity * df),
+                  2.0 * (M->use_maxwell ? 1.0 : 1.1781) * P->velocity * df, P);
+    if (F->count & MFG_COUNT_TRANS) texture_hit(M, T, ms, nms, F, P, 1, 2.0, 2.0);
+    if ((F->count & MFG_COUNT_DIR) && F->dir_off >= 0) direction_hit(M, T, ms, nms, F, P);
+    profile_hit(M, T, ms, nms, F, P, 1, 2.0, 2.0);
+    if (F->ang_off >= 0) anglemap_hit(M, T, F, P);
+    P->u = su; P->v = sv;
+}
+
+/* RecordAbsorb (Particle.cpp:888-924) */
+static void record_absorb(const orc_model* M, otally* T, int fi, opart* P) {
+    const ofacet* F = &M->f[fi];
+    T->global[MFG_G_NBMCHIT] += 1; T->global[MFG_G_NBHITEQUIV] += P->ori; T->global[MFG_G_NBABSEQUIV] += P->ori;
+    int ms[256]; int nms = moments_of(M, P->time, ms, 256);
+    double ort = P->velocity * fabs(dot3(P->d, F->N));
+    facet_counter(M, T, ms, nms, fi, 1, 0, 1, 2.0 / ort, (M->use_maxwell ? 1.0 : 1.1781) * ort, P);
+    profile_hit(M, T, ms, nms, F, P, 1, 2.0, 1.0);
+    if (F->ang_off >= 0) anglemap_hit(M, T, F, P);
+    if (F->count & MFG_COUNT_ABS) texture_hit(M, T, ms, nms, F, P, 1, 2.0, 1.0);
+    if ((F->count & MFG_COUNT_DIR) && F->dir_off >= 0) direction_hit(M, T, ms, nms, F, P);
+}
+
+/* UpdateVelocity (Particle.cpp:1138-1163) */
+static void update_velocity(const orc_model* M, const ofacet* F, rng_t* r, opart* P) {
+    double temp = temperature_at(M, F, P->time);
+    double sqrtT = (F->p_temp < 0) ? F->sqrtT : sqrt(temp);
+    if (F->accommodation > 0.9999) {
+        if (M->use_maxwell) P->velocity = maxwell_speed(M, sqrtT, rnd(r));
+        else P->velocity = 145.469 * sqrtT / M->gas_mass;   /* reference quirk kept (Particle.cpp:1152) */
+    } else {
+        double old2 = P->velocity * P->velocity, new2;
+        if (M->use_maxwell) { double v = maxwell_speed(M, sqrtT, rnd(r)); new2 = v * v; }
+        else new2 = 29369.939 * (temp / M->gas_mass);
+        P->velocity = sqrt(old2 + (new2 - old2) * F->accommodation);
+    }
+}
+
+/* PerformBounce (Particle.cpp:691-838), no link/moving facets */
+static void perform_bounce(const orc_model* M, otally* T, int fi, rng_t* r, opart* P) {
+    const ofacet* F = &M->f[fi];
+    T->global[MFG_G_NBMCHIT] += 1; T->global[MFG_G_NBHITEQUIV] += P->ori;
+    int revert = F->two_sided ? (dot3(P->d, F->N) > 0.0) : 0;
+    double ort = P->velocity * fabs(dot3(P->d, F->N));
+    double vf = M->use_maxwell ? 1.0 : 1.1781;
+    int ms[256]; int nms = moments_of(M, P->time, ms, 256);
+    facet_counter(M, T, ms, nms, fi, 1, 0, 0, 1.0 / ort, vf * ort, P);
+    P->bounces++;
+    if (F->count & MFG_COUNT_REFL) texture_hit(M, T, ms, nms, F, P, 1, 1.0, 1.0);
+    if ((F->count & MFG_COUNT_DIR) && F->dir_off >= 0) direction_hit(M, T, ms, nms, F, P);
+    profile_hit(M, T, ms, nms, F, P, 1, 1.0, 1.0);
+    if (F->ang_off >= 0) anglemap_hit(M, T, F, P);
+    update_velocity(M, F, r, P);
+    if (F->sojourn) {
+        double A = exp(-F->soj_e / (8.31 * temperature_at(M, F, P->time)));
+        P->time += -log(1.0 - rnd(r)) / (A * F->soj_freq);
+        nms = moments_of(M, P->time, ms, 256);
+    }
+    if (F->diffuse > 0.999999) {
+        double th = acos(sqrt(rnd(r))); double ph = rnd(r) * 2.0 * PI_D;
+        polar_to_cart(F, th, ph, revert, P->d);
+    } else {
+        double rt = rnd(r);
+        if (rt < F->diffuse) {
+            double th = acos(sqrt(rnd(r))); double ph = rnd(r) * 2.0 * PI_D;
+            polar_to_cart(F, th, ph, revert, P->d);
+        } else if (rt < F->diffuse + F->specular) {
+            double th, ph; cart_to_polar(F, P->d, &th, &ph);
+            polar_to_cart(F, PI_D - th, ph, 0, P->d);
+        } else {
+            double th = acos(pow(rnd(r), 1.0 / (F->cos_exp + 1.0))); double ph = rnd(r) * 2.0 * PI_D;
+            polar_to_cart(F, th, ph, revert, P->d);
+        }
+    }
+    ort = P->velocity * fabs(dot3(P->d, F->N));
+    facet_counter(M, T, ms, nms, fi, 0, 0, 0, 1.0 / ort, vf * ort, P);
+    if (F->count & MFG_COUNT_REFL) texture_hit(M, T, ms, nms, F, P, 0, 1.0, 1.0);
+    profile_hit(M, T, ms, nms, F, P, 0, 1.0, 1.0);
+    P->last = fi;
+}
+
+typedef struct { otally T; orc_stats st; } othread;
+
+static void tally_alloc(const orc_model* M, otally* T) {
+    const mfg_state_layout* L = &M->L;
+    T->global = (double*)calloc(L->n_global, sizeof(double));
+    T->fc = (uint64_t*)calloc(L->n_facet_counts + 1, sizeof(uint64_t));
+    T->fs = (double*)calloc(L->n_facet_sums + 1, sizeof(double));
+    T->tex = (double*)calloc(L->n_texture + 1, sizeof(double));
+    T->prof = (double*)calloc(L->n_profile + 1, sizeof(double));
+    T->dir = (double*)calloc(L->n_direction + 1, sizeof(double));
+    T->ang = (uint64_t*)calloc(L->n_anglemap + 1, sizeof(uint64_t));
+}
+static void tally_free(otally* T) {
+    free(T->global); free(T->fc); free(T->fs); free(T->tex); free(T->prof); free(T->dir); free(T->ang);
+}
+
+/* trace one particle to absorption/leak: the body of SimulationMCStep (Particle.cpp:221-393) */
+static int trace_particle(const orc_model* M, otally* T, rng_t* r, uint64_t max_steps, orc_stats* st,
+                          int64_t* nrec, int64_t maxrec, double* ro, double* rd, int32_t* rl, int32_t* rh, double* rt) {
+    opart P;
+    if (!start_from_source(M, T, r, &P)) return -1;
+    st->desorbed++;
+    oisect H;
+    for (uint64_t step = 0;; ++step) {
+        if (step >= max_steps) { st->dropped++; return 0; }
+        H.nodes = 0; H.prims = 0;
+        intersect(M, P.structure, P.o, P.d, P.last, P.time, r, step, &H);
+        st->rays++; st->node_visits += H.nodes; st->prim_tests += H.prims;
+        if (nrec && *nrec < maxrec) {
+            int64_t k = (*nrec)++;
+            for (int a = 0; a < 3; ++a) { ro[3 * k + a] = P.o[a]; rd[3 * k + a] = P.d[a]; }
+            rl[k] = P.last; rh[k] = H.hard; rt[k] = H.t;
+        }
+        if (H.hard < 0) {
+            T->global[MFG_G_NBLEAK] += 1; st->leaks++;
+            return 0;
+        }
+        int fi = H.hard;
+        const ofacet* F = &M->f[fi];
+        double travel = H.t;
+        int event = 0;   /* 0 facet hit, 1 overtime, 2 decay */
+        if (!M->constant_flow) {
+            double dl = P.velocity * 100.0 * (M->latest - P.time);
+            if (dl < travel) { travel = dl; event = 1; }
+        }
+        if (M->decay) {
+            double dd = P.velocity * 100.0 * (P.decay_at - P.time);
+            if (dd < travel) { travel = dd; event = 2; }
+        }
+        for (int k = 0; k < H.ntr; ++k)
+            if (H.tr[k].t < travel) transparent_pass(M, T, H.tr[k].facet, &H.tr[k], &P);
+        for (int a = 0; a < 3; ++a) P.o[a] = P.o[a] + travel * P.d[a];
+        P.time += travel / 100.0 / P.velocity;
+        if (event != 0) {
+            T->global[MFG_G_DIST_TOTAL] += travel;
+            return 0;
+        }
+        T->global[MFG_G_DIST_TOTAL] += travel; T->global[MFG_G_DIST_FULLHITS] += travel; P.dist += travel;
+        P.u = H.u; P.v = H.v;
+        double s = (F->p_stick >= 0) ? param_at(M, F->p_stick, P.time) : F->sticking;
+        if (!M->low_flux) {
+            if (s == 1.0 || (s > 0.0 && rnd(r) < s)) { record_absorb(M, T, fi, &P); st->hits++; return 0; }
+            perform_bounce(M, T, fi, r, &P); st->hits++;
+        } else {
+            st->hits++;
+            if (s > 0.0) {
+                double before = P.ori;
+                P.ori *= s;
+                record_absorb(M, T, fi, &P);
+                P.ori = before * (1.0 - s);
+            } else P.ori *= (1.0 - s);
+            if (P.ori > M->low_flux_cutoff) perform_bounce(M, T, fi, r, &P);
+            else return 0;
+        }
+    }
+}
+
+static double now_s(void) {
+    struct timespec ts; clock_gettime(CLOCK_MONOTONIC, &ts);
+    return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+int orc_run(orc_model* M, uint64_t n_des, const orc_run_opts* o, mfg_state_view* view, orc_stats* st) {
+    if (M->nsrc == 0) return MFG_ERR_NO_SOURCE;
+    int nt = o->n_threads;
+#ifdef _OPENMP
+    if (nt <= 0) nt = omp_get_max_threads();
+#else
+    nt = 1;
+#endif
+    uint64_t max_steps = o->max_steps ? o->max_steps : ((uint64_t)1 << 40);
+    othread* th = (othread*)calloc(nt, sizeof(othread));
+    double t0 = now_s();
+    int err = 0;
+#pragma omp parallel num_threads(nt)
+    {
+        int tid = 0;
+#ifdef _OPENMP
+        tid = omp_get_thread_num();
+#endif
+        othread* me = &th[tid];
+        tally_alloc(M, &me->T);
+        rng_t r; memset(&r, 0, sizeof r);
+        r.mode = o->rng_mode;
+        r.key[0] = (uint32_t)o->seed; r.key[1] = (uint32_t)(o->seed >> 32);
+        if (r.mode == ORC_RNG_MT) mt_seed(&r.mt, 42424242u + (uint32_t)tid);
+#pragma omp for schedule(dynamic, 256)
+        for (long long i = 0; i < (long long)n_des; ++i) {
+            rng_start_particle(&r, o->first_particle + (uint64_t)i);
+            if (trace_particle(M, &me->T, &r, max_steps, &me->st, NULL, 0, NULL, NULL, NULL, NULL, NULL) < 0) err = 1;
+        }
+    }
+    double t1 = now_s();
+    /* reduce into the view (GlobalSimuState::operator+=, MolflowSimGeom.cpp:452-458) */
+    const mfg_state_layout* L = &M->L;
+    memset(st, 0, sizeof *st);
+    for (int t = 0; t < nt; ++t) {
+        otally* T = &th[t].T;
+        if (view->global) for (int64_t k = 0; k < L->n_global; ++k) view->global[k] += T->global[k];
+        if (view->facet_counts) for (int64_t k = 0; k < L->n_facet_counts; ++k) view->facet_counts[k] += T->fc[k];
+        if (view->facet_sums) for (int64_t k = 0; k < L->n_facet_sums; ++k) view->facet_sums[k] += T->fs[k];
+        if (view->texture) for (int64_t k = 0; k < L->n_texture; ++k) view->texture[k] += T->tex[k];
+        if (view->profile) for (int64_t k = 0; k < L->n_profile; ++k) view->profile[k] += T->prof[k];
+        if (view->direction) for (int64_t k = 0; k < L->n_direction; ++k) view->direction[k] += T->dir[k];
+        if (view->anglemap) for (int64_t k = 0; k < L->n_anglemap; ++k) view->anglemap[k] += T->ang[k];
+        st->desorbed += th[t].st.desorbed; st->hits += th[t].st.hits; st->leaks += th[t].st.leaks;
+        st->dropped += th[t].st.dropped; st->rays += th[t].st.rays;
+        st->node_visits += th[t].st.node_visits; st->prim_tests += th[t].st.prim_tests;
+        tally_free(T);
+    }
+    st->seconds = t1 - t0;
+    st->threads = nt;
+    free(th);
+    return err ? MFG_ERR_NO_SOURCE : MFG_OK;
+}
+
+int orc_replay(orc_model* M, int64_t n, const double* origin, const double* dir, const int32_t* last,
+               int32_t* hit_facet, double* hit_t, orc_stats* st) {
+    uint64_t nodes = 0, prims = 0;
+#pragma omp parallel for reduction(+:nodes, prims) schedule(static)
+    for (long long i = 0; i < (long long)n; ++i) {
+        oisect H; H.nodes = 0; H.prims = 0;
+        rng_t r; memset(&r, 0, sizeof r);
+        intersect(M, 0, origin + 3 * i, dir + 3 * i, last[i], 0.0, &r, 0, &H);
+        hit_facet[i] = H.hard; hit_t[i] = (H.hard >= 0) ? H.t : -1.0;
+        nodes += H.nodes; prims += H.prims;
+    }
+    if (st) { memset(st, 0, sizeof *st); st->rays = n; st->node_visits = nodes; st->prim_tests = prims; }
+    return MFG_OK;
+}
+
+int64_t orc_record_rays(orc_model* M, uint64_t n_des, uint64_t seed, int64_t max_rays,
+                        double* origin, double* dir, int32_t* last, int32_t* hit_facet, double* hit_t) {
+    otally T; tally_alloc(M, &T);
+    orc_stats st; memset(&st, 0, sizeof st);
+    rng_t r; memset(&r, 0, sizeof r);
+    r.key[0] = (uint32_t)seed; r.key[1] = (uint32_t)(seed >> 32);
+    int64_t nrec = 0;
+    for (uint64_t i = 0; i < n_des && nrec < max_rays; ++i) {
+        rng_start_particle(&r, i);
+        trace_particle(M, &T, &r, (uint64_t)1 << 40, &st, &nrec, max_rays, origin, dir, last, hit_facet, hit_t);
+    }
+    tally_free(&T);
+    return nrec;
+}

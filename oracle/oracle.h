@@ -1,0 +1,77 @@
+/*
+ * oracle.h — CPU FP64 restatement of MolFlow+'s test-particle tracer.
+ *
+ * TEST INFRASTRUCTURE.  This code is the checker for the GB300 library: only the
+ * tests, the smoke check and bench.py's CPU-baseline leg may load it.  The product
+ * path never calls it.
+ *
+ * It restates, in plain C with OpenMP (one tracer per thread, as
+ * src/Simulation/MolflowSimulation.cpp:44-55), the algorithm of
+ *   src/Simulation/Particle.cpp:207-1379   (SimulationMCStep and the Record* tallies)
+ *   src/Simulation/Physics.cpp:6-19         (Maxwell speed, desorption time)
+ *   src/Simulation/CDFGeneration.cpp:54-83  (Maxwell CDF)
+ *   src/Simulation/IDGeneration.cpp:45-207  (integrated desorption)
+ *   src/Simulation/MolflowSimGeom.cpp:194-335 (PrepareToRun, CalcTotalOutgassing)
+ *   src/Simulation/SimulationMC.cpp:15-40   (time-dependent sticking/opacity/temperature)
+ * plus the geometry primitives that live in the (absent) src_shared submodule,
+ * restated from their observable contract: facet (O,U,V,N) basis, crossing-number
+ * point-in-polygon, SAH BVH with 2 facets per leaf, ray/facet intersection that
+ * skips the last hit facet and back faces of one-sided facets.
+ *
+ * Parity status: pinned statistically against the reference's stored converged
+ * states (tests/TestCases/B01, B02, 01 via tests/golden); bit-level parity with
+ * the reference is unpinned because its RNG and intersection code are absent.
+ */
+#ifndef MFG_ORACLE_H
+#define MFG_ORACLE_H
+
+#include "../include/mfg.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_model orc_model;
+
+#define ORC_RNG_PHILOX 0   /* Philox4x32-10 stream per particle (same streams as the GPU kernels) */
+#define ORC_RNG_MT     1   /* MT19937 per thread seeded 42424242+thread (MolflowSimulation.cpp:50) */
+
+typedef struct orc_run_opts {
+    uint64_t seed;
+    uint64_t first_particle;   /* particle id of the first desorption (Philox counter) */
+    int32_t  n_threads;        /* 0 = all cores */
+    int32_t  rng_mode;         /* ORC_RNG_* */
+    uint64_t max_steps;        /* bounce cap per particle, 0 = 2^40 */
+} orc_run_opts;
+
+typedef struct orc_stats {
+    uint64_t desorbed, hits, leaks, dropped;
+    uint64_t rays;             /* Intersect calls */
+    uint64_t node_visits;      /* BVH nodes whose box was tested */
+    uint64_t prim_tests;       /* facet intersection tests */
+    double   seconds;
+    int32_t  threads;
+} orc_stats;
+
+int  orc_model_create(const mfg_model_desc* desc, orc_model** out, char* err, size_t errlen);
+void orc_model_destroy(orc_model* m);
+int  orc_layout(const orc_model* m, mfg_state_layout* out);
+/* derived facet basis: O,U,V,N,nU,nV (18 doubles per facet) and area */
+int  orc_facet_geometry(const orc_model* m, double* out18, double* area);
+/* Simulate n_des particles and ADD the tallies into view (like UpdateMCHits). */
+int  orc_run(orc_model* m, uint64_t n_des, const orc_run_opts* o, mfg_state_view* view, orc_stats* st);
+/* Intersect given rays (replay mode). */
+int  orc_replay(orc_model* m, int64_t n, const double* origin, const double* dir, const int32_t* last,
+                int32_t* hit_facet, double* hit_t, orc_stats* st);
+/* Record the first max_rays rays traced by a Philox run (origin, direction, last facet, hit facet, t). */
+int64_t orc_record_rays(orc_model* m, uint64_t n_des, uint64_t seed, int64_t max_rays,
+                        double* origin, double* dir, int32_t* last, int32_t* hit_facet, double* hit_t);
+/* Philox4x32-10 block for tests: out[4] from counter[4], key[2]. */
+void orc_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+/* Maxwell CDF at 1 K (100 entries of speed, cumulative probability). */
+void orc_maxwell_cdf(double gas_mass, double* speed, double* cumul);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
