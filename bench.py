@@ -167,6 +167,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=os.environ.get("MFG_BENCH_WORKLOAD", "c2"), choices=list(WORKLOADS))
     ap.add_argument("--step-desorptions", type=int, default=0)
+    ap.add_argument("--fp64-step", type=int, default=0)
     ap.add_argument("--ref-step-s", type=float, default=6.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -201,12 +202,12 @@ def main():
             dist.barrier()
 
     # plain FP64 kernel on the same workload (smaller batch; hits/s is a rate)
-    for _ in range(1):
-        sim.SimulationMCStep(W["fp64_step"] // 10, precision=A.PREC_FP64, seed=seed)
+    fp64_step = args.fp64_step or W["fp64_step"]
+    sim.SimulationMCStep(max(1, fp64_step // 10), precision=A.PREC_FP64, seed=seed)
     f64_ms = 0.0
     f64_hits = 0
     for _ in range(2):
-        sim.SimulationMCStep(W["fp64_step"], precision=A.PREC_FP64, seed=seed)
+        sim.SimulationMCStep(fp64_step, precision=A.PREC_FP64, seed=seed)
         f64_ms += sim.last_stats["kernel_ms"]
         f64_hits += sim.last_stats["hits"]
     fp64_rate = f64_hits / (f64_ms / 1e3)

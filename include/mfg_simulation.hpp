@@ -1,0 +1,133 @@
+// mfg_simulation.hpp — C++ host adapter over the C ABI (include/mfg.h).
+//
+// GpuSimulation offers the surface molflowCLI's thread controller uses on
+// MolflowSimulation (src/Simulation/MolflowSimulation.h:22-45) and on each
+// MFSim::ParticleTracer (src/Simulation/Particle.h:45,86): load a model, reset,
+// step a number of desorptions, and add the results into a GlobalSimuState-shaped
+// container under a timed lock (UpdateHitsAndLog, src/Simulation/Particle.cpp:21-73,
+// 1294-1312).  Header-only; link against libmfg.so.  Errors are reported as
+// return codes from the ABI and raised here as mfg::Error.
+#pragma once
+#include <chrono>
+#include <cstdint>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "mfg.h"
+
+namespace mfg {
+
+class Error : public std::runtime_error {
+public:
+    Error(int code, const std::string& what) : std::runtime_error(what), code(code) {}
+    int code;
+};
+
+inline std::string last_error() {
+    char buf[1024];
+    mfg_last_error(buf, sizeof buf);
+    return buf;
+}
+inline void check(int rc) {
+    if (rc != MFG_OK) throw Error(rc, last_error());
+}
+
+// MCStepResult of the reference (src/Simulation/Particle.h:24-28)
+enum class MCStepResult { Success, DesorptionError, MaxReached };
+
+// GlobalSimuState-shaped tallies in host memory (src/Simulation/MolflowSimGeom.h:56-154)
+struct HostState {
+    mfg_state_layout layout{};
+    std::vector<double> global;
+    std::vector<uint64_t> facet_counts;
+    std::vector<double> facet_sums, texture, profile, direction;
+    std::vector<uint64_t> anglemap;
+    std::timed_mutex mutex;   // simuStateMutex
+
+    void resize(const mfg_state_layout& L) {
+        layout = L;
+        global.assign(size_t(L.n_global), 0.0);
+        facet_counts.assign(size_t(L.n_facet_counts), 0);
+        facet_sums.assign(size_t(L.n_facet_sums), 0.0);
+        texture.assign(size_t(L.n_texture), 0.0);
+        profile.assign(size_t(L.n_profile), 0.0);
+        direction.assign(size_t(L.n_direction), 0.0);
+        anglemap.assign(size_t(L.n_anglemap), 0);
+    }
+    mfg_state_view view() {
+        return mfg_state_view{global.data(), facet_counts.data(), facet_sums.data(), texture.data(),
+                              profile.data(), direction.data(), anglemap.data()};
+    }
+    // GlobalSimuState::operator+= (src/Simulation/MolflowSimGeom.cpp:452-458)
+    HostState& operator+=(const HostState& o) {
+        for (size_t i = 0; i < global.size(); ++i) global[i] += o.global[i];
+        for (size_t i = 0; i < facet_counts.size(); ++i) facet_counts[i] += o.facet_counts[i];
+        for (size_t i = 0; i < facet_sums.size(); ++i) facet_sums[i] += o.facet_sums[i];
+        for (size_t i = 0; i < texture.size(); ++i) texture[i] += o.texture[i];
+        for (size_t i = 0; i < profile.size(); ++i) profile[i] += o.profile[i];
+        for (size_t i = 0; i < direction.size(); ++i) direction[i] += o.direction[i];
+        for (size_t i = 0; i < anglemap.size(); ++i) anglemap[i] += o.anglemap[i];
+        return *this;
+    }
+};
+
+class GpuSimulation {
+public:
+    explicit GpuSimulation(int device = 0) : device_(device) {}
+    ~GpuSimulation() { release(); }
+    GpuSimulation(const GpuSimulation&) = delete;
+    GpuSimulation& operator=(const GpuSimulation&) = delete;
+
+    // LoadSimulation (MolflowSimulation.cpp:92-154): prepare geometry, BVH, tables; upload.
+    void LoadSimulation(const mfg_model_desc& desc) {
+        release();
+        check(mfg_model_create(&desc, &model_));
+        check(mfg_sim_create(model_, device_, &sim_));
+        check(mfg_state_layout_of(model_, &layout_));
+    }
+    void ResetSimulation() { check(mfg_reset(sim_)); }
+    const mfg_state_layout& layout() const { return layout_; }
+
+    // SimulationMCStep: desorb and trace nbDesorptions particles (Particle.cpp:207-396).
+    MCStepResult SimulationMCStep(uint64_t nbDesorptions, const mfg_run_options& opt, mfg_run_stats* stats = nullptr) {
+        mfg_run_stats st{};
+        int rc = mfg_run(sim_, nbDesorptions, &opt, &st);
+        if (stats) *stats = st;
+        if (rc == MFG_ERR_NO_SOURCE) return MCStepResult::DesorptionError;
+        check(rc);
+        return MCStepResult::Success;
+    }
+
+    // UpdateHitsAndLog: add the tallies into the global state under its timed lock, then clear them.
+    bool UpdateHitsAndLog(HostState& global, size_t timeout_ms) {
+        HostState local;
+        local.resize(layout_);
+        mfg_state_view v = local.view();
+        check(mfg_fetch(sim_, &v));
+        std::unique_lock<std::timed_mutex> lk(global.mutex, std::defer_lock);
+        if (!lk.try_lock_for(std::chrono::milliseconds(timeout_ms))) return false;   // GetHitLock timeout
+        if (global.global.empty()) global.resize(layout_);
+        global += local;
+        lk.unlock();
+        check(mfg_reset(sim_));
+        return true;
+    }
+
+    mfg_sim* handle() const { return sim_; }
+
+private:
+    void release() {
+        if (sim_) mfg_sim_destroy(sim_);
+        if (model_) mfg_model_destroy(model_);
+        sim_ = nullptr;
+        model_ = nullptr;
+    }
+    int device_;
+    mfg_model* model_ = nullptr;
+    mfg_sim* sim_ = nullptr;
+    mfg_state_layout layout_{};
+};
+
+}  // namespace mfg

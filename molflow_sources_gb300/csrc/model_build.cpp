@@ -654,7 +654,18 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
             r[12 + a] = F.V[a] / v2;
         }
         r[3] = F.N[0] * F.O[0] + F.N[1] * F.O[1] + F.N[2] * F.O[2];
-        for (int k = 0; k < 16; ++k) m.isect_f[i].v[k] = float(r[k]);
+        // FP32 copy: [N | O hi/lo split | U/|U|^2 | V/|V|^2] (origin-relative FP32 facet test)
+        float* q = m.isect_f[i].v;
+        for (int k = 0; k < 16; ++k) q[k] = 0.0f;
+        for (int a = 0; a < 3; ++a) {
+            q[a] = float(r[a]);
+            q[8 + a] = float(r[8 + a]);
+            q[12 + a] = float(r[12 + a]);
+            q[4 + a] = float(F.O[a]);
+        }
+        q[3] = float(F.O[0] - double(q[4]));
+        q[7] = float(F.O[1] - double(q[5]));
+        q[11] = float(F.O[2] - double(q[6]));
         // circle shortcut for the point-in-polygon test
         double su = std::sqrt(u2), sv = std::sqrt(v2);
         const double* pv = &m.v2[2 * size_t(F.vstart)];

@@ -43,8 +43,10 @@ __device__ __forceinline__ double u01d(uint32_t a, uint32_t b) {
     uint64_t m = ((((uint64_t)a) << 32) | b) >> 12;
     return __longlong_as_double((long long)(0x3FF0000000000000ull | m)) - 1.0;
 }
+// uniform float in (0,1): (k + 1/2) * 2^-23; never 0, so cos(theta) = sqrt(u) never
+// gives a direction lying in the facet plane
 __device__ __forceinline__ float u01f(uint32_t a) {
-    return __uint_as_float(0x3F800000u | (a >> 9)) - 1.0f;
+    return (__uint_as_float(0x3F800000u | (a >> 9)) - 1.0f) + 5.9604645e-8f;
 }
 
 // double stream: two uniforms per Philox block (the CPU oracle's order)
@@ -276,14 +278,30 @@ __device__ __forceinline__ bool edge_inside_f(const DevModel& M, const PolyF& P,
     return in;
 }
 
-__device__ __noinline__ HitF trace_f(const DevModel& M, int root, float ox, float oy, float oz,
-                                     float dx, float dy, float dz, int last, float eps_num, bool& ambiguous,
+// Ray for the FP32 traversal: origin split into hi + lo floats so that O - o is
+// formed to ~1e-7 of its own size, whatever the absolute coordinates.
+struct RayF {
+    float ohx, ohy, ohz, olx, oly, olz;
+    float dx, dy, dz;
+};
+__device__ __forceinline__ RayF make_ray_f(double ox, double oy, double oz, float dx, float dy, float dz) {
+    RayF r;
+    r.ohx = (float)ox; r.ohy = (float)oy; r.ohz = (float)oz;
+    r.olx = (float)(ox - (double)r.ohx); r.oly = (float)(oy - (double)r.ohy); r.olz = (float)(oz - (double)r.ohz);
+    r.dx = dx; r.dy = dy; r.dz = dz;
+    return r;
+}
+
+// FacetIsectF layout: [N0 N1 N2 Olo0 | Ohi0 Ohi1 Ohi2 Olo1 | Us0 Us1 Us2 Olo2 | Vs0 Vs1 Vs2 -]
+__device__ __noinline__ HitF trace_f(const DevModel& M, int root, const RayF& ray, int last, bool& ambiguous,
                                      unsigned long long* status) {
     HitF h;
     h.f = -1;
     h.t = 3.0e38f;
     h.u = h.v = 0;
     float htol = 0.0f;    // error bound of h.t
+    const float dx = ray.dx, dy = ray.dy, dz = ray.dz;
+    const float ox = ray.ohx, oy = ray.ohy, oz = ray.ohz;
     float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
     int stack[kStack];
     int sp = 0;
@@ -311,25 +329,29 @@ __device__ __noinline__ HitF trace_f(const DevModel& M, int root, float ox, floa
                 int f = M.prims[nd.a + k];
                 if (f == last) continue;
                 const FacetIsectF& R = M.isect_f[f];
-                float Nx = R.v[0], Ny = R.v[1], Nz = R.v[2], D = R.v[3];
+                float Nx = R.v[0], Ny = R.v[1], Nz = R.v[2];
                 float den = Nx * dx + Ny * dy + Nz * dz;
                 bool two = (M.info[f].flags & FF_TWO_SIDED) != 0;
                 float aden = fabsf(den);
-                // back-face culling is exact for |den| well above its rounding error
-                if (!two && den >= 0.0f) {
-                    if (den > 1e-6f) continue;
-                }
-                if (aden < 1e-30f) { continue; }
-                float num = D - (Nx * ox + Ny * oy + Nz * oz);
+                // back-face culling is exact when N.d is well above its rounding error
+                if (!two && den > 1e-6f) continue;
+                if (aden < 1e-30f) continue;
+                // w = O - o to ~1e-7 |w| (Sterbenz for nearby facets)
+                float wx = (R.v[4] - ray.ohx) + (R.v[3] - ray.olx);
+                float wy = (R.v[5] - ray.ohy) + (R.v[7] - ray.oly);
+                float wz = (R.v[6] - ray.ohz) + (R.v[11] - ray.olz);
+                float wabs = fabsf(wx) + fabsf(wy) + fabsf(wz);
+                float num = Nx * wx + Ny * wy + Nz * wz;
                 float t = num / den;
-                float tol = eps_num / aden + 2.5e-7f * fabsf(t);
+                float at = fabsf(t);
+                float tol = (5e-7f * wabs + 4e-7f * at) / aden + 3e-7f * at;   // error bound of t
                 if (t + tol <= 0.0f) continue;                       // certainly behind
                 if (t - tol > h.t + htol) continue;                  // certainly beyond the best
-                float px = ox + t * dx - R.v[4], py = oy + t * dy - R.v[5], pz = oz + t * dz - R.v[6];
+                float px = t * dx - wx, py = t * dy - wy, pz = t * dz - wz;   // hit point - O
                 float u = px * R.v[8] + py * R.v[9] + pz * R.v[10];
                 float v = px * R.v[12] + py * R.v[13] + pz * R.v[14];
                 const PolyF P = M.poly_f[f];
-                float em = tol + eps_num;                            // position error bound, cm
+                float em = tol + 3e-7f * (wabs + at) + 2e-7f * fmaxf(P.su, P.sv);   // position error bound, cm
                 float eu = em / P.su, ev = em / P.sv;
                 if (u < -eu || u > 1.0f + eu || v < -ev || v > 1.0f + ev) continue;   // certainly outside
                 bool amb = (t - tol <= 0.0f) || (!two && den >= 0.0f);
@@ -341,7 +363,7 @@ __device__ __noinline__ HitF trace_f(const DevModel& M, int root, float ox, floa
                     inside = true;                                   // rectangle: [0,1]^2 decided above
                 } else if (r * r < P.rin2 && r + em < sqrtf(P.rin2)) {
                     inside = true;
-                    amb = false || (t - tol <= 0.0f);
+                    amb = (t - tol <= 0.0f) || (!two && den >= 0.0f);
                 } else if (r - em > sqrtf(P.rout2)) {
                     continue;
                 } else {
@@ -555,6 +577,9 @@ __global__ void __launch_bounds__(256) trace_kernel(const __grid_constant__ DevM
     int pend_cell = -1;
     bool pend = false;
     unsigned iter = 0;
+    // per-thread global counters (no contended shared atomics on the hot path)
+    unsigned long long c_hits = 0, c_des = 0, c_abs = 0, c_leak = 0, c_drop = 0, c_rechk = 0;
+    unsigned long long c_dist = 0, c_distf = 0;
     unsigned long long deadline;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(deadline));
     deadline += C.time_limit_ns;
@@ -581,7 +606,7 @@ __global__ void __launch_bounds__(256) trace_kernel(const __grid_constant__ DevM
             if (stop) {
                 if (active) {
                     flush_pending();
-                    if (!need_new) atomicAdd(B.sglob + TG_DROPPED, 1ull);
+                    if (!need_new) ++c_drop;
                 }
                 break;
             }
@@ -668,12 +693,13 @@ __global__ void __launch_bounds__(256) trace_kernel(const __grid_constant__ DevM
             else ct = (R)sqrt(r1);
             polar_dir<kFP32>(M, fo, ct, r2, flip, dx, dy, dz);
             // desorption tallies (Particle.cpp:646-680)
-            double cosn = fabs((double)dx * Rr.v[0] + (double)dy * Rr.v[1] + (double)dz * Rr.v[2]);
+            double cosn = kFP32 ? (double)fabsf(dx * M.phys_f[fo].N[0] + dy * M.phys_f[fo].N[1] + dz * M.phys_f[fo].N[2])
+                                : fabs((double)dx * Rr.v[0] + (double)dy * Rr.v[1] + (double)dz * Rr.v[2]);
             R ort = vel * (R)cosn;
             unsigned long long q1 = kFP32 ? qf(1.0f / (float)ort, (float)MFG_SCALE_INV) : qd(1.0 / (double)ort, MFG_SCALE_INV);
             unsigned long long q2 = kFP32 ? qf((float)ort, (float)MFG_SCALE_V) : qd((double)ort, MFG_SCALE_V);
             unsigned long long q3 = kFP32 ? qf(1.0f / (float)vel, (float)MFG_SCALE_INV) : qd(1.0 / (double)vel, MFG_SCALE_INV);
-            atomicAdd(B.sglob + TG_DES, 1ull);
+            ++c_des;
             int cell = -1;
             if ((In.count & MFG_COUNT_DES) && In.tex_off >= 0) {
                 int tu = (int)(su * M.phys_d[fo].texw_p), tv = (int)(sv * M.phys_d[fo].texh_p);
@@ -697,10 +723,12 @@ __global__ void __launch_bounds__(256) trace_kernel(const __grid_constant__ DevM
             const FacetIsectD& Rr = M.isect_d[fo];
             const FacetPhysD& Ph = M.phys_d[fo];
             bool flip = false;
-            if (In.flags & FF_TWO_SIDED) flip = ((double)dx * Rr.v[0] + (double)dy * Rr.v[1] + (double)dz * Rr.v[2]) > 0.0;
+            if (In.flags & FF_TWO_SIDED)
+                flip = kFP32 ? (dx * M.phys_f[fo].N[0] + dy * M.phys_f[fo].N[1] + dz * M.phys_f[fo].N[2]) > 0.0f
+                             : ((double)dx * Rr.v[0] + (double)dy * Rr.v[1] + (double)dz * Rr.v[2]) > 0.0;
             double temp = (In.flags & FF_TEMP_PARAM) ? param_at(M, M.info2[fo].temp_param, P.time) : M.info2[fo].temperature;
             double sqT = (In.flags & FF_TEMP_PARAM) ? sqrt(temp) : Ph.sqrtT;
-            if (Ph.accommodation > 0.9999) {   // UpdateVelocity (Particle.cpp:1138-1163)
+            if ((kFP32 ? (double)M.phys_f[fo].accommodation : Ph.accommodation) > 0.9999) {   // UpdateVelocity (Particle.cpp:1138-1163)
                 if (M.use_maxwell) {
                     if (kFP32) vel = (R)((float)sqT * interp_x_f((float)rng.next(), s_cdf_vf, s_cdf_pf, MFG_MAXWELL_N));
                     else vel = (R)(sqT * interp_x_d((double)rng.next(), s_cdf_v, s_cdf_p, MFG_MAXWELL_N));
@@ -737,7 +765,8 @@ __global__ void __launch_bounds__(256) trace_kernel(const __grid_constant__ DevM
                 R ct = (kind == 2) ? (R)pow((double)r1, 1.0 / (Ph.cos_exp + 1.0)) : (R)sqrt(r1);
                 polar_dir<kFP32>(M, fo, ct, r2, flip, dx, dy, dz);
             }
-            double cosn = fabs((double)dx * Rr.v[0] + (double)dy * Rr.v[1] + (double)dz * Rr.v[2]);
+            double cosn = kFP32 ? (double)fabsf(dx * M.phys_f[fo].N[0] + dy * M.phys_f[fo].N[1] + dz * M.phys_f[fo].N[2])
+                                : fabs((double)dx * Rr.v[0] + (double)dy * Rr.v[1] + (double)dz * Rr.v[2]);
             R ort = vel * (R)cosn;
             unsigned long long q1 = kFP32 ? qf(1.0f / (float)ort, (float)MFG_SCALE_INV) : qd(1.0 / (double)ort, MFG_SCALE_INV);
             unsigned long long q2 = kFP32 ? qf((float)ort, (float)MFG_SCALE_V) : qd((double)ort, MFG_SCALE_V);
@@ -766,11 +795,10 @@ __global__ void __launch_bounds__(256) trace_kernel(const __grid_constant__ DevM
         double ht, hu, hv;
         if (kFP32) {
             bool amb = false;
-            float eps_num = 1.0e-6f * (float)M.scene_scale + 4.0e-7f * (float)(fabs(P.ox) + fabs(P.oy) + fabs(P.oz));
-            HitF h = trace_f(M, root, (float)P.ox, (float)P.oy, (float)P.oz, (float)dx, (float)dy, (float)dz, P.last,
-                             eps_num, amb, T.global + TG_STATUS);
+            HitF h = trace_f(M, root, make_ray_f(P.ox, P.oy, P.oz, (float)dx, (float)dy, (float)dz), P.last, amb,
+                             T.global + TG_STATUS);
             if (amb || h.f < 0) {
-                atomicAdd(B.sglob + TG_RECHECK, 1ull);
+                ++c_rechk;
                 HitD hd = trace_d(M, root, P.ox, P.oy, P.oz, (double)dx, (double)dy, (double)dz, P.last, T.global + TG_STATUS);
                 hf = hd.f; ht = hd.t; hu = hd.u; hv = hd.v;
             } else {
@@ -790,7 +818,7 @@ __global__ void __launch_bounds__(256) trace_kernel(const __grid_constant__ DevM
             hf = h.f; ht = h.t; hu = h.u; hv = h.v;
         }
         if (hf < 0) {   // leak (Particle.cpp:387-392)
-            atomicAdd(B.sglob + TG_LEAK, 1ull);
+            ++c_leak;
             need_new = true;
             continue;
         }
@@ -808,19 +836,26 @@ __global__ void __launch_bounds__(256) trace_kernel(const __grid_constant__ DevM
         P.ox = P.ox + travel * (double)dx;
         P.oy = P.oy + travel * (double)dy;
         P.oz = P.oz + travel * (double)dz;
-        P.time += travel / 100.0 / (double)vel;
-        unsigned long long qdist = qd(travel, MFG_SCALE_DIST);
-        sadd(B.sglob + TG_DIST_LO, qdist, T.global + TG_DIST_LO);
+        if (kFP32) P.time += (double)((float)travel * (0.01f / (float)vel));   // cm -> m
+        else P.time += travel / 100.0 / (double)vel;
+        unsigned long long qdist = kFP32 ? qf((float)travel, (float)MFG_SCALE_DIST) : qd(travel, MFG_SCALE_DIST);
+        c_dist += qdist;
         if (event != 0) { need_new = true; continue; }
-        sadd(B.sglob + TG_DISTF_LO, qdist, T.global + TG_DISTF_LO);
+        c_distf += qdist;
         // ---- 4. stick or reflect at facet hf (Particle.cpp:323-357) ----
         const FacetInfo& In = M.info[hf];
         const FacetIsectD& Rh = M.isect_d[hf];
-        double s = (In.flags & FF_STICK_PARAM) ? param_at(M, M.info2[hf].stick_param, P.time) : M.phys_d[hf].sticking;
         bool absorb;
-        if (kFP32) absorb = (s == 1.0) || (s > 0.0 && (float)rng.next() < (float)s);
-        else absorb = (s == 1.0) || (s > 0.0 && (double)rng.next() < s);
-        double cosn = fabs((double)dx * Rh.v[0] + (double)dy * Rh.v[1] + (double)dz * Rh.v[2]);
+        double cosn;
+        if (kFP32) {
+            float s = (In.flags & FF_STICK_PARAM) ? (float)param_at(M, M.info2[hf].stick_param, P.time) : M.phys_f[hf].sticking;
+            absorb = (s == 1.0f) || (s > 0.0f && (float)rng.next() < s);
+            cosn = (double)fabsf(dx * M.phys_f[hf].N[0] + dy * M.phys_f[hf].N[1] + dz * M.phys_f[hf].N[2]);
+        } else {
+            double s = (In.flags & FF_STICK_PARAM) ? param_at(M, M.info2[hf].stick_param, P.time) : M.phys_d[hf].sticking;
+            absorb = (s == 1.0) || (s > 0.0 && (double)rng.next() < s);
+            cosn = fabs((double)dx * Rh.v[0] + (double)dy * Rh.v[1] + (double)dz * Rh.v[2]);
+        }
         R ort = vel * (R)cosn;
         unsigned long long q1 = kFP32 ? qf(1.0f / (float)ort, (float)MFG_SCALE_INV) : qd(1.0 / (double)ort, MFG_SCALE_INV);
         unsigned long long q2 = kFP32 ? qf((float)ort, (float)MFG_SCALE_V) : qd((double)ort, MFG_SCALE_V);
@@ -834,10 +869,10 @@ __global__ void __launch_bounds__(256) trace_kernel(const __grid_constant__ DevM
             tv = min(max(tv, 0), In.tex_h - 1);
             cell = In.tex_off + tu + tv * In.tex_w;
         }
-        atomicAdd(B.sglob + TG_HITS, 1ull);
+        ++c_hits;
         if (In.flags & FF_ANGLEMAP) anglemap_add(M, T, hf, (double)dx, (double)dy, (double)dz);
         if (absorb) {   // RecordAbsorb (Particle.cpp:888-924)
-            atomicAdd(B.sglob + TG_ABS, 1ull);
+            ++c_abs;
             facet_add(M, T, B, hf, 0, 1, 0, 1, 2 * q1, q2, q3);
             if (cell >= 0) cell_add(T.texture + (size_t)cell * TT_N, 1, 2 * q1, q2);
             if (In.flags & FF_PROFILE) profile_add(M, T, hf, 0, true, 2, 1, cosn, (double)vel, hu, hv, q1, q2);
@@ -863,12 +898,20 @@ __global__ void __launch_bounds__(256) trace_kernel(const __grid_constant__ DevM
             need_new = false;
             if (++P.bounces > C.max_steps) {   // step cap: count the hit, drop the particle
                 flush_pending();
-                atomicAdd(B.sglob + TG_DROPPED, 1ull);
+                ++c_drop;
                 need_new = true;
             }
         }
     }
-    // ---- flush the block partials ----
+    // ---- flush the per-thread counters, then the block partials ----
+    if (c_hits) atomicAdd(B.sglob + TG_HITS, c_hits);
+    if (c_des) atomicAdd(B.sglob + TG_DES, c_des);
+    if (c_abs) atomicAdd(B.sglob + TG_ABS, c_abs);
+    if (c_leak) atomicAdd(B.sglob + TG_LEAK, c_leak);
+    if (c_drop) atomicAdd(B.sglob + TG_DROPPED, c_drop);
+    if (c_rechk) atomicAdd(B.sglob + TG_RECHECK, c_rechk);
+    sadd(B.sglob + TG_DIST_LO, c_dist, T.global + TG_DIST_LO);
+    sadd(B.sglob + TG_DISTF_LO, c_distf, T.global + TG_DISTF_LO);
     __syncthreads();
     if (threadIdx.x < TG_N) {
         int i = threadIdx.x;
@@ -907,9 +950,7 @@ __global__ void replay_kernel(const __grid_constant__ DevModel M, int precision,
         hit_t[i] = h.f >= 0 ? h.t : -1.0;
     } else {
         bool amb = false;
-        float eps_num = 1.0e-6f * (float)M.scene_scale + 4.0e-7f * (float)(fabs(ox) + fabs(oy) + fabs(oz));
-        HitF h = trace_f(M, root, (float)ox, (float)oy, (float)oz, (float)dx, (float)dy, (float)dz, last[i], eps_num,
-                         amb, status);
+        HitF h = trace_f(M, root, make_ray_f(ox, oy, oz, (float)dx, (float)dy, (float)dz), last[i], amb, status);
         if (amb || h.f < 0) {
             atomicAdd(rechecks, 1ull);
             HitD hd = trace_d(M, root, ox, oy, oz, dx, dy, dz, last[i], status);
