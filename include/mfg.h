@@ -261,6 +261,13 @@ int mfg_abort(mfg_sim* sim);                     /* sets the host-mapped abort w
  * UpdateMCHits / GlobalSimuState::operator+= (Particle.cpp:21-73, MolflowSimGeom.cpp:452-458). */
 int mfg_fetch(mfg_sim* sim, mfg_state_view* view);
 
+/* Autotuner: times short trial runs (n_trial desorptions each) over block sizes and register
+ * budgets for the given precision, keeps the fastest launch shape as this handle's default
+ * (used when mfg_run_options.block_size and blocks_per_sm are 0) and writes it to *best.
+ * Trial tallies are cleared; the particle counter keeps running.  No reference counterpart:
+ * the reference has fixed CPU threads (MolflowSimulation.cpp:44-55). */
+int mfg_autotune(mfg_sim* sim, uint64_t n_trial, int32_t precision, uint64_t seed, mfg_run_options* best);
+
 /* Replay mode: intersect caller-given rays (no physics).  For ray i:
  * origin[3i..], direction[3i..], last_facet[i] (facet to skip, -1 none).
  * Out: hit_facet[i] (-1 = no hit), hit_t[i] (distance in |direction| units).

@@ -78,6 +78,8 @@ struct mfg_sim {
     std::chrono::steady_clock::time_point t_start;
     std::mutex mu;
     int launches = 0;
+    int tuned_block[2] = {0, 0};     // per precision, from mfg_autotune
+    int tuned_bps[2] = {0, 0};
 };
 
 extern "C" {
@@ -323,23 +325,35 @@ int mfg_run_async(mfg_sim* s, uint64_t n, const mfg_run_options* opt) {
     size_t fac_bytes = size_t(h.nf) * SF_N * 8;
     C.smem_facets = fac_bytes <= 64 * 1024 ? 1 : 0;
     size_t dyn = (TG_N + (C.smem_facets ? size_t(h.nf) * SF_N : 0)) * 8;
+    if (o.block_size == 0 && o.blocks_per_sm == 0 && s->tuned_block[o.precision]) {
+        o.block_size = s->tuned_block[o.precision];
+        o.blocks_per_sm = s->tuned_bps[o.precision];
+    }
     int block = o.block_size > 0 ? o.block_size : 256;
     if (block % 32 || block > 256) return fail(MFG_ERR_INVALID_ARGUMENT, "block_size must be a multiple of 32, at most 256");
-    const void* fn = o.precision == MFG_PREC_FP32R ? (const void*)mfgk::trace_kernel<true> : (const void*)mfgk::trace_kernel<false>;
+    // kernel variant: FP64, or FP32R compiled for at least 2, 3 or 4 resident blocks per SM
+    // (register budgets 128, 85, 64); blocks_per_sm selects the FP32R variant
+    int variant = 0;
+    const void* fn = (const void*)mfgk::trace_kernel<false, 2>;
+    if (o.precision == MFG_PREC_FP32R) {
+        variant = (o.blocks_per_sm == 3) ? 3 : (o.blocks_per_sm == 4 ? 4 : 2);
+        fn = variant == 3 ? (const void*)mfgk::trace_kernel<true, 3>
+           : variant == 4 ? (const void*)mfgk::trace_kernel<true, 4> : (const void*)mfgk::trace_kernel<true, 2>;
+    }
     CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn)));
     int per_sm = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, dyn));
     if (per_sm < 1) return fail(MFG_ERR_LIMIT, "kernel does not fit on an SM with this block size");
-    if (o.blocks_per_sm > 0) per_sm = std::min(per_sm, int(o.blocks_per_sm));
+    if (o.blocks_per_sm > 0) per_sm = std::min(per_sm, std::max(int(o.blocks_per_sm), 1));
     long long grid = (long long)per_sm * s->sm_count;
     long long need = (long long)((n + block - 1) / block);
     grid = std::max(1LL, std::min(grid, need));
     s->t_start = std::chrono::steady_clock::now();
     CK(cudaEventRecord(s->ev0, s->stream));
-    if (o.precision == MFG_PREC_FP32R)
-        mfgk::trace_kernel<true><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
-    else
-        mfgk::trace_kernel<false><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
+    if (variant == 3) mfgk::trace_kernel<true, 3><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
+    else if (variant == 4) mfgk::trace_kernel<true, 4><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
+    else if (variant == 2) mfgk::trace_kernel<true, 2><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
+    else mfgk::trace_kernel<false, 2><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
     CK(cudaGetLastError());
     CK(cudaEventRecord(s->ev1, s->stream));
     s->launches = 1;
@@ -405,6 +419,40 @@ int mfg_wait(mfg_sim* s, int64_t timeout_ms, mfg_run_stats* stats) {
     }
     if (stats) *stats = st;
     return st.status;
+}
+
+int mfg_autotune(mfg_sim* s, uint64_t n_trial, int32_t precision, uint64_t seed, mfg_run_options* best) {
+    if (!s || (precision != MFG_PREC_FP64 && precision != MFG_PREC_FP32R)) return fail(MFG_ERR_INVALID_ARGUMENT, "bad argument");
+    const int blocks[] = {128, 256};
+    const int bps64[] = {0};
+    const int bps32[] = {2, 3, 4};
+    double best_rate = -1;
+    mfg_run_options bo{};
+    for (int b : blocks) {
+        const int* bl = precision == MFG_PREC_FP32R ? bps32 : bps64;
+        int nb = precision == MFG_PREC_FP32R ? 3 : 1;
+        for (int k = 0; k < nb; ++k) {
+            mfg_run_options o{};
+            o.precision = precision;
+            o.seed = seed;
+            o.block_size = b;
+            o.blocks_per_sm = bl[k] ? bl[k] : 0;
+            o.time_limit_s = 60;
+            mfg_run_stats st{};
+            double rate = 0;
+            for (int rep = 0; rep < 2; ++rep) {   // the second run is timed
+                int rc = mfg_run(s, n_trial, &o, &st);
+                if (rc != MFG_OK) return rc;
+                rate = double(st.hits) / (st.kernel_ms * 1e-3 + 1e-12);
+            }
+            if (o.blocks_per_sm == 0) o.blocks_per_sm = 0;
+            if (rate > best_rate) { best_rate = rate; bo = o; }
+        }
+    }
+    s->tuned_block[precision] = bo.block_size;
+    s->tuned_bps[precision] = bo.blocks_per_sm ? bo.blocks_per_sm : 0;
+    if (best) *best = bo;
+    return mfg_reset(s);
 }
 
 int mfg_run(mfg_sim* s, uint64_t n, const mfg_run_options* opt, mfg_run_stats* stats) {

@@ -28,10 +28,11 @@ struct __align__(16) NodeF {
 };
 
 // Facet intersection record FP64 (128 B):
-//  [0..2] N, [3] D = N.O, [4..6] O, [7] pad, [8..10] U/|U|^2, [11] pad, [12..14] V/|V|^2, [15] pad
+//  [0..2] N, [3] D = N.O, [4..6] O, [7] two-sided flag (nonzero bits), [8..10] U/|U|^2, [11] pad,
+//  [12..14] V/|V|^2, [15] pad
 struct __align__(16) FacetIsectD { double v[16]; };
 // FP32 copy (64 B): [0..2] N, [3] Olo.x, [4..6] Ohi, [7] Olo.y, [8..10] U/|U|^2, [11] Olo.z,
-// [12..14] V/|V|^2 — O as a hi+lo float pair for the origin-relative test
+// [12..14] V/|V|^2, [15] two-sided flag (1.0f) — O as a hi+lo float pair for the origin-relative test
 struct __align__(16) FacetIsectF { float v[16]; };
 
 // Polygon record: circle shortcut + vertex range (64 B / 32 B).
@@ -49,6 +50,7 @@ struct __align__(16) PolyF { float cu, cv, su, sv, rin2, rout2; int32_t vstart, 
 #define FF_ANGLEMAP    32u
 #define FF_PROFILE     64u
 #define FF_DIFFUSE_ONLY 128u
+#define FF_FAST_REFL   256u   // diffuse, full accommodation, Maxwell speeds, no sojourn, constant temperature
 
 // Per-facet physics record (FP64, 128 B).
 struct __align__(16) FacetPhysD {

@@ -654,6 +654,10 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
             r[12 + a] = F.V[a] / v2;
         }
         r[3] = F.N[0] * F.O[0] + F.N[1] * F.O[1] + F.N[2] * F.O[2];
+        if (m.two_sided[i]) {   // two-sided flag in the record's padding: nonzero bits
+            long long one = 1;
+            std::memcpy(&r[7], &one, sizeof one);
+        }
         // FP32 copy: [N | O hi/lo split | U/|U|^2 | V/|V|^2] (origin-relative FP32 facet test)
         float* q = m.isect_f[i].v;
         for (int k = 0; k < 16; ++k) q[k] = 0.0f;
@@ -666,6 +670,7 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
         q[3] = float(F.O[0] - double(q[4]));
         q[7] = float(F.O[1] - double(q[5]));
         q[11] = float(F.O[2] - double(q[6]));
+        q[15] = m.two_sided[i] ? 1.0f : 0.0f;
         // circle shortcut for the point-in-polygon test
         double su = std::sqrt(u2), sv = std::sqrt(v2);
         const double* pv = &m.v2[2 * size_t(F.vstart)];
@@ -742,6 +747,8 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
                    (m.p_stick[i] >= 0 ? FF_STICK_PARAM : 0) | (m.p_temp[i] >= 0 ? FF_TEMP_PARAM : 0) |
                    (m.sojourn[i] ? FF_SOJOURN : 0) | (m.ang_off[i] >= 0 ? FF_ANGLEMAP : 0) |
                    (m.prof_idx[i] >= 0 ? FF_PROFILE : 0) | (m.diffuse[i] > 0.999999 ? FF_DIFFUSE_ONLY : 0);
+        if (m.diffuse[i] > 0.999999 && m.accommodation[i] > 0.9999 && m.use_maxwell && !m.sojourn[i] && m.p_temp[i] < 0)
+            in.flags |= FF_FAST_REFL;
         in.count = m.count[i];
         in.tex_off = int32_t(m.tex_off[i]);
         in.tex_w = m.tex_w[i];

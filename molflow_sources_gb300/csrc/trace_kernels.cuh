@@ -23,7 +23,6 @@
 
 namespace mfgk {
 
-constexpr int kStack = 64;
 constexpr double kPi = 3.14159265358979323846;
 
 // ------------------------------------------------------------------ Philox --
@@ -140,7 +139,7 @@ __device__ __forceinline__ float interp_x_f(float y, const float* xs, const floa
     return xs[i] + (xs[i + 1] - xs[i]) * w;
 }
 // InterpolateY (no extrapolation) for time-dependent parameters
-__device__ double param_at(const DevModel& M, int p, double t) {
+__device__ __noinline__ double param_at(const DevModel& M, int p, double t) {
     int s = M.par_start[p], e = M.par_start[p + 1], n = e - s;
     const double* xs = M.par_t + s;
     const double* ys = M.par_v + s;
@@ -156,237 +155,11 @@ __device__ double param_at(const DevModel& M, int p, double t) {
     return ys[i] + (ys[i + 1] - ys[i]) * w;
 }
 
-// -------------------------------------------------- point in polygon ----
-__device__ __forceinline__ bool crossing_d(const double2* v2, int vs, int nv, double u, double v) {
-    bool in = false;
-    double2 pj = v2[vs + nv - 1];
-    for (int i = 0; i < nv; ++i) {
-        double2 pi = v2[vs + i];
-        if ((pi.y > v) != (pj.y > v)) {
-            double cr = (pj.x - pi.x) * (v - pi.y) - (u - pi.x) * (pj.y - pi.y);
-            if ((cr > 0) == (pj.y > pi.y)) in = !in;
-        }
-        pj = pi;
-    }
-    return in;
-}
-__device__ __forceinline__ bool in_facet_d(const DevModel& M, int f, double u, double v) {
-    const PolyD P = M.poly_d[f];
-    double du = (u - P.cu) * P.su, dv = (v - P.cv) * P.sv;
-    double r2 = du * du + dv * dv;
-    if (r2 < P.rin2) return true;
-    if (r2 > P.rout2) return false;
-    return crossing_d(M.v2_d, P.vstart, P.nv, u, v);
-}
+}  // namespace mfgk
 
-// --------------------------------------------------------- FP64 trace ---
-struct HitD {
-    int f;
-    double t, u, v;
-};
+#include "traversal.cuh"
 
-// closest hard hit of the ray (skipping facet `last`); BVH of structure `root`
-__device__ __noinline__ HitD trace_d(const DevModel& M, int root, double ox, double oy, double oz,
-                                     double dx, double dy, double dz, int last, unsigned long long* status) {
-    HitD h;
-    h.f = -1;
-    h.t = 1.0e99;
-    h.u = h.v = 0;
-    double ix = 1.0 / dx, iy = 1.0 / dy, iz = 1.0 / dz;
-    int stack[kStack];
-    int sp = 0;
-    int node = root;
-    while (true) {
-        const NodeD nd = M.nodes_d[node];
-        double tx0 = (nd.lo[0] - ox) * ix, tx1 = (nd.hi[0] - ox) * ix;
-        double ty0 = (nd.lo[1] - oy) * iy, ty1 = (nd.hi[1] - oy) * iy;
-        double tz0 = (nd.lo[2] - oz) * iz, tz1 = (nd.hi[2] - oz) * iz;
-        double tmin = fmax(fmax(fmin(tx0, tx1), fmin(ty0, ty1)), fmax(fmin(tz0, tz1), 0.0));
-        double tmax = fmin(fmin(fmax(tx0, tx1), fmax(ty0, ty1)), fmin(fmax(tz0, tz1), h.t));
-        bool hit = tmin <= tmax;
-        if (hit && nd.b >= 0) {
-            int near = nd.a, far = nd.a + 1;
-            double dax = nd.b == 0 ? dx : (nd.b == 1 ? dy : dz);
-            if (dax < 0) { near = nd.a + 1; far = nd.a; }
-            if (sp < kStack) stack[sp++] = far;
-            else atomicOr(status, KS_STACK);
-            node = near;
-            continue;
-        }
-        if (hit) {
-            int cnt = -1 - nd.b;
-            for (int k = 0; k < cnt; ++k) {
-                int f = M.prims[nd.a + k];
-                if (f == last) continue;
-                const FacetIsectD& R = M.isect_d[f];
-                double Nx = R.v[0], Ny = R.v[1], Nz = R.v[2], D = R.v[3];
-                double den = Nx * dx + Ny * dy + Nz * dz;
-                bool two = (M.info[f].flags & FF_TWO_SIDED) != 0;
-                if (!two && den >= 0.0) continue;
-                if (den == 0.0) continue;
-                double t = (D - (Nx * ox + Ny * oy + Nz * oz)) / den;
-                if (!(t > 0.0) || t > h.t) continue;
-                double px = ox + t * dx - R.v[4], py = oy + t * dy - R.v[5], pz = oz + t * dz - R.v[6];
-                double u = px * R.v[8] + py * R.v[9] + pz * R.v[10];
-                if (u < 0.0 || u > 1.0) continue;
-                double v = px * R.v[12] + py * R.v[13] + pz * R.v[14];
-                if (v < 0.0 || v > 1.0) continue;
-                if (!in_facet_d(M, f, u, v)) continue;
-                if (t < h.t || f < h.f) { h.f = f; h.t = t; h.u = u; h.v = v; }
-            }
-        }
-        if (sp == 0) break;
-        node = stack[--sp];
-    }
-    return h;
-}
-
-// --------------------------------------------------------- FP32 trace ---
-// FP32 traversal with per-candidate error bounds.  Returns the hit and sets
-// `ambiguous` when a candidate could be classified differently in exact
-// arithmetic (near an edge, near the origin, or too close to the best hit).
-struct HitF {
-    int f;
-    float t, u, v;
-};
-
-__device__ __forceinline__ bool edge_inside_f(const DevModel& M, const PolyF& P, float u, float v, float em,
-                                              bool& amb) {
-    // crossing test, plus ambiguity when the point is within em (cm) of an edge line
-    bool in = false;
-    float pu = u * P.su, pv = v * P.sv;
-    float2 pj = M.v2_f[P.vstart + P.nv - 1];
-    float pju = pj.x * P.su, pjv = pj.y * P.sv;
-    for (int i = 0; i < P.nv; ++i) {
-        float2 pi = M.v2_f[P.vstart + i];
-        float piu = pi.x * P.su, piv = pi.y * P.sv;
-        float eu = pju - piu, ev = pjv - piv;
-        float cr = eu * (pv - piv) - (pu - piu) * ev;
-        // |cr| / |e| is the distance to the edge line; a point beyond the segment's
-        // ends is at least as far from the segment, so the test stays conservative.
-        float l2 = eu * eu + ev * ev;
-        if (cr * cr <= em * em * l2) {
-            // within em of this edge's line: ambiguous if also within em of the segment span
-            float tt = ((pu - piu) * eu + (pv - piv) * ev);
-            if (tt >= -em * sqrtf(l2) && tt <= l2 + em * sqrtf(l2)) amb = true;
-        }
-        if ((piv > pv) != (pjv > pv)) {
-            if ((cr > 0) == (pjv > piv)) in = !in;
-        }
-        pju = piu; pjv = piv;
-    }
-    return in;
-}
-
-// Ray for the FP32 traversal: origin split into hi + lo floats so that O - o is
-// formed to ~1e-7 of its own size, whatever the absolute coordinates.
-struct RayF {
-    float ohx, ohy, ohz, olx, oly, olz;
-    float dx, dy, dz;
-};
-__device__ __forceinline__ RayF make_ray_f(double ox, double oy, double oz, float dx, float dy, float dz) {
-    RayF r;
-    r.ohx = (float)ox; r.ohy = (float)oy; r.ohz = (float)oz;
-    r.olx = (float)(ox - (double)r.ohx); r.oly = (float)(oy - (double)r.ohy); r.olz = (float)(oz - (double)r.ohz);
-    r.dx = dx; r.dy = dy; r.dz = dz;
-    return r;
-}
-
-// FacetIsectF layout: [N0 N1 N2 Olo0 | Ohi0 Ohi1 Ohi2 Olo1 | Us0 Us1 Us2 Olo2 | Vs0 Vs1 Vs2 -]
-__device__ __noinline__ HitF trace_f(const DevModel& M, int root, const RayF& ray, int last, bool& ambiguous,
-                                     unsigned long long* status) {
-    HitF h;
-    h.f = -1;
-    h.t = 3.0e38f;
-    h.u = h.v = 0;
-    float htol = 0.0f;    // error bound of h.t
-    const float dx = ray.dx, dy = ray.dy, dz = ray.dz;
-    const float ox = ray.ohx, oy = ray.ohy, oz = ray.ohz;
-    float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
-    int stack[kStack];
-    int sp = 0;
-    int node = root;
-    while (true) {
-        const NodeF nd = M.nodes_f[node];
-        float tx0 = (nd.lo[0] - ox) * ix, tx1 = (nd.hi[0] - ox) * ix;
-        float ty0 = (nd.lo[1] - oy) * iy, ty1 = (nd.hi[1] - oy) * iy;
-        float tz0 = (nd.lo[2] - oz) * iz, tz1 = (nd.hi[2] - oz) * iz;
-        float tmin = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.0f));
-        float tmax = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), h.t + 2.0f * htol));
-        bool hit = tmin <= tmax * 1.0000005f;
-        if (hit && nd.b >= 0) {
-            int near = nd.a, far = nd.a + 1;
-            float dax = nd.b == 0 ? dx : (nd.b == 1 ? dy : dz);
-            if (dax < 0) { near = nd.a + 1; far = nd.a; }
-            if (sp < kStack) stack[sp++] = far;
-            else atomicOr(status, KS_STACK);
-            node = near;
-            continue;
-        }
-        if (hit) {
-            int cnt = -1 - nd.b;
-            for (int k = 0; k < cnt; ++k) {
-                int f = M.prims[nd.a + k];
-                if (f == last) continue;
-                const FacetIsectF& R = M.isect_f[f];
-                float Nx = R.v[0], Ny = R.v[1], Nz = R.v[2];
-                float den = Nx * dx + Ny * dy + Nz * dz;
-                bool two = (M.info[f].flags & FF_TWO_SIDED) != 0;
-                float aden = fabsf(den);
-                // back-face culling is exact when N.d is well above its rounding error
-                if (!two && den > 1e-6f) continue;
-                if (aden < 1e-30f) continue;
-                // w = O - o to ~1e-7 |w| (Sterbenz for nearby facets)
-                float wx = (R.v[4] - ray.ohx) + (R.v[3] - ray.olx);
-                float wy = (R.v[5] - ray.ohy) + (R.v[7] - ray.oly);
-                float wz = (R.v[6] - ray.ohz) + (R.v[11] - ray.olz);
-                float wabs = fabsf(wx) + fabsf(wy) + fabsf(wz);
-                float num = Nx * wx + Ny * wy + Nz * wz;
-                float t = num / den;
-                float at = fabsf(t);
-                float tol = (5e-7f * wabs + 4e-7f * at) / aden + 3e-7f * at;   // error bound of t
-                if (t + tol <= 0.0f) continue;                       // certainly behind
-                if (t - tol > h.t + htol) continue;                  // certainly beyond the best
-                float px = t * dx - wx, py = t * dy - wy, pz = t * dz - wz;   // hit point - O
-                float u = px * R.v[8] + py * R.v[9] + pz * R.v[10];
-                float v = px * R.v[12] + py * R.v[13] + pz * R.v[14];
-                const PolyF P = M.poly_f[f];
-                float em = tol + 3e-7f * (wabs + at) + 2e-7f * fmaxf(P.su, P.sv);   // position error bound, cm
-                float eu = em / P.su, ev = em / P.sv;
-                if (u < -eu || u > 1.0f + eu || v < -ev || v > 1.0f + ev) continue;   // certainly outside
-                bool amb = (t - tol <= 0.0f) || (!two && den >= 0.0f);
-                amb = amb || u < eu || u > 1.0f - eu || v < ev || v > 1.0f - ev;
-                bool inside;
-                float du = (u - P.cu) * P.su, dv = (v - P.cv) * P.sv;
-                float r = sqrtf(du * du + dv * dv);
-                if (P.rin2 > 1e29f) {
-                    inside = true;                                   // rectangle: [0,1]^2 decided above
-                } else if (r * r < P.rin2 && r + em < sqrtf(P.rin2)) {
-                    inside = true;
-                    amb = (t - tol <= 0.0f) || (!two && den >= 0.0f);
-                } else if (r - em > sqrtf(P.rout2)) {
-                    continue;
-                } else {
-                    bool eamb = false;
-                    inside = edge_inside_f(M, P, u, v, em, eamb);
-                    amb = amb || eamb;
-                }
-                if (amb) {
-                    // could be a hit closer than the best one: let FP64 decide the ray
-                    if (t - tol <= h.t + htol) ambiguous = true;
-                    continue;
-                }
-                if (!inside) continue;
-                // certain hit; ambiguous ordering when it is within error bounds of the best
-                if (h.f >= 0 && fabsf(t - h.t) <= tol + htol) ambiguous = true;
-                if (t < h.t) { h.f = f; h.t = t; h.u = u; h.v = v; htol = tol; }
-            }
-        }
-        if (sp == 0) break;
-        node = stack[--sp];
-    }
-    return h;
-}
+namespace mfgk {
 
 // ------------------------------------------------------- block tallies --
 struct BlockTally {
@@ -443,7 +216,7 @@ struct ParticleState {
 };
 
 // ProfileFacet (Particle.cpp:1026-1085); profiles are tallied in global memory
-__device__ __forceinline__ void profile_add(const DevModel& M, const DevTally& T, int f, int m, bool count_hit,
+__device__ __noinline__ void profile_add(const DevModel& M, const DevTally& T, int f, int m, bool count_hit,
                                             unsigned long long vfac, unsigned long long ofac, double cosn, double vel,
                                             double u, double v, unsigned long long q1, unsigned long long q2) {
     const FacetInfo& In = M.info[f];
@@ -476,7 +249,7 @@ __device__ __forceinline__ void profile_add(const DevModel& M, const DevTally& T
 }
 
 // RecordAngleMap (Particle.cpp:1104-1136): incident (theta, phi) histogram, not time resolved
-__device__ __forceinline__ void anglemap_add(const DevModel& M, const DevTally& T, int f, double dx, double dy, double dz) {
+__device__ __noinline__ void anglemap_add(const DevModel& M, const DevTally& T, int f, double dx, double dy, double dz) {
     const FacetInfo& In = M.info[f];
     const FacetInfo2& I2 = M.info2[f];
     const FacetIsectD& R = M.isect_d[f];
@@ -534,8 +307,59 @@ __device__ __forceinline__ void polar_dir(const DevModel& M, int f, R ct, R r2, 
     }
 }
 
-template <bool kFP32>
-__global__ void __launch_bounds__(256) trace_kernel(const __grid_constant__ DevModel M, DevTally T, LaunchCtl C) {
+// General relaunch (any accommodation, temperature parameter, sojourn time, reflection
+// mix): UpdateVelocity, sojourn, diffuse / specular / cos^N direction, with the random
+// numbers drawn in the order of PerformBounce (Particle.cpp:769-802).
+template <bool kFP32, class Rng, class R>
+__device__ __noinline__ void reflect_general(const DevModel& M, int fo, bool flip, Rng& rng, double& time, R& vel,
+                                             R& dx, R& dy, R& dz, const double* cv, const double* cp,
+                                             const float* cvf, const float* cpf) {
+    const FacetInfo& In = M.info[fo];
+    const FacetPhysD& Ph = M.phys_d[fo];
+    const FacetIsectD& Rr = M.isect_d[fo];
+    double temp = (In.flags & FF_TEMP_PARAM) ? param_at(M, M.info2[fo].temp_param, time) : M.info2[fo].temperature;
+    double sqT = (In.flags & FF_TEMP_PARAM) ? sqrt(temp) : Ph.sqrtT;
+    if (Ph.accommodation > 0.9999) {
+        if (M.use_maxwell) {
+            if (kFP32) vel = (R)((float)sqT * interp_x_f((float)rng.next(), cvf, cpf, MFG_MAXWELL_N));
+            else vel = (R)(sqT * interp_x_d((double)rng.next(), cv, cp, MFG_MAXWELL_N));
+        } else {
+            vel = (R)(145.469 * sqT / M.gas_mass);   // the reference's formula (Particle.cpp:1152)
+        }
+    } else {
+        double o2 = (double)vel * (double)vel, n2;
+        if (M.use_maxwell) {
+            double v = sqT * interp_x_d((double)rng.next(), cv, cp, MFG_MAXWELL_N);
+            n2 = v * v;
+        } else {
+            n2 = 29369.939 * (temp / M.gas_mass);
+        }
+        vel = (R)sqrt(o2 + (n2 - o2) * Ph.accommodation);
+    }
+    if (In.flags & FF_SOJOURN) {
+        double A = exp(-Ph.soj_e / (8.31 * temp));
+        time += -log(1.0 - (double)rng.next()) / (A * Ph.soj_freq);
+    }
+    int kind = 0;   // 0 diffuse, 1 specular, 2 cos^N
+    if (!(In.flags & FF_DIFFUSE_ONLY)) {
+        double rt = (double)rng.next();
+        kind = (rt < Ph.diffuse) ? 0 : (rt < Ph.diffuse + Ph.specular ? 1 : 2);
+    }
+    if (kind == 1) {
+        // mirror reflection: the normal component changes sign (Particle.cpp:790-794)
+        double dn = (double)dx * Rr.v[0] + (double)dy * Rr.v[1] + (double)dz * Rr.v[2];
+        dx = (R)((double)dx - 2.0 * dn * Rr.v[0]);
+        dy = (R)((double)dy - 2.0 * dn * Rr.v[1]);
+        dz = (R)((double)dz - 2.0 * dn * Rr.v[2]);
+    } else {
+        R r1 = (R)rng.next(), r2 = (R)rng.next();
+        R ct = (kind == 2) ? (R)pow((double)r1, 1.0 / (Ph.cos_exp + 1.0)) : (R)sqrt(r1);
+        polar_dir<kFP32>(M, fo, ct, r2, flip, dx, dy, dz);
+    }
+}
+
+template <bool kFP32, int kMinBlocks>
+__global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_constant__ DevModel M, DevTally T, LaunchCtl C) {
     typedef typename Real_<kFP32>::T R;
     extern __shared__ unsigned long long smem[];
     __shared__ double s_cdf_v[MFG_MAXWELL_N], s_cdf_p[MFG_MAXWELL_N];
@@ -702,7 +526,9 @@ __global__ void __launch_bounds__(256) trace_kernel(const __grid_constant__ DevM
             ++c_des;
             int cell = -1;
             if ((In.count & MFG_COUNT_DES) && In.tex_off >= 0) {
-                int tu = (int)(su * M.phys_d[fo].texw_p), tv = (int)(sv * M.phys_d[fo].texh_p);
+                double tw = kFP32 ? (double)M.phys_f[fo].texw_p : M.phys_d[fo].texw_p;
+                double th = kFP32 ? (double)M.phys_f[fo].texh_p : M.phys_d[fo].texh_p;
+                int tu = (int)(su * tw), tv = (int)(sv * th);
                 tu = min(max(tu, 0), In.tex_w - 1);
                 tv = min(max(tv, 0), In.tex_h - 1);
                 cell = In.tex_off + tu + tv * In.tex_w;
@@ -720,51 +546,26 @@ __global__ void __launch_bounds__(256) trace_kernel(const __grid_constant__ DevM
             // relaunch half of PerformBounce (Particle.cpp:769-836)
             fo = P.last;
             const FacetInfo& In = M.info[fo];
-            const FacetIsectD& Rr = M.isect_d[fo];
-            const FacetPhysD& Ph = M.phys_d[fo];
             bool flip = false;
-            if (In.flags & FF_TWO_SIDED)
-                flip = kFP32 ? (dx * M.phys_f[fo].N[0] + dy * M.phys_f[fo].N[1] + dz * M.phys_f[fo].N[2]) > 0.0f
-                             : ((double)dx * Rr.v[0] + (double)dy * Rr.v[1] + (double)dz * Rr.v[2]) > 0.0;
-            double temp = (In.flags & FF_TEMP_PARAM) ? param_at(M, M.info2[fo].temp_param, P.time) : M.info2[fo].temperature;
-            double sqT = (In.flags & FF_TEMP_PARAM) ? sqrt(temp) : Ph.sqrtT;
-            if ((kFP32 ? (double)M.phys_f[fo].accommodation : Ph.accommodation) > 0.9999) {   // UpdateVelocity (Particle.cpp:1138-1163)
-                if (M.use_maxwell) {
-                    if (kFP32) vel = (R)((float)sqT * interp_x_f((float)rng.next(), s_cdf_vf, s_cdf_pf, MFG_MAXWELL_N));
-                    else vel = (R)(sqT * interp_x_d((double)rng.next(), s_cdf_v, s_cdf_p, MFG_MAXWELL_N));
+            if (In.flags & FF_TWO_SIDED) {
+                if (kFP32) {
+                    const FacetPhysF& Pf = M.phys_f[fo];
+                    flip = (dx * Pf.N[0] + dy * Pf.N[1] + dz * Pf.N[2]) > 0.0f;
                 } else {
-                    vel = (R)(145.469 * sqT / M.gas_mass);
+                    const FacetIsectD& Rf = M.isect_d[fo];
+                    flip = ((double)dx * Rf.v[0] + (double)dy * Rf.v[1] + (double)dz * Rf.v[2]) > 0.0;
                 }
-            } else {
-                double o2 = (double)vel * (double)vel, n2;
-                if (M.use_maxwell) {
-                    double v = sqT * interp_x_d((double)rng.next(), s_cdf_v, s_cdf_p, MFG_MAXWELL_N);
-                    n2 = v * v;
-                } else {
-                    n2 = 29369.939 * (temp / M.gas_mass);
-                }
-                vel = (R)sqrt(o2 + (n2 - o2) * Ph.accommodation);
             }
-            if (In.flags & FF_SOJOURN) {
-                double A = exp(-Ph.soj_e / (8.31 * temp));
-                P.time += -log(1.0 - (double)rng.next()) / (A * Ph.soj_freq);
-            }
-            int kind = 0;   // 0 diffuse, 1 specular, 2 cos^N
-            if (!(In.flags & FF_DIFFUSE_ONLY)) {
-                double rt = (double)rng.next();
-                kind = (rt < Ph.diffuse) ? 0 : (rt < Ph.diffuse + Ph.specular ? 1 : 2);
-            }
-            if (kind == 1) {
-                // mirror reflection: the normal component changes sign (Particle.cpp:790-794)
-                double dn = (double)dx * Rr.v[0] + (double)dy * Rr.v[1] + (double)dz * Rr.v[2];
-                dx = (R)((double)dx - 2.0 * dn * Rr.v[0]);
-                dy = (R)((double)dy - 2.0 * dn * Rr.v[1]);
-                dz = (R)((double)dz - 2.0 * dn * Rr.v[2]);
-            } else {
+            if (In.flags & FF_FAST_REFL) {
+                // UpdateVelocity with full accommodation and Maxwell speeds, then a diffuse direction
+                if (kFP32) vel = (R)(M.phys_f[fo].sqrtT * interp_x_f((float)rng.next(), s_cdf_vf, s_cdf_pf, MFG_MAXWELL_N));
+                else vel = (R)(M.phys_d[fo].sqrtT * interp_x_d((double)rng.next(), s_cdf_v, s_cdf_p, MFG_MAXWELL_N));
                 R r1 = (R)rng.next(), r2 = (R)rng.next();
-                R ct = (kind == 2) ? (R)pow((double)r1, 1.0 / (Ph.cos_exp + 1.0)) : (R)sqrt(r1);
-                polar_dir<kFP32>(M, fo, ct, r2, flip, dx, dy, dz);
+                polar_dir<kFP32>(M, fo, (R)sqrt(r1), r2, flip, dx, dy, dz);
+            } else {
+                reflect_general<kFP32>(M, fo, flip, rng, P.time, vel, dx, dy, dz, s_cdf_v, s_cdf_p, s_cdf_vf, s_cdf_pf);
             }
+            const FacetIsectD& Rr = M.isect_d[fo];
             double cosn = kFP32 ? (double)fabsf(dx * M.phys_f[fo].N[0] + dy * M.phys_f[fo].N[1] + dz * M.phys_f[fo].N[2])
                                 : fabs((double)dx * Rr.v[0] + (double)dy * Rr.v[1] + (double)dz * Rr.v[2]);
             R ort = vel * (R)cosn;
@@ -776,7 +577,9 @@ __global__ void __launch_bounds__(256) trace_kernel(const __grid_constant__ DevM
             flush_pending();
             int cell = -1;
             if ((In.count & MFG_COUNT_REFL) && In.tex_off >= 0) {
-                int tu = (int)(P.u * Ph.texw_p), tv = (int)(P.v * Ph.texh_p);
+                double tw = kFP32 ? (double)M.phys_f[fo].texw_p : M.phys_d[fo].texw_p;
+                double th = kFP32 ? (double)M.phys_f[fo].texh_p : M.phys_d[fo].texh_p;
+                int tu = (int)(P.u * tw), tv = (int)(P.v * th);
                 tu = min(max(tu, 0), In.tex_w - 1);
                 tv = min(max(tv, 0), In.tex_h - 1);
                 cell = In.tex_off + tu + tv * In.tex_w;
@@ -864,7 +667,9 @@ __global__ void __launch_bounds__(256) trace_kernel(const __grid_constant__ DevM
         P.v = hv;
         int cell = -1;
         if (In.tex_off >= 0 && (In.count & (absorb ? MFG_COUNT_ABS : MFG_COUNT_REFL))) {
-            int tu = (int)(hu * M.phys_d[hf].texw_p), tv = (int)(hv * M.phys_d[hf].texh_p);
+            double tw = kFP32 ? (double)M.phys_f[hf].texw_p : M.phys_d[hf].texw_p;
+            double th = kFP32 ? (double)M.phys_f[hf].texh_p : M.phys_d[hf].texh_p;
+            int tu = (int)(hu * tw), tv = (int)(hv * th);
             tu = min(max(tu, 0), In.tex_w - 1);
             tv = min(max(tv, 0), In.tex_h - 1);
             cell = In.tex_off + tu + tv * In.tex_w;

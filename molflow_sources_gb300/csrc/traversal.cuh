@@ -1,0 +1,250 @@
+// traversal.cuh — ray/BVH traversal for the tracer: FP64 (trace_d) and FP32 with
+// error bounds (trace_f), point-in-polygon tests.  Host-compilable with the shims in
+// the CPU harness of the tests; device code otherwise.
+#pragma once
+#include <stdint.h>
+
+#include "device_model.h"
+
+#ifndef MFG_AMB_HOOK
+#define MFG_AMB_HOOK(reason)
+#endif
+
+namespace mfgk {
+
+constexpr int kStack = 64;
+
+// -------------------------------------------------- point in polygon ----
+__device__ __forceinline__ bool crossing_d(const double2* v2, int vs, int nv, double u, double v) {
+    bool in = false;
+    double2 pj = v2[vs + nv - 1];
+    for (int i = 0; i < nv; ++i) {
+        double2 pi = v2[vs + i];
+        if ((pi.y > v) != (pj.y > v)) {
+            double cr = (pj.x - pi.x) * (v - pi.y) - (u - pi.x) * (pj.y - pi.y);
+            if ((cr > 0) == (pj.y > pi.y)) in = !in;
+        }
+        pj = pi;
+    }
+    return in;
+}
+__device__ __forceinline__ bool in_facet_d(const DevModel& M, int f, double u, double v) {
+    const PolyD P = M.poly_d[f];
+    double du = (u - P.cu) * P.su, dv = (v - P.cv) * P.sv;
+    double r2 = du * du + dv * dv;
+    if (r2 < P.rin2) return true;
+    if (r2 > P.rout2) return false;
+    return crossing_d(M.v2_d, P.vstart, P.nv, u, v);
+}
+
+// --------------------------------------------------------- FP64 trace ---
+struct HitD {
+    int f;
+    double t, u, v;
+};
+
+// closest hard hit of the ray (skipping facet `last`); BVH of structure `root`
+__device__ __noinline__ HitD trace_d(const DevModel& M, int root, double ox, double oy, double oz,
+                                     double dx, double dy, double dz, int last, unsigned long long* status) {
+    HitD h;
+    h.f = -1;
+    h.t = 1.0e99;
+    h.u = h.v = 0;
+    double ix = 1.0 / dx, iy = 1.0 / dy, iz = 1.0 / dz;
+    int stack[kStack];
+    int sp = 0;
+    int node = root;
+    while (true) {
+        const NodeD nd = M.nodes_d[node];
+        double tx0 = (nd.lo[0] - ox) * ix, tx1 = (nd.hi[0] - ox) * ix;
+        double ty0 = (nd.lo[1] - oy) * iy, ty1 = (nd.hi[1] - oy) * iy;
+        double tz0 = (nd.lo[2] - oz) * iz, tz1 = (nd.hi[2] - oz) * iz;
+        double tmin = fmax(fmax(fmin(tx0, tx1), fmin(ty0, ty1)), fmax(fmin(tz0, tz1), 0.0));
+        double tmax = fmin(fmin(fmax(tx0, tx1), fmax(ty0, ty1)), fmin(fmax(tz0, tz1), h.t));
+        bool hit = tmin <= tmax;
+        if (hit && nd.b >= 0) {
+            int near = nd.a, far = nd.a + 1;
+            double dax = nd.b == 0 ? dx : (nd.b == 1 ? dy : dz);
+            if (dax < 0) { near = nd.a + 1; far = nd.a; }
+            if (sp < kStack) stack[sp++] = far;
+            else atomicOr(status, KS_STACK);
+            node = near;
+            continue;
+        }
+        if (hit) {
+            int cnt = -1 - nd.b;
+            for (int k = 0; k < cnt; ++k) {
+                int f = M.prims[nd.a + k];
+                if (f == last) continue;
+                const FacetIsectD& R = M.isect_d[f];
+                double Nx = R.v[0], Ny = R.v[1], Nz = R.v[2], D = R.v[3];
+                double den = Nx * dx + Ny * dy + Nz * dz;
+                bool two = __double_as_longlong(R.v[7]) != 0;   // two-sided flag kept in the record
+                if (!two && den >= 0.0) continue;
+                if (den == 0.0) continue;
+                double t = (D - (Nx * ox + Ny * oy + Nz * oz)) / den;
+                if (!(t > 0.0) || t > h.t) continue;
+                double px = ox + t * dx - R.v[4], py = oy + t * dy - R.v[5], pz = oz + t * dz - R.v[6];
+                double u = px * R.v[8] + py * R.v[9] + pz * R.v[10];
+                if (u < 0.0 || u > 1.0) continue;
+                double v = px * R.v[12] + py * R.v[13] + pz * R.v[14];
+                if (v < 0.0 || v > 1.0) continue;
+                if (!in_facet_d(M, f, u, v)) continue;
+                if (t < h.t || f < h.f) { h.f = f; h.t = t; h.u = u; h.v = v; }
+            }
+        }
+        if (sp == 0) break;
+        node = stack[--sp];
+    }
+    return h;
+}
+
+// --------------------------------------------------------- FP32 trace ---
+// FP32 traversal with per-candidate error bounds.  Returns the hit and sets
+// `ambiguous` when a candidate could be classified differently in exact
+// arithmetic (near an edge, near the origin, or too close to the best hit).
+struct HitF {
+    int f;
+    float t, u, v;
+};
+
+__device__ __forceinline__ bool edge_inside_f(const DevModel& M, const PolyF& P, float u, float v, float em,
+                                              bool& amb) {
+    // crossing test, plus ambiguity when the point is within em (cm) of an edge line
+    bool in = false;
+    float pu = u * P.su, pv = v * P.sv;
+    float2 pj = M.v2_f[P.vstart + P.nv - 1];
+    float pju = pj.x * P.su, pjv = pj.y * P.sv;
+    for (int i = 0; i < P.nv; ++i) {
+        float2 pi = M.v2_f[P.vstart + i];
+        float piu = pi.x * P.su, piv = pi.y * P.sv;
+        float eu = pju - piu, ev = pjv - piv;
+        float cr = eu * (pv - piv) - (pu - piu) * ev;
+        // |cr| / |e| is the distance to the edge line; a point beyond the segment's
+        // ends is at least as far from the segment, so the test stays conservative.
+        float l2 = eu * eu + ev * ev;
+        if (cr * cr <= em * em * l2) {
+            // within em of this edge's line: ambiguous if also within em of the segment span
+            float tt = ((pu - piu) * eu + (pv - piv) * ev);
+            if (tt >= -em * sqrtf(l2) && tt <= l2 + em * sqrtf(l2)) amb = true;
+        }
+        if ((piv > pv) != (pjv > pv)) {
+            if ((cr > 0) == (pjv > piv)) in = !in;
+        }
+        pju = piu; pjv = piv;
+    }
+    return in;
+}
+
+// Ray for the FP32 traversal: origin split into hi + lo floats so that O - o is
+// formed to ~1e-7 of its own size, whatever the absolute coordinates.
+struct RayF {
+    float ohx, ohy, ohz, olx, oly, olz;
+    float dx, dy, dz;
+};
+__device__ __forceinline__ RayF make_ray_f(double ox, double oy, double oz, float dx, float dy, float dz) {
+    RayF r;
+    r.ohx = (float)ox; r.ohy = (float)oy; r.ohz = (float)oz;
+    r.olx = (float)(ox - (double)r.ohx); r.oly = (float)(oy - (double)r.ohy); r.olz = (float)(oz - (double)r.ohz);
+    r.dx = dx; r.dy = dy; r.dz = dz;
+    return r;
+}
+
+// FacetIsectF layout: [N0 N1 N2 Olo0 | Ohi0 Ohi1 Ohi2 Olo1 | Us0 Us1 Us2 Olo2 | Vs0 Vs1 Vs2 -]
+__device__ __noinline__ HitF trace_f(const DevModel& M, int root, const RayF& ray, int last, bool& ambiguous,
+                                     unsigned long long* status) {
+    HitF h;
+    h.f = -1;
+    h.t = 3.0e38f;
+    h.u = h.v = 0;
+    float htol = 0.0f;    // error bound of h.t
+    const float dx = ray.dx, dy = ray.dy, dz = ray.dz;
+    const float ox = ray.ohx, oy = ray.ohy, oz = ray.ohz;
+    float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
+    int stack[kStack];
+    int sp = 0;
+    int node = root;
+    while (true) {
+        const NodeF nd = M.nodes_f[node];
+        float tx0 = (nd.lo[0] - ox) * ix, tx1 = (nd.hi[0] - ox) * ix;
+        float ty0 = (nd.lo[1] - oy) * iy, ty1 = (nd.hi[1] - oy) * iy;
+        float tz0 = (nd.lo[2] - oz) * iz, tz1 = (nd.hi[2] - oz) * iz;
+        float tmin = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.0f));
+        float tmax = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), h.t + 2.0f * htol));
+        bool hit = tmin <= tmax * 1.0000005f;
+        if (hit && nd.b >= 0) {
+            int near = nd.a, far = nd.a + 1;
+            float dax = nd.b == 0 ? dx : (nd.b == 1 ? dy : dz);
+            if (dax < 0) { near = nd.a + 1; far = nd.a; }
+            if (sp < kStack) stack[sp++] = far;
+            else atomicOr(status, KS_STACK);
+            node = near;
+            continue;
+        }
+        if (hit) {
+            int cnt = -1 - nd.b;
+            for (int k = 0; k < cnt; ++k) {
+                int f = M.prims[nd.a + k];
+                if (f == last) continue;
+                const FacetIsectF& R = M.isect_f[f];
+                float Nx = R.v[0], Ny = R.v[1], Nz = R.v[2];
+                float den = Nx * dx + Ny * dy + Nz * dz;
+                bool two = R.v[15] != 0.0f;                      // two-sided flag kept in the record
+                float aden = fabsf(den);
+                // back-face culling is exact when N.d is well above its rounding error
+                if (!two && den > 1e-6f) continue;
+                if (aden < 1e-30f) continue;
+                // w = O - o to ~1e-7 |w| (Sterbenz for nearby facets)
+                float wx = (R.v[4] - ray.ohx) + (R.v[3] - ray.olx);
+                float wy = (R.v[5] - ray.ohy) + (R.v[7] - ray.oly);
+                float wz = (R.v[6] - ray.ohz) + (R.v[11] - ray.olz);
+                float wabs = fabsf(wx) + fabsf(wy) + fabsf(wz);
+                float num = Nx * wx + Ny * wy + Nz * wz;
+                float t = num / den;
+                float at = fabsf(t);
+                float tol = (5e-7f * wabs + 4e-7f * at) / aden + 3e-7f * at;   // error bound of t
+                if (t + tol <= 0.0f) continue;                       // certainly behind
+                if (t - tol > h.t + htol) continue;                  // certainly beyond the best
+                float px = t * dx - wx, py = t * dy - wy, pz = t * dz - wz;   // hit point - O
+                float u = px * R.v[8] + py * R.v[9] + pz * R.v[10];
+                float v = px * R.v[12] + py * R.v[13] + pz * R.v[14];
+                const PolyF P = M.poly_f[f];
+                float em = tol + 3e-7f * (wabs + at) + 2e-7f * fmaxf(P.su, P.sv);   // position error bound, cm
+                float eu = em / P.su, ev = em / P.sv;
+                if (u < -eu || u > 1.0f + eu || v < -ev || v > 1.0f + ev) continue;   // certainly outside
+                // reason codes: 1 near the origin, 2 nearly parallel back face, 3 near a rectangle
+                // edge, 4 near a polygon edge, 5 two hits within error bounds.  A candidate that is
+                // certainly outside its polygon is dropped whatever its distance (coplanar facets
+                // of a baffle have t = 0 exactly for a ray leaving a neighbour).
+                bool inside, eamb = false;
+                if (P.rin2 > 1e29f) {
+                    inside = true;                                   // rectangle: [0,1]^2 decided above
+                    eamb = u < eu || u > 1.0f - eu || v < ev || v > 1.0f - ev;
+                } else {
+                    float du = (u - P.cu) * P.su, dv = (v - P.cv) * P.sv;
+                    float r = sqrtf(du * du + dv * dv);
+                    if (r * r < P.rin2 && r + em < sqrtf(P.rin2)) inside = true;
+                    else if (r - em > sqrtf(P.rout2)) continue;
+                    else inside = edge_inside_f(M, P, u, v, em, eamb);
+                }
+                if (!inside && !eamb) continue;                      // certainly outside
+                int why = (t - tol <= 0.0f) ? 1 : ((!two && den >= 0.0f) ? 2 : (eamb ? (P.rin2 > 1e29f ? 3 : 4) : 0));
+                if (why) {
+                    // could be a hit closer than the best one: let FP64 decide the ray
+                    if (t - tol <= h.t + htol) { ambiguous = true; MFG_AMB_HOOK(why); }
+                    continue;
+                }
+                if (!inside) continue;
+                // certain hit; ambiguous ordering when it is within error bounds of the best
+                if (h.f >= 0 && fabsf(t - h.t) <= tol + htol) { ambiguous = true; MFG_AMB_HOOK(5); }
+                if (t < h.t) { h.f = f; h.t = t; h.u = u; h.v = v; htol = tol; }
+            }
+        }
+        if (sp == 0) break;
+        node = stack[--sp];
+    }
+    return h;
+}
+
+
+}  // namespace mfgk

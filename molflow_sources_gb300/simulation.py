@@ -75,6 +75,7 @@ def load_library(build_if_missing=True):
         L.mfg_wait.argtypes = [vp, C.c_int64, C.POINTER(A.RunStats)]
         L.mfg_abort.argtypes = [vp]
         L.mfg_fetch.argtypes = [vp, C.POINTER(A.StateView)]
+        L.mfg_autotune.argtypes = [vp, C.c_uint64, C.c_int32, C.c_uint64, C.POINTER(A.RunOptions)]
         L.mfg_replay.argtypes = [vp, C.c_int32, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                  C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_double),
                                  C.POINTER(C.c_uint64)]
@@ -183,6 +184,12 @@ class GpuSimulation:
             return MCStepResult.DesorptionError
         _check(rc)
         return MCStepResult.Success
+
+    def autotune(self, n_trial, precision=A.PREC_FP32R, seed=0x4D6F6C66):
+        """Pick the fastest launch shape for this model (clears tallies); returns it as a dict."""
+        o = A.RunOptions()
+        _check(load_library().mfg_autotune(self.h, int(n_trial), precision, seed, C.byref(o)))
+        return {"block_size": o.block_size, "blocks_per_sm": o.blocks_per_sm}
 
     def run_async(self, n_desorptions, precision=A.PREC_FP64, seed=0x4D6F6C66, time_limit_s=0.0):
         o = A.RunOptions(precision=precision, seed=seed, smem_bvh_nodes=-1, time_limit_s=time_limit_s)

@@ -99,12 +99,13 @@ def test_fp32r_agrees_with_oracle_within_3_sigma(tube):
     zz = zscores(gh, np.sqrt(gh / g.n_desorbed), m[:, A.FC_NBMCHIT], s[:, A.FC_NBMCHIT])
     assert np.abs(zz).max() < z_threshold(66), np.abs(zz).max()
     # texture counts on the 64x64 wall texture, family of 4096 cells
-    tex_o = np.array([b.texture[0, :, 0] / b.n_desorbed for b in batches])
-    tm, ts = batch_means(tex_o)
-    tg = g.texture[0, :, 0] / g.n_desorbed
-    zt = zscores(tg, np.sqrt(g.texture[0, :, 0]) / g.n_desorbed, tm, ts)
+    # (Poisson sigma of each cell count: a particle rarely hits the same cell twice)
+    n_o = sum(b.n_desorbed for b in batches)
+    co = sum(b.texture[0, :, 0] for b in batches)
+    cg = g.texture[0, :, 0]
+    zt = zscores(cg / g.n_desorbed, np.sqrt(cg) / g.n_desorbed, co / n_o, np.sqrt(co) / n_o)
     assert np.abs(zt).max() < z_threshold(4096) + 0.5, np.abs(zt).max()
-    assert abs(np.mean(zt ** 2) - 1.0) < 0.15
+    assert abs(np.mean(zt ** 2) - 1.0) < 0.1, np.mean(zt ** 2)
     # pressure-like sums per hit on the walls (Maxwell speeds)
     fs = g.facet_sums[0, 2:, A.FS_SUM_V_ORT].sum() / g.facet_counts[0, 2:, A.FC_NBMCHIT].sum()
     fo = np.mean([b.facet_sums[0, 2:, A.FS_SUM_V_ORT].sum() / b.facet_counts[0, 2:, A.FC_NBMCHIT].sum() for b in batches])
@@ -228,6 +229,23 @@ def test_kernel_time_limit_returns_status_and_context_survives():
     t = GpuSimulation(config1_tube())
     t.SimulationMCStep(1000)
     assert t.fetch().n_desorbed == 1000
+
+
+def test_autotune_and_occupancy_variants_agree(tube):
+    """Every launch shape gives identical FP32R tallies for the same particles."""
+    sim = GpuSimulation(tube)
+    ref = None
+    for bps in (2, 3, 4):
+        sim.ResetSimulation()
+        sim.set_particle_offset(0)
+        sim.SimulationMCStep(20000, precision=A.PREC_FP32R, seed=SEED, blocks_per_sm=bps)
+        st = sim.fetch()
+        if ref is None:
+            ref = st
+        assert np.array_equal(st.facet_counts, ref.facet_counts)
+    best = sim.autotune(20000)
+    assert best["block_size"] in (128, 256)
+    assert sim.fetch().n_desorbed == 0
 
 
 def test_unsupported_feature_is_reported():
