@@ -25,6 +25,7 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     "c1": dict(name="config1_tube_L10cm_R1cm_64gon_tex64x64_maxwell_N2_293K", step=100_000_000, fp64_step=5_000_000),
     "c2": dict(name="config2_beam_chamber_200k_triangles", step=10_000_000, fp64_step=500_000),
+    "c4": dict(name="config4_batch_256_instances_1k-50k_facets", step=1_000_000, fp64_step=0),
 }
 
 
@@ -159,6 +160,59 @@ def run_reference(args, rank, world):
     return 0
 
 
+def run_batch(args, torch, dist, rank, world, local, W, n_step):
+    """Config 4: 256 instances in one persistent launch (graph-captured) vs 256 separate launches."""
+    from molflow_sources_gb300 import _abi as A
+    from molflow_sources_gb300 import batch_workloads as BW
+    from molflow_sources_gb300.simulation import GpuBatch, GpuSimulation
+    models = BW.config4_batch()
+    t0 = time.time()
+    batch = GpuBatch(models, device=local)
+    batch.set_particle_offset(rank * (1 << 48))
+    load_s = time.time() - t0
+    seed = 0x4D6F6C66
+    for _ in range(args.warmup):
+        batch.run(n_step // 10, precision=A.PREC_FP32R, seed=seed, use_graph=True)
+    batch.reset()
+    sampler = ClockSampler(local)
+    sampler.start()
+    torch.cuda.synchronize()
+    ms, hits, des, launches = 0.0, 0, 0, 0
+    for k in range(args.steps):
+        st = batch.run(n_step, precision=A.PREC_FP32R, seed=seed, use_graph=True)
+        ms += st["kernel_ms"]
+        hits += st["hits"]
+        des += st["desorbed"]
+        launches += st["kernel_launches"]
+    clocks = sampler.stop()
+    # separate launches: one simulation per instance, each stepped on its own
+    sims = [GpuSimulation(m, device=local) for m in models]
+    sep_ms, sep_hits = 0.0, 0
+    for s_ in sims:
+        s_.SimulationMCStep(max(n_step // 100, 1000), precision=A.PREC_FP32R, seed=seed)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for s_ in sims:
+        s_.SimulationMCStep(n_step // 10, precision=A.PREC_FP32R, seed=seed)
+        sep_hits += s_.last_stats["hits"]
+        sep_ms += s_.last_stats["kernel_ms"]
+    sep_wall = time.perf_counter() - t1
+    rate = hits / (ms / 1e3)
+    line = {"metric": "hits/s per GB300, 256-instance batch in one persistent launch", "value": rate, "unit": "hits/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": W["name"], "instances": len(models), "facets_total": int(sum(m.n_facets for m in models)),
+                       "desorptions_per_instance_per_step": n_step, "launch": "CUDA graph, one persistent kernel"},
+            "separate_launches": {"hits_per_s_device": sep_hits / (sep_ms / 1e3), "hits_per_s_wall": sep_hits / sep_wall,
+                                  "desorptions_per_instance": n_step // 10, "launches": len(models)},
+            "gpu_launches": launches, "model_load_s": load_s, "clocks": clocks,
+            "e2e": {"value": rate, "unit": "hits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "cpu_baseline": None}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -188,6 +242,8 @@ def main():
 
     W = WORKLOADS[args.workload]
     n_step = args.step_desorptions or W["step"]
+    if args.workload == "c4":
+        return run_batch(args, torch, dist, rank, world, local, W, n_step)
     model = make_model(args.workload)
     t0 = time.time()
     sim = GpuSimulation(model, device=local)
@@ -212,6 +268,7 @@ def main():
         f64_hits += sim.last_stats["hits"]
     fp64_rate = f64_hits / (f64_ms / 1e3)
 
+    tuned = sim.autotune(max(n_step // 20, 10000), precision=A.PREC_FP32R, seed=seed)   # launch shape
     for _ in range(args.warmup):
         sim.SimulationMCStep(n_step, precision=A.PREC_FP32R, seed=seed)
     sim.ResetSimulation()
@@ -291,6 +348,7 @@ def main():
         "e2e": {"value": e2e_rate, "unit": "hits/s", "h2d_bytes_per_step": int(A.RunOptions.__basicsize__ if hasattr(A.RunOptions, "__basicsize__") else 48),
                 "d2h_bytes_per_step": int(d2h), "api": "SimulationMCStep + UpdateHitsAndLog (C ABI mfg_run + mfg_fetch)"},
         "gpu_launches": launches,
+        "launch_shape": tuned,
         "model_load_s": load_s,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "bytes_per_hit": bph, "nodes_per_ray": nodes, "facets_per_ray": prims,

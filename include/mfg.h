@@ -204,6 +204,7 @@ typedef struct mfg_run_options {
     int32_t  smem_bvh_nodes;     /* BVH nodes staged in shared memory, -1 = auto */
     double   time_limit_s;       /* kernel self-stops after this wall time (status MFG_ERR_TIMEOUT), 0 = 600 s */
     uint64_t max_steps_per_particle; /* a particle that exceeds this many bounces is dropped and counted, 0 = 2^40 */
+    int32_t  use_graph;          /* 1: launch through a captured CUDA graph (captured once per launch shape) */
 } mfg_run_options;
 
 /* Run statistics of the last run (filled by mfg_run / mfg_wait). */
@@ -232,6 +233,13 @@ size_t   mfg_last_error(char* buf, size_t buflen);
 int mfg_model_create(const mfg_model_desc* desc, mfg_model** out);
 void mfg_model_destroy(mfg_model* model);
 int mfg_state_layout_of(const mfg_model* model, mfg_state_layout* out);
+/* Merge prepared models into one batch model of n instances (C4-style batching; no reference
+ * counterpart: the reference runs one model per process).  Instances keep their own geometry,
+ * BVH, sources and tallies; they must share gas, speed law, flow mode and moments. */
+int mfg_model_merge(const mfg_model* const* models, int32_t n, mfg_model** out);
+int32_t mfg_model_instances(const mfg_model* model);
+/* Layout of instance i's own GlobalSimuState (for mfg_fetch_instance). */
+int mfg_instance_layout(const mfg_model* model, int32_t i, mfg_state_layout* out);
 /* Derived per-facet geometry as computed by the library (O,U,V,N,nU,nV as 18 doubles per facet, area) for checks. */
 int mfg_model_facet_geometry(const mfg_model* model, double* out18, double* area);
 /* BVH statistics: node count, depth, leaf count. */
@@ -252,6 +260,10 @@ uint64_t mfg_particle_offset(const mfg_sim* sim);
  * Replaces SimulationMCStep(nbStep, threadNum, remainingDes) over all threads
  * (Particle.cpp:207-396) with the desorption limit as the work unit. */
 int mfg_run(mfg_sim* sim, uint64_t n_desorptions, const mfg_run_options* opt, mfg_run_stats* stats);
+/* Batch (several models merged with mfg_model_merge): counts[i] particles for instance i, one
+ * persistent launch over a shared particle queue.  mfg_run gives every instance n particles. */
+int mfg_run_batch(mfg_sim* sim, const uint64_t* counts, const mfg_run_options* opt, mfg_run_stats* stats);
+int mfg_run_batch_async(mfg_sim* sim, const uint64_t* counts, const mfg_run_options* opt);
 /* Asynchronous form: mfg_run_async returns at once; mfg_wait blocks up to timeout_ms. */
 int mfg_run_async(mfg_sim* sim, uint64_t n_desorptions, const mfg_run_options* opt);
 int mfg_poll(mfg_sim* sim);                      /* MFG_OK when done, MFG_ERR_BUSY while running */
@@ -267,6 +279,9 @@ int mfg_fetch(mfg_sim* sim, mfg_state_view* view);
  * Trial tallies are cleared; the particle counter keeps running.  No reference counterpart:
  * the reference has fixed CPU threads (MolflowSimulation.cpp:44-55). */
 int mfg_autotune(mfg_sim* sim, uint64_t n_trial, int32_t precision, uint64_t seed, mfg_run_options* best);
+
+/* Tallies of one instance of a batch, in that instance's own layout (overwrites). */
+int mfg_fetch_instance(mfg_sim* sim, int32_t instance, mfg_state_view* view);
 
 /* Replay mode: intersect caller-given rays (no physics).  For ray i:
  * origin[3i..], direction[3i..], last_facet[i] (facet to skip, -1 none).

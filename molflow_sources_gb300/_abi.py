@@ -131,6 +131,7 @@ class RunOptions(C.Structure):
         ("smem_bvh_nodes", C.c_int32),
         ("time_limit_s", C.c_double),
         ("max_steps_per_particle", C.c_uint64),
+        ("use_graph", C.c_int32),
     ]
 
 

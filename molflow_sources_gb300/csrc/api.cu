@@ -71,7 +71,12 @@ struct mfg_sim {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     size_t n_global = TG_N, n_facet = 0, n_texture = 0, n_profile = 0, n_anglemap = 0;
-    uint64_t particles_started = 0;
+    std::vector<uint64_t> particles_started;   // per instance
+    unsigned char* h_run = nullptr;            // pinned RunDesc + prefix + first (staging)
+    unsigned char* d_run = nullptr;
+    size_t run_bytes = 0;
+    cudaGraphExec_t graph_exec = nullptr;
+    long long graph_key = -1;
     bool running = false;
     mfg_run_stats pending{};
     std::vector<unsigned long long> g_before;
@@ -198,6 +203,22 @@ static int sim_upload(mfg_sim* s) {
     M.profile_facets = h.layout.profile_facets;
     M.anglemap_cells = h.layout.anglemap_cells;
     M.scene_scale = h.scene_scale;
+    {
+        std::vector<int32_t> sb, sc;
+        std::vector<double> st;
+        for (const auto& in : h.instances) { sb.push_back(in.src_base); sc.push_back(in.nsrc); st.push_back(in.src_total); }
+        M.n_inst = int32_t(h.instances.size());
+        if ((rc = upload(s->owned, sb, &M.inst_src_base)) != MFG_OK) return rc;
+        if ((rc = upload(s->owned, sc, &M.inst_src_count)) != MFG_OK) return rc;
+        if ((rc = upload(s->owned, st, &M.inst_src_total)) != MFG_OK) return rc;
+        s->particles_started.assign(h.instances.size(), 0);
+        s->run_bytes = sizeof(RunDesc) + 8 * (2 * h.instances.size() + 1);
+        CK(cudaHostAlloc((void**)&s->h_run, s->run_bytes, cudaHostAllocDefault));
+        void* q = nullptr;
+        CK(cudaMalloc(&q, s->run_bytes));
+        s->owned.push_back(q);
+        s->d_run = static_cast<unsigned char*>(q);
+    }
     // tallies
     const size_t B = 1 + size_t(h.nm);
     s->n_facet = B * size_t(h.nf) * TF_N;
@@ -240,11 +261,11 @@ int mfg_set_particle_offset(mfg_sim* s, uint64_t first_particle) {
     if (!s) return fail(MFG_ERR_INVALID_ARGUMENT, "null sim");
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
-    s->particles_started = first_particle;
+    for (auto& p : s->particles_started) p = first_particle;
     return MFG_OK;
 }
 
-uint64_t mfg_particle_offset(const mfg_sim* s) { return s ? s->particles_started : 0; }
+uint64_t mfg_particle_offset(const mfg_sim* s) { return (s && !s->particles_started.empty()) ? s->particles_started[0] : 0; }
 
 int mfg_sim_create(const mfg_model* model, int device, mfg_sim** out) {
     if (!model || !out) return fail(MFG_ERR_INVALID_ARGUMENT, "null argument");
@@ -284,6 +305,8 @@ void mfg_sim_destroy(mfg_sim* s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     for (void* p : s->owned) cudaFree(p);
     if (s->h_abort) cudaFreeHost(s->h_abort);
+    if (s->h_run) cudaFreeHost(s->h_run);
+    if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -297,13 +320,13 @@ static int read_global(mfg_sim* s, std::vector<unsigned long long>& g) {
     return MFG_OK;
 }
 
-int mfg_run_async(mfg_sim* s, uint64_t n, const mfg_run_options* opt) {
-    if (!s) return fail(MFG_ERR_INVALID_ARGUMENT, "null sim");
-    std::lock_guard<std::mutex> lk(s->mu);
-    if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
+static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options* opt) {
     const mfg::HostModel& h = s->model->h;
     if (!h.gpu_supported) return fail(MFG_ERR_UNSUPPORTED_FEATURE, "not traced on the GPU: " + h.gpu_unsupported_reason);
-    if (h.src_facet.empty()) return fail(MFG_ERR_NO_SOURCE, "no desorbing facet (total outgassing is zero)");
+    const int ni = int(h.instances.size());
+    for (int i = 0; i < ni; ++i)
+        if (counts[i] > 0 && h.instances[i].nsrc == 0)
+            return fail(MFG_ERR_NO_SOURCE, "no desorbing facet (total outgassing is zero) in instance " + std::to_string(i));
     mfg_run_options o{};
     if (opt) o = *opt;
     if (o.precision != MFG_PREC_FP64 && o.precision != MFG_PREC_FP32R) return fail(MFG_ERR_INVALID_ARGUMENT, "unknown precision");
@@ -311,16 +334,29 @@ int mfg_run_async(mfg_sim* s, uint64_t n, const mfg_run_options* opt) {
     int rc = read_global(s, s->g_before);
     if (rc) return rc;
     *s->h_abort = 0;
-    CK(cudaMemsetAsync(s->d_counter, 0, 8, s->stream));
+    // per-run descriptor into the pinned staging buffer
+    RunDesc* R = reinterpret_cast<RunDesc*>(s->h_run);
+    unsigned long long* prefix = reinterpret_cast<unsigned long long*>(s->h_run + sizeof(RunDesc));
+    unsigned long long* first = prefix + ni + 1;
+    uint64_t total = 0;
+    prefix[0] = 0;
+    for (int i = 0; i < ni; ++i) {
+        first[i] = s->particles_started[i];
+        total += counts[i];
+        prefix[i + 1] = total;
+    }
+    R->n_total = total;
+    R->max_steps = o.max_steps_per_particle ? o.max_steps_per_particle : (1ull << 40);
+    double lim = o.time_limit_s > 0 ? o.time_limit_s : 600.0;
+    R->time_limit_ns = (unsigned long long)(lim * 1e9);
+    R->key0 = uint32_t(o.seed);
+    R->key1 = uint32_t(o.seed >> 32);
+    R->n_inst = ni;
     LaunchCtl C{};
     C.next_particle = s->d_counter;
-    C.first_particle = s->particles_started;
-    C.n_particles = n;
-    C.max_steps = o.max_steps_per_particle ? o.max_steps_per_particle : (1ull << 40);
-    double lim = o.time_limit_s > 0 ? o.time_limit_s : 600.0;
-    C.time_limit_ns = (unsigned long long)(lim * 1e9);
-    C.key0 = uint32_t(o.seed);
-    C.key1 = uint32_t(o.seed >> 32);
+    C.run = reinterpret_cast<const RunDesc*>(s->d_run);
+    C.inst_prefix = reinterpret_cast<const unsigned long long*>(s->d_run + sizeof(RunDesc));
+    C.inst_first = C.inst_prefix + ni + 1;
     C.abort_flag = s->d_abort;
     size_t fac_bytes = size_t(h.nf) * SF_N * 8;
     C.smem_facets = fac_bytes <= 64 * 1024 ? 1 : 0;
@@ -346,22 +382,69 @@ int mfg_run_async(mfg_sim* s, uint64_t n, const mfg_run_options* opt) {
     if (per_sm < 1) return fail(MFG_ERR_LIMIT, "kernel does not fit on an SM with this block size");
     if (o.blocks_per_sm > 0) per_sm = std::min(per_sm, std::max(int(o.blocks_per_sm), 1));
     long long grid = (long long)per_sm * s->sm_count;
-    long long need = (long long)((n + block - 1) / block);
-    grid = std::max(1LL, std::min(grid, need));
+    if (!o.use_graph) grid = std::max(1LL, std::min(grid, (long long)((total + block - 1) / block)));
+    auto enqueue = [&]() -> cudaError_t {
+        cudaError_t e = cudaMemcpyAsync(s->d_run, s->h_run, s->run_bytes, cudaMemcpyHostToDevice, s->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(s->d_counter, 0, 8, s->stream);
+        if (e != cudaSuccess) return e;
+        if (variant == 3) mfgk::trace_kernel<true, 3><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
+        else if (variant == 4) mfgk::trace_kernel<true, 4><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
+        else if (variant == 2) mfgk::trace_kernel<true, 2><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
+        else mfgk::trace_kernel<false, 2><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
+        return cudaGetLastError();
+    };
     s->t_start = std::chrono::steady_clock::now();
-    CK(cudaEventRecord(s->ev0, s->stream));
-    if (variant == 3) mfgk::trace_kernel<true, 3><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
-    else if (variant == 4) mfgk::trace_kernel<true, 4><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
-    else if (variant == 2) mfgk::trace_kernel<true, 2><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
-    else mfgk::trace_kernel<false, 2><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
-    CK(cudaGetLastError());
+    if (o.use_graph) {
+        // one captured graph per launch shape: [run descriptor copy, counter reset, tracer]
+        long long key = (long long)variant * 1000003LL + block * 1009LL + grid;
+        if (!s->graph_exec || s->graph_key != key) {
+            if (s->graph_exec) { cudaGraphExecDestroy(s->graph_exec); s->graph_exec = nullptr; }
+            cudaGraph_t g = nullptr;
+            CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+            cudaError_t e = enqueue();
+            cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
+            if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(e, "graph capture"); }
+            if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+            e = cudaGraphInstantiate(&s->graph_exec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) { s->graph_exec = nullptr; return cuda_fail(e, "cudaGraphInstantiate"); }
+            s->graph_key = key;
+        }
+        CK(cudaEventRecord(s->ev0, s->stream));
+        CK(cudaGraphLaunch(s->graph_exec, s->stream));
+    } else {
+        CK(cudaEventRecord(s->ev0, s->stream));
+        cudaError_t e = enqueue();
+        if (e != cudaSuccess) return cuda_fail(e, "tracer launch");
+    }
     CK(cudaEventRecord(s->ev1, s->stream));
     s->launches = 1;
     s->running = true;
     s->pending = mfg_run_stats{};
-    s->pending.desorbed = n;
-    s->particles_started += n;
+    s->pending.desorbed = total;
+    for (int i = 0; i < ni; ++i) s->particles_started[i] += counts[i];
     return MFG_OK;
+}
+
+int mfg_run_async(mfg_sim* s, uint64_t n, const mfg_run_options* opt) {
+    if (!s) return fail(MFG_ERR_INVALID_ARGUMENT, "null sim");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
+    std::vector<uint64_t> counts(s->model->h.instances.size(), n);
+    return launch_run(s, counts.data(), opt);
+}
+
+int mfg_run_batch_async(mfg_sim* s, const uint64_t* counts, const mfg_run_options* opt) {
+    if (!s || !counts) return fail(MFG_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
+    return launch_run(s, counts, opt);
+}
+
+int mfg_run_batch(mfg_sim* s, const uint64_t* counts, const mfg_run_options* opt, mfg_run_stats* stats) {
+    int rc = mfg_run_batch_async(s, counts, opt);
+    if (rc != MFG_OK) return rc;
+    return mfg_wait(s, -1, stats);
 }
 
 int mfg_poll(mfg_sim* s) {
@@ -467,40 +550,28 @@ int mfg_abort(mfg_sim* s) {
     return MFG_OK;
 }
 
-int mfg_fetch(mfg_sim* s, mfg_state_view* v) {
-    if (!s || !v) return fail(MFG_ERR_INVALID_ARGUMENT, "null argument");
-    std::lock_guard<std::mutex> lk(s->mu);
-    if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
+// Copy tallies of facets [fb, fb+nf), texture cells [tb, tb+nt), profiles [pb, pb+np),
+// angle-map cells [ab, ab+na) into a view laid out for exactly that range.
+static int fetch_range(mfg_sim* s, mfg_state_view* v, int fb, int nf, int64_t tb, int64_t nt, int64_t pb, int64_t np,
+                       int64_t ab, int64_t na, bool whole) {
     CK(cudaSetDevice(s->device));
     const mfg::HostModel& h = s->model->h;
     const double f = h.use_maxwell ? 1.0 : 1.1781;
-    std::vector<unsigned long long> g, fa, tx, pr, am;
-    g.resize(TG_N);
-    fa.resize(s->n_facet);
-    tx.resize(s->n_texture);
-    pr.resize(s->n_profile);
-    am.resize(s->n_anglemap);
+    const size_t B = 1 + size_t(h.nm);
+    const size_t NF = size_t(h.nf), NT = size_t(h.layout.texture_cells), NP = size_t(h.layout.profile_facets) * MFG_PROFILE_SIZE;
+    std::vector<unsigned long long> g(TG_N), fa(s->n_facet), tx(s->n_texture), pr(s->n_profile), am(s->n_anglemap);
     CK(cudaMemcpyAsync(g.data(), s->dt.global, TG_N * 8, cudaMemcpyDeviceToHost, s->stream));
     if (s->n_facet) CK(cudaMemcpyAsync(fa.data(), s->dt.facet, s->n_facet * 8, cudaMemcpyDeviceToHost, s->stream));
     if (s->n_texture && v->texture) CK(cudaMemcpyAsync(tx.data(), s->dt.texture, s->n_texture * 8, cudaMemcpyDeviceToHost, s->stream));
     if (s->n_profile && v->profile) CK(cudaMemcpyAsync(pr.data(), s->dt.profile, s->n_profile * 8, cudaMemcpyDeviceToHost, s->stream));
     if (s->n_anglemap && v->anglemap) CK(cudaMemcpyAsync(am.data(), s->dt.anglemap, s->n_anglemap * 8, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
-    if (v->global) {
-        std::fill(v->global, v->global + MFG_G_N, 0.0);
-        v->global[MFG_G_NBMCHIT] = double(g[TG_HITS]);
-        v->global[MFG_G_NBHITEQUIV] = double(g[TG_HITS]);
-        v->global[MFG_G_NBDESORBED] = double(g[TG_DES]);
-        v->global[MFG_G_NBABSEQUIV] = double(g[TG_ABS]);
-        v->global[MFG_G_NBLEAK] = double(g[TG_LEAK]);
-        v->global[MFG_G_DIST_TOTAL] = u128(&g[TG_DIST_LO]) / MFG_SCALE_DIST;
-        v->global[MFG_G_DIST_FULLHITS] = u128(&g[TG_DISTF_LO]) / MFG_SCALE_DIST;
-    }
-    const size_t B = 1 + size_t(h.nm);
+    uint64_t sh = 0, sd = 0, sa = 0;
     for (size_t m = 0; m < B; ++m)
-        for (int i = 0; i < h.nf; ++i) {
-            const unsigned long long* t = &fa[(m * h.nf + i) * TF_N];
-            size_t k = m * h.nf + i;
+        for (int i = 0; i < nf; ++i) {
+            const unsigned long long* t = &fa[(m * NF + fb + i) * TF_N];
+            size_t k = m * size_t(nf) + i;
+            if (m == 0) { sh += t[TF_HITS]; sd += t[TF_DES]; sa += t[TF_ABS]; }
             if (v->facet_counts) {
                 v->facet_counts[k * MFG_FC_N + MFG_FC_NBMCHIT] = t[TF_HITS];
                 v->facet_counts[k * MFG_FC_N + MFG_FC_NBDESORBED] = t[TF_DES];
@@ -515,31 +586,92 @@ int mfg_fetch(mfg_sim* s, mfg_state_view* v) {
                 o[MFG_FS_SUM_1_PER_VELOCITY] = u128(t + TF_S1V) / MFG_SCALE_INV;
             }
         }
-    if (v->texture) {
-        const size_t C = size_t(h.layout.texture_cells);
+    if (v->global) {
+        std::fill(v->global, v->global + MFG_G_N, 0.0);
+        if (whole) {
+            v->global[MFG_G_NBMCHIT] = double(g[TG_HITS]);
+            v->global[MFG_G_NBHITEQUIV] = double(g[TG_HITS]);
+            v->global[MFG_G_NBDESORBED] = double(g[TG_DES]);
+            v->global[MFG_G_NBABSEQUIV] = double(g[TG_ABS]);
+            v->global[MFG_G_NBLEAK] = double(g[TG_LEAK]);
+            v->global[MFG_G_DIST_TOTAL] = u128(&g[TG_DIST_LO]) / MFG_SCALE_DIST;
+            v->global[MFG_G_DIST_FULLHITS] = u128(&g[TG_DISTF_LO]) / MFG_SCALE_DIST;
+        } else {   // one instance of a batch: counters summed over its facets (leaks and distances are batch totals)
+            v->global[MFG_G_NBMCHIT] = double(sh);
+            v->global[MFG_G_NBHITEQUIV] = double(sh);
+            v->global[MFG_G_NBDESORBED] = double(sd);
+            v->global[MFG_G_NBABSEQUIV] = double(sa);
+        }
+    }
+    if (v->texture)
         for (size_t m = 0; m < B; ++m)
-            for (size_t c = 0; c < C; ++c) {
-                const unsigned long long* t = &tx[(m * C + c) * TT_N];
-                double* o = v->texture + (m * C + c) * 3;
+            for (int64_t c = 0; c < nt; ++c) {
+                const unsigned long long* t = &tx[(m * NT + tb + c) * TT_N];
+                double* o = v->texture + (m * size_t(nt) + c) * 3;
                 o[0] = double(t[TT_COUNT]);
-                o[1] = u128(t + TT_SVORT) / MFG_SCALE_V * f * h.tex_inc[c];
+                o[1] = u128(t + TT_SVORT) / MFG_SCALE_V * f * h.tex_inc[tb + c];
                 o[2] = u128(t + TT_S1OV) / MFG_SCALE_INV / f;
             }
-    }
-    if (v->profile) {
-        const size_t P = size_t(h.layout.profile_facets) * MFG_PROFILE_SIZE;
+    if (v->profile)
         for (size_t m = 0; m < B; ++m)
-            for (size_t c = 0; c < P; ++c) {
-                const unsigned long long* t = &pr[(m * P + c) * TT_N];
-                double* o = v->profile + (m * P + c) * 3;
+            for (int64_t c = 0; c < np * MFG_PROFILE_SIZE; ++c) {
+                const unsigned long long* t = &pr[(m * NP + pb * MFG_PROFILE_SIZE + c) * TT_N];
+                double* o = v->profile + (m * size_t(np) * MFG_PROFILE_SIZE + c) * 3;
                 o[0] = double(t[TT_COUNT]);
                 o[1] = u128(t + TT_SVORT) / MFG_SCALE_V * f;
                 o[2] = u128(t + TT_S1OV) / MFG_SCALE_INV;
             }
-    }
     if (v->anglemap)
-        for (size_t c = 0; c < s->n_anglemap; ++c) v->anglemap[c] = am[c];
-    if (v->direction) std::fill(v->direction, v->direction + h.layout.n_direction, 0.0);
+        for (int64_t c = 0; c < na; ++c) v->anglemap[c] = am[ab + c];
+    if (v->direction) {
+        int64_t nd = 0;
+        for (int i = 0; i < nf; ++i)
+            if (h.dir_off.size() > size_t(fb + i) && h.dir_off[fb + i] >= 0) nd += int64_t(h.tex_w[fb + i]) * h.tex_h[fb + i];
+        std::fill(v->direction, v->direction + B * size_t(nd) * 4, 0.0);
+    }
+    return MFG_OK;
+}
+
+int mfg_fetch(mfg_sim* s, mfg_state_view* v) {
+    if (!s || !v) return fail(MFG_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
+    const mfg::HostModel& h = s->model->h;
+    return fetch_range(s, v, 0, h.nf, 0, h.layout.texture_cells, 0, h.layout.profile_facets, 0, h.layout.anglemap_cells, true);
+}
+
+int mfg_fetch_instance(mfg_sim* s, int32_t i, mfg_state_view* v) {
+    if (!s || !v) return fail(MFG_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
+    const mfg::HostModel& h = s->model->h;
+    if (i < 0 || i >= int(h.instances.size())) return fail(MFG_ERR_INVALID_ARGUMENT, "instance index out of range");
+    const auto& in = h.instances[i];
+    return fetch_range(s, v, in.facet_base, in.nf, in.tex_base, in.layout.texture_cells, in.prof_base,
+                       in.layout.profile_facets, in.ang_base, in.layout.anglemap_cells, h.instances.size() == 1);
+}
+
+int mfg_model_merge(const mfg_model* const* models, int32_t n, mfg_model** out) {
+    if (!models || n <= 0 || !out) return fail(MFG_ERR_INVALID_ARGUMENT, "bad argument");
+    *out = nullptr;
+    std::vector<const mfg::HostModel*> parts;
+    for (int i = 0; i < n; ++i) {
+        if (!models[i]) return fail(MFG_ERR_INVALID_ARGUMENT, "null model in batch");
+        parts.push_back(&models[i]->h);
+    }
+    auto* m = new mfg_model();
+    std::string err;
+    int rc = mfg::merge_host_models(parts, m->h, err);
+    if (rc != MFG_OK) { delete m; return fail(rc, err); }
+    *out = m;
+    return MFG_OK;
+}
+
+int32_t mfg_model_instances(const mfg_model* m) { return m ? int32_t(m->h.instances.size()) : 0; }
+
+int mfg_instance_layout(const mfg_model* m, int32_t i, mfg_state_layout* out) {
+    if (!m || !out || i < 0 || i >= int(m->h.instances.size())) return fail(MFG_ERR_INVALID_ARGUMENT, "bad argument");
+    *out = m->h.instances[i].layout;
     return MFG_OK;
 }
 

@@ -175,6 +175,11 @@ struct DevModel {
     int64_t profile_facets;
     int64_t anglemap_cells;
     double scene_scale;          // max |coordinate| of the scene (for FP32 tolerances)
+    // instances of a batch (one for a plain model): source-table range and total weight
+    int32_t n_inst, pad1;
+    const int32_t* inst_src_base;
+    const int32_t* inst_src_count;
+    const double* inst_src_total;
 };
 
 struct DevTally {
@@ -185,14 +190,22 @@ struct DevTally {
     unsigned long long* anglemap;    // anglemap_cells
 };
 
-struct LaunchCtl {
-    unsigned long long* next_particle;   // work counter (particles handed out)
-    unsigned long long first_particle;   // Philox counter of particle 0 of this run
-    unsigned long long n_particles;
+// Per-run values live in device memory so one captured CUDA graph serves every run:
+// the host fills a pinned staging copy and the graph's first node copies it over.
+struct RunDesc {
+    unsigned long long n_total;          // particles of all instances
     unsigned long long max_steps;
     unsigned long long time_limit_ns;    // a warp stops this long after it started
-    uint32_t key0, key1;
-    const volatile int* abort_flag;      // host-mapped
-    int smem_textures;                   // 1: moment-0 texture partials in shared memory
-    int smem_facets;                     // 1: moment-0 facet partials in shared memory
+    uint32_t key0, key1;                 // Philox key
+    int32_t n_inst, pad;
+    // followed in memory by inst_prefix[n_inst + 1] and inst_first[n_inst] (u64)
+};
+
+struct LaunchCtl {
+    unsigned long long* next_particle;   // work counter (particles handed out)
+    const RunDesc* run;
+    const unsigned long long* inst_prefix;   // particle index ranges per instance
+    const unsigned long long* inst_first;    // Philox counter of each instance's first particle
+    const volatile int* abort_flag;          // host-mapped
+    int smem_facets;                         // 1: moment-0 facet partials in shared memory
 };

@@ -771,6 +771,122 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
         i2.temperature = m.temperature[i];
         for (int a = 0; a < 3; ++a) m.centers[3 * i + a] = F.center[a];
     }
+    HostModel::Instance inst;
+    inst.nf = nf;
+    inst.nstruct = m.nstruct;
+    inst.nsrc = int(m.src_facet.size());
+    inst.src_total = m.src_total;
+    inst.layout = m.layout;
+    m.instances.assign(1, inst);
+    return MFG_OK;
+}
+
+int merge_host_models(const std::vector<const HostModel*>& parts, HostModel& out, std::string& err) {
+    if (parts.empty()) { err = "no models to merge"; return MFG_ERR_INVALID_ARGUMENT; }
+    const HostModel& p0 = *parts[0];
+    for (const HostModel* p : parts) {
+        if (p->instances.size() != 1) { err = "merged models cannot be merged again"; return MFG_ERR_INVALID_ARGUMENT; }
+        if (p->gas_mass != p0.gas_mass || p->use_maxwell != p0.use_maxwell || p->constant_flow != p0.constant_flow ||
+            p->enable_decay != p0.enable_decay || p->half_life != p0.half_life || p->time_window != p0.time_window ||
+            p->mstart != p0.mstart || p->mend != p0.mend || p->low_flux != p0.low_flux) {
+            err = "batched models must share gas, speed law, flow mode, decay and moments";
+            return MFG_ERR_INVALID_ARGUMENT;
+        }
+    }
+    out = HostModel();
+    out.nm = p0.nm;
+    out.gas_mass = p0.gas_mass; out.time_window = p0.time_window; out.half_life = p0.half_life;
+    out.low_flux_cutoff = p0.low_flux_cutoff; out.use_maxwell = p0.use_maxwell;
+    out.constant_flow = p0.constant_flow; out.enable_decay = p0.enable_decay; out.low_flux = p0.low_flux;
+    out.latest = p0.latest; out.mstart = p0.mstart; out.mend = p0.mend; out.maxwin = p0.maxwin;
+    std::copy(p0.cdf_v, p0.cdf_v + MFG_MAXWELL_N, out.cdf_v);
+    std::copy(p0.cdf_p, p0.cdf_p + MFG_MAXWELL_N, out.cdf_p);
+    out.par_start.assign(1, 0);
+    out.id_start.assign(1, 0);
+    out.layout = mfg_state_layout{};
+    out.layout.n_moments = p0.nm;
+    out.nstruct = 0;
+    out.bvh_depth = 0;
+    out.scene_scale = 0;
+    for (const HostModel* pp : parts) {
+        const HostModel& p = *pp;
+        HostModel::Instance in = p.instances[0];
+        in.facet_base = out.nf;
+        in.struct_base = out.nstruct;
+        in.src_base = int(out.src_facet.size());
+        in.tex_base = out.layout.texture_cells;
+        in.prof_base = out.layout.profile_facets;
+        in.ang_base = out.layout.anglemap_cells;
+        in.dir_base = out.layout.direction_cells;
+        const int node_base = int(out.nodes_d.size()), prim_base = int(out.prims.size());
+        const int v2_base = int(out.v2_d.size()), par_base = int(out.par_logx.size()), id_base = int(out.id_start.size()) - 1;
+        if (!p.gpu_supported && out.gpu_supported) { out.gpu_supported = false; out.gpu_unsupported_reason = p.gpu_unsupported_reason; }
+        for (NodeD nd : p.nodes_d) {
+            if (nd.b >= 0) nd.a += node_base; else nd.a += prim_base;
+            out.nodes_d.push_back(nd);
+        }
+        for (NodeF nd : p.nodes_f) {
+            if (nd.b >= 0) nd.a += node_base; else nd.a += prim_base;
+            out.nodes_f.push_back(nd);
+        }
+        for (int r : p.roots) out.roots.push_back(r + node_base);
+        for (int f : p.prims) out.prims.push_back(f + in.facet_base);
+        out.isect_d.insert(out.isect_d.end(), p.isect_d.begin(), p.isect_d.end());
+        out.isect_f.insert(out.isect_f.end(), p.isect_f.begin(), p.isect_f.end());
+        for (PolyD q : p.poly_d) { q.vstart += v2_base; out.poly_d.push_back(q); }
+        for (PolyF q : p.poly_f) { q.vstart += v2_base; out.poly_f.push_back(q); }
+        out.v2_d.insert(out.v2_d.end(), p.v2_d.begin(), p.v2_d.end());
+        out.v2_f.insert(out.v2_f.end(), p.v2_f.begin(), p.v2_f.end());
+        out.phys_d.insert(out.phys_d.end(), p.phys_d.begin(), p.phys_d.end());
+        out.phys_f.insert(out.phys_f.end(), p.phys_f.begin(), p.phys_f.end());
+        for (FacetInfo fi : p.info) {
+            if (fi.tex_off >= 0) fi.tex_off += int32_t(in.tex_base);
+            if (fi.prof_idx >= 0) fi.prof_idx += int32_t(in.prof_base);
+            if (fi.ang_off >= 0) fi.ang_off += int32_t(in.ang_base);
+            out.info.push_back(fi);
+        }
+        for (FacetInfo2 f2 : p.info2) {
+            if (f2.structure >= 0) f2.structure += in.struct_base;
+            if (f2.stick_param >= 0) f2.stick_param += par_base;
+            if (f2.temp_param >= 0) f2.temp_param += par_base;
+            out.info2.push_back(f2);
+        }
+        out.centers.insert(out.centers.end(), p.centers.begin(), p.centers.end());
+        out.src_cdf.insert(out.src_cdf.end(), p.src_cdf.begin(), p.src_cdf.end());
+        for (int f : p.src_facet) out.src_facet.push_back(f + in.facet_base);
+        for (int k : p.src_id) out.src_id.push_back(k >= 0 ? k + id_base : -1);
+        for (size_t k = 1; k < p.id_start.size(); ++k) out.id_start.push_back(p.id_start[k] + int32_t(out.id_t.size()));
+        out.id_t.insert(out.id_t.end(), p.id_t.begin(), p.id_t.end());
+        out.id_cum.insert(out.id_cum.end(), p.id_cum.begin(), p.id_cum.end());
+        for (size_t k = 1; k < p.par_start.size(); ++k) out.par_start.push_back(p.par_start[k] + int32_t(out.par_t.size()));
+        out.par_t.insert(out.par_t.end(), p.par_t.begin(), p.par_t.end());
+        out.par_v.insert(out.par_v.end(), p.par_v.begin(), p.par_v.end());
+        out.par_logx.insert(out.par_logx.end(), p.par_logx.begin(), p.par_logx.end());
+        out.par_logy.insert(out.par_logy.end(), p.par_logy.begin(), p.par_logy.end());
+        out.tex_inc.insert(out.tex_inc.end(), p.tex_inc.begin(), p.tex_inc.end());
+        out.facets.insert(out.facets.end(), p.facets.begin(), p.facets.end());
+        out.nf += p.nf;
+        out.nstruct += p.nstruct;
+        out.layout.texture_cells += p.layout.texture_cells;
+        out.layout.profile_facets += p.layout.profile_facets;
+        out.layout.anglemap_cells += p.layout.anglemap_cells;
+        out.layout.direction_cells += p.layout.direction_cells;
+        out.bvh_depth = std::max(out.bvh_depth, p.bvh_depth);
+        out.bvh_leaves += p.bvh_leaves;
+        out.scene_scale = std::max(out.scene_scale, p.scene_scale);
+        out.instances.push_back(in);
+    }
+    mfg_state_layout& L = out.layout;
+    const int64_t B = 1 + out.nm;
+    L.n_facets = out.nf;
+    L.n_global = MFG_G_N;
+    L.n_facet_counts = B * out.nf * MFG_FC_N;
+    L.n_facet_sums = B * out.nf * MFG_FS_N;
+    L.n_texture = B * L.texture_cells * 3;
+    L.n_profile = B * L.profile_facets * MFG_PROFILE_SIZE * 3;
+    L.n_direction = B * L.direction_cells * 4;
+    L.n_anglemap = L.anglemap_cells;
+    out.src_total = 0;
     return MFG_OK;
 }
 

@@ -77,7 +77,19 @@ struct HostModel {
     double scene_scale = 1;
     bool gpu_supported = true;
     std::string gpu_unsupported_reason;
+    // instances (one for a plain model; several after merge_host_models)
+    struct Instance {
+        int facet_base = 0, nf = 0, struct_base = 0, nstruct = 1, src_base = 0, nsrc = 0;
+        int64_t tex_base = 0, prof_base = 0, ang_base = 0, dir_base = 0;
+        double src_total = 0;
+        mfg_state_layout layout{};
+    };
+    std::vector<Instance> instances;
 };
+
+// Merge prepared models into one multi-instance model (batch of independent geometries).
+// All parts must share the global settings (gas, speed law, flow mode, moments).
+int merge_host_models(const std::vector<const HostModel*>& parts, HostModel& out, std::string& err);
 
 // Build a HostModel from a descriptor.  Returns MFG_OK or an error code with a message.
 int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, int leaf_max = 2);

@@ -49,14 +49,17 @@ __device__ __forceinline__ float u01f(uint32_t a) {
 }
 
 // double stream: two uniforms per Philox block (the CPU oracle's order)
+// counter = (particle id lo, hi, draw index, instance)
 struct RngD {
-    uint32_t p0, p1, ctr, k0, k1;
+    uint32_t p0, p1, ctr, k0, k1, inst;
     bool have;
     double cache;
-    __device__ void start(uint64_t pid) { p0 = (uint32_t)pid; p1 = (uint32_t)(pid >> 32); ctr = 0; have = false; }
+    __device__ void start(uint64_t pid, uint32_t instance) {
+        p0 = (uint32_t)pid; p1 = (uint32_t)(pid >> 32); ctr = 0; inst = instance; have = false;
+    }
     __device__ double next() {
         if (have) { have = false; return cache; }
-        uint32_t c0 = p0, c1 = p1, c2 = ctr++, c3 = 0u;
+        uint32_t c0 = p0, c1 = p1, c2 = ctr++, c3 = inst;
         philox4x32_10(c0, c1, c2, c3, k0, k1);
         cache = u01d(c2, c3);
         have = true;
@@ -65,13 +68,15 @@ struct RngD {
 };
 // float stream: four uniforms per Philox block
 struct RngF {
-    uint32_t p0, p1, ctr, k0, k1;
+    uint32_t p0, p1, ctr, k0, k1, inst;
     uint32_t w[4];
     int n;
-    __device__ void start(uint64_t pid) { p0 = (uint32_t)pid; p1 = (uint32_t)(pid >> 32); ctr = 0; n = 0; }
+    __device__ void start(uint64_t pid, uint32_t instance) {
+        p0 = (uint32_t)pid; p1 = (uint32_t)(pid >> 32); ctr = 0; inst = instance; n = 0;
+    }
     __device__ float next() {
         if (n == 0) {
-            uint32_t c0 = p0, c1 = p1, c2 = ctr++, c3 = 0u;
+            uint32_t c0 = p0, c1 = p1, c2 = ctr++, c3 = inst;
             philox4x32_10(c0, c1, c2, c3, k0, k1);
             w[0] = c0; w[1] = c1; w[2] = c2; w[3] = c3;
             n = 4;
@@ -210,7 +215,6 @@ struct Real_<true> {
 struct ParticleState {
     double ox, oy, oz;
     double time, decay_at;
-    double u, v;              // (u,v) of the current facet (facetHitDetails)
     uint64_t bounces;
     int last, structure;
 };
@@ -307,6 +311,89 @@ __device__ __forceinline__ void polar_dir(const DevModel& M, int f, R ct, R r2, 
     }
 }
 
+// Desorption time from a facet's integrated desorption table (Physics.cpp:11-19)
+__device__ __noinline__ double desorption_time(const DevModel& M, int idt, double r) {
+    int s = M.id_start[idt], e = M.id_start[idt + 1];
+    return interp_x_d(r * M.id_cum[e - 1], M.id_t + s, M.id_cum + s, e - s);
+}
+
+// point-in-polygon in FP32 for start points (FP32R kernel)
+__device__ __forceinline__ bool in_facet_f(const DevModel& M, int f, float u, float v) {
+    const PolyF P = M.poly_f[f];
+    if (P.rin2 > 1e29f) return true;
+    float du = (u - P.cu) * P.su, dv = (v - P.cv) * P.sv;
+    float r2 = du * du + dv * dv;
+    if (r2 < P.rin2) return true;
+    if (r2 > P.rout2) return false;
+    bool in = false;
+    float2 pj = M.v2_f[P.vstart + P.nv - 1];
+    for (int i = 0; i < P.nv; ++i) {
+        float2 pi = M.v2_f[P.vstart + i];
+        if ((pi.y > v) != (pj.y > v)) {
+            float cr = (pj.x - pi.x) * (v - pi.y) - (u - pi.x) * (pj.y - pi.y);
+            if ((cr > 0) == (pj.y > pi.y)) in = !in;
+        }
+        pj = pi;
+    }
+    return in;
+}
+
+// Start point of a desorption: uniform (u,v) in the bounding rectangle until inside the polygon,
+// at most 1000 tries, else the facet centre (Particle.cpp:513-570).  The point is formed in FP64.
+template <bool kFP32, class Rng, class R>
+__device__ __noinline__ void start_point(const DevModel& M, int fo, Rng& rng, double& ox, double& oy, double& oz,
+                                         R& pu, R& pv) {
+    const FacetIsectD& Rr = M.isect_d[fo];
+    const PolyD& PP = M.poly_d[fo];
+    bool found = false;
+    double su = 0.5, sv = 0.5;
+    for (int tr = 0; tr < 1000 && !found; ++tr) {
+        R u = (R)rng.next(), v = (R)rng.next();
+        bool in = kFP32 ? in_facet_f(M, fo, (float)u, (float)v) : in_facet_d(M, fo, (double)u, (double)v);
+        if (in) { su = (double)u; sv = (double)v; found = true; }
+    }
+    if (found) {
+        double a = su * PP.su * PP.su, b = sv * PP.sv * PP.sv;   // O + u*U + v*V (record keeps U/|U|^2)
+        ox = Rr.v[4] + a * Rr.v[8] + b * Rr.v[12];
+        oy = Rr.v[5] + a * Rr.v[9] + b * Rr.v[13];
+        oz = Rr.v[6] + a * Rr.v[10] + b * Rr.v[14];
+    } else {
+        ox = M.center[3 * fo];
+        oy = M.center[3 * fo + 1];
+        oz = M.center[3 * fo + 2];
+    }
+    pu = (R)su;
+    pv = (R)sv;
+}
+
+// texture cell index floor(u*w) + floor(v*h)*width of a facet (RecordHitOnTexture, Particle.cpp:981-983)
+template <bool kFP32, class R>
+__device__ __forceinline__ int texture_cell(const DevModel& M, int f, R u, R v) {
+    const FacetInfo& In = M.info[f];
+    if (In.tex_off < 0) return -1;
+    int tu, tv;
+    if (kFP32) { tu = (int)((float)u * M.phys_f[f].texw_p); tv = (int)((float)v * M.phys_f[f].texh_p); }
+    else { tu = (int)((double)u * M.phys_d[f].texw_p); tv = (int)((double)v * M.phys_d[f].texh_p); }
+    tu = min(max(tu, 0), In.tex_w - 1);
+    tv = min(max(tv, 0), In.tex_h - 1);
+    return In.tex_off + tu + tv * In.tex_w;
+}
+
+// Time-moment tallies of one event (moments >= 1): facet counter, texture cell, profile
+__device__ __noinline__ void tally_moments(const DevModel& M, const DevTally& T, const BlockTally& B, int f, double time,
+                                           unsigned long long des, unsigned long long hits, unsigned long long abs_,
+                                           unsigned long long s1ov, unsigned long long svort, unsigned long long s1v,
+                                           int cell, unsigned long long cell_count, bool count_hit,
+                                           unsigned long long vf, double cosn, double vel, double u, double v,
+                                           unsigned long long q1, unsigned long long q2) {
+    const bool prof = (M.info[f].flags & FF_PROFILE) != 0;
+    for_moments(M, time, [&](int m) {
+        facet_add(M, T, B, f, m, hits, des, abs_, s1ov, svort, s1v);
+        if (cell >= 0) cell_add(T.texture + ((size_t)m * M.texture_cells + cell) * TT_N, cell_count, s1ov, svort);
+        if (prof) profile_add(M, T, f, m, count_hit, vf, 1, cosn, vel, u, v, q1, q2);
+    });
+}
+
 // General relaunch (any accommodation, temperature parameter, sojourn time, reflection
 // mix): UpdateVelocity, sojourn, diffuse / specular / cos^N direction, with the random
 // numbers drawn in the order of PerformBounce (Particle.cpp:769-802).
@@ -382,18 +469,21 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
     unsigned long long pool_next = 0, pool_end = 0;   // warp pool of particle ids
     const unsigned long long chunk = 64;
 
+    const unsigned long long n_total = C.run->n_total;
+    const unsigned long long max_steps = C.run->max_steps;
+    const int n_inst = C.run->n_inst;
     typename std::conditional<kFP32, RngF, RngD>::type rng;
-    rng.k0 = C.key0;
-    rng.k1 = C.key1;
+    rng.k0 = C.run->key0;
+    rng.k1 = C.run->key1;
     ParticleState P;
     P.ox = P.oy = P.oz = 0;
     P.time = 0;
     P.decay_at = 1e100;
-    P.u = P.v = 0;
     P.bounces = 0;
     P.last = -1;
     P.structure = 0;
     R dx = 0, dy = 0, dz = 0, vel = 1;
+    R pu = 0, pv = 0;         // (u,v) on the current facet (facetHitDetails)
     bool active = true;       // lane still has particles to trace
     bool need_new = true;     // lane must desorb a new particle
     // incoming half of the last reflection, added together with the outgoing half (moment 0)
@@ -406,7 +496,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
     unsigned long long c_dist = 0, c_distf = 0;
     unsigned long long deadline;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(deadline));
-    deadline += C.time_limit_ns;
+    deadline += C.run->time_limit_ns;
 
     auto flush_pending = [&]() {
         if (!pend) return;
@@ -454,100 +544,47 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                 if (want) P.bounces = pool_next + rank;
                 pool_next += n;
             }
-            if (want && P.bounces >= C.n_particles) { active = false; want = false; }
+            if (want && P.bounces >= n_total) { active = false; want = false; }
         }
         if (!active) continue;
 
-        // ---- 1. emit a direction: desorption or reflection from facet fo ----
-        int fo;
-        if (want) {
-            // StartFromSource (Particle.cpp:407-685)
-            rng.start(C.first_particle + P.bounces);
-            double sr = (double)rng.next() * M.src_total;
-            int lo = 0, hi = M.n_src;
-            while (lo < hi) { int mid = (lo + hi) >> 1; if (M.src_cdf[mid] > sr) hi = mid; else lo = mid + 1; }
-            if (lo >= M.n_src) lo = M.n_src - 1;
-            fo = M.src_facet[lo];
-            const FacetInfo& In = M.info[fo];
-            const FacetInfo2& I2 = M.info2[fo];
-            bool flip = (In.flags & FF_TWO_SIDED) ? ((double)rng.next() > 0.5) : false;
-            int idt = M.src_id[lo];
-            if (idt >= 0) {
-                int s = M.id_start[idt], e = M.id_start[idt + 1];
-                double r = (double)rng.next() * M.id_cum[e - 1];
-                P.time = interp_x_d(r, M.id_t + s, M.id_cum + s, e - s);
-            } else {
-                P.time = (double)rng.next() * M.latest;
+        // ---- 1. emit: desorption (want) or reflection from P.last.  The two share the speed,
+        //      direction and tally code; only short prologues differ.  Random numbers are drawn in
+        //      the reference's order: desorption = source, [reverse], time, speed, [decay], (u,v)..., theta,
+        //      phi (Particle.cpp:418-625); reflection = speed, [sojourn], [type], theta, phi (:769-802).
+        const bool des = want;
+        int fo, law;              // law: 0 cosine, 1 uniform, 2 cos^N, 3 general reflection
+        bool flip = false;
+        R lexp = 0;
+        if (des) {
+            int inst = 0;
+            if (n_inst > 1) {
+                int a = 0, b = n_inst;   // last instance whose prefix <= id
+                while (b - a > 1) { int mid = (a + b) >> 1; if (C.inst_prefix[mid] <= P.bounces) a = mid; else b = mid; }
+                inst = a;
             }
+            rng.start(C.inst_first[inst] + (P.bounces - C.inst_prefix[inst]), (uint32_t)inst);
+            // source facet by cumulative outgassing (Particle.cpp:418-464)
+            const int sbase = M.inst_src_base[inst], scount = M.inst_src_count[inst];
+            double sr = (double)rng.next() * M.inst_src_total[inst];
+            int lo = 0, hi = scount;
+            while (lo < hi) { int mid = (lo + hi) >> 1; if (M.src_cdf[sbase + mid] > sr) hi = mid; else lo = mid + 1; }
+            if (lo >= scount) lo = scount - 1;
+            lo += sbase;
+            fo = M.src_facet[lo];
+            const FacetInfo2& I2 = M.info2[fo];
+            if (M.info[fo].flags & FF_TWO_SIDED) flip = (double)rng.next() > 0.5;
+            int idt = M.src_id[lo];
+            if (idt >= 0) P.time = desorption_time(M, idt, (double)rng.next());
+            else P.time = (double)rng.next() * M.latest;
             P.structure = I2.structure;
             P.bounces = 0;
-            if (M.use_maxwell) {
-                if (kFP32) vel = (R)(M.phys_f[fo].sqrtT * interp_x_f((float)rng.next(), s_cdf_vf, s_cdf_pf, MFG_MAXWELL_N));
-                else vel = (R)(M.phys_d[fo].sqrtT * interp_x_d((double)rng.next(), s_cdf_v, s_cdf_p, MFG_MAXWELL_N));
-            } else {
-                vel = (R)(145.469 * sqrt(I2.temperature / M.gas_mass));
-            }
-            P.decay_at = M.enable_decay ? P.time - 1.44269 * M.half_life * log(1.0 - (double)rng.next()) : 1e100;
-            // start point: rejection in the (u,v) rectangle, at most 1000 tries (Particle.cpp:513-570)
-            const FacetIsectD& Rr = M.isect_d[fo];
-            const PolyD& PP = M.poly_d[fo];
-            bool found = false;
-            double su = 0.5, sv = 0.5;
-            for (int tr = 0; tr < 1000 && !found; ++tr) {
-                double u = (double)rng.next(), v = (double)rng.next();
-                if (in_facet_d(M, fo, u, v)) { su = u; sv = v; found = true; }
-            }
-            if (found) {
-                double a = su * PP.su * PP.su, b = sv * PP.sv * PP.sv;   // O + u*U + v*V (record keeps U/|U|^2)
-                P.ox = Rr.v[4] + a * Rr.v[8] + b * Rr.v[12];
-                P.oy = Rr.v[5] + a * Rr.v[9] + b * Rr.v[13];
-                P.oz = Rr.v[6] + a * Rr.v[10] + b * Rr.v[14];
-            } else {
-                P.ox = M.center[3 * fo];
-                P.oy = M.center[3 * fo + 1];
-                P.oz = M.center[3 * fo + 2];
-            }
-            P.u = su;
-            P.v = sv;
-            P.last = fo;
-            R r1 = (R)rng.next(), r2 = (R)rng.next();
-            R ct;
-            if (I2.desorb_type == MFG_DES_UNIFORM) ct = r1;
-            else if (I2.desorb_type == MFG_DES_COSINE_N) ct = (R)pow((double)r1, 1.0 / (I2.desorb_exp + 1.0));
-            else ct = (R)sqrt(r1);
-            polar_dir<kFP32>(M, fo, ct, r2, flip, dx, dy, dz);
-            // desorption tallies (Particle.cpp:646-680)
-            double cosn = kFP32 ? (double)fabsf(dx * M.phys_f[fo].N[0] + dy * M.phys_f[fo].N[1] + dz * M.phys_f[fo].N[2])
-                                : fabs((double)dx * Rr.v[0] + (double)dy * Rr.v[1] + (double)dz * Rr.v[2]);
-            R ort = vel * (R)cosn;
-            unsigned long long q1 = kFP32 ? qf(1.0f / (float)ort, (float)MFG_SCALE_INV) : qd(1.0 / (double)ort, MFG_SCALE_INV);
-            unsigned long long q2 = kFP32 ? qf((float)ort, (float)MFG_SCALE_V) : qd((double)ort, MFG_SCALE_V);
-            unsigned long long q3 = kFP32 ? qf(1.0f / (float)vel, (float)MFG_SCALE_INV) : qd(1.0 / (double)vel, MFG_SCALE_INV);
-            ++c_des;
-            int cell = -1;
-            if ((In.count & MFG_COUNT_DES) && In.tex_off >= 0) {
-                double tw = kFP32 ? (double)M.phys_f[fo].texw_p : M.phys_d[fo].texw_p;
-                double th = kFP32 ? (double)M.phys_f[fo].texh_p : M.phys_d[fo].texh_p;
-                int tu = (int)(su * tw), tv = (int)(sv * th);
-                tu = min(max(tu, 0), In.tex_w - 1);
-                tv = min(max(tv, 0), In.tex_h - 1);
-                cell = In.tex_off + tu + tv * In.tex_w;
-            }
-            facet_add(M, T, B, fo, 0, 0, 1, 0, 2 * q1, q2, q3);
-            if (cell >= 0) cell_add(T.texture + (size_t)cell * TT_N, 1, 2 * q1, q2);
-            if (In.flags & FF_PROFILE) profile_add(M, T, fo, 0, false, 2, 1, cosn, (double)vel, su, sv, q1, q2);
-            for_moments(M, P.time, [&](int m) {
-                facet_add(M, T, B, fo, m, 0, 1, 0, 2 * q1, q2, q3);
-                if (cell >= 0) cell_add(T.texture + ((size_t)m * M.texture_cells + cell) * TT_N, 1, 2 * q1, q2);
-                if (In.flags & FF_PROFILE) profile_add(M, T, fo, m, false, 2, 1, cosn, (double)vel, su, sv, q1, q2);
-            });
-            need_new = false;
+            law = I2.desorb_type == MFG_DES_UNIFORM ? 1 : (I2.desorb_type == MFG_DES_COSINE_N ? 2 : 0);
+            lexp = (R)I2.desorb_exp;
+            if (!M.use_maxwell) law |= 4;   // fixed speed 145.469 sqrt(T/m) (Particle.cpp:483)
         } else {
-            // relaunch half of PerformBounce (Particle.cpp:769-836)
             fo = P.last;
-            const FacetInfo& In = M.info[fo];
-            bool flip = false;
-            if (In.flags & FF_TWO_SIDED) {
+            if (M.info[fo].flags & FF_TWO_SIDED) {
                 if (kFP32) {
                     const FacetPhysF& Pf = M.phys_f[fo];
                     flip = (dx * Pf.N[0] + dy * Pf.N[1] + dz * Pf.N[2]) > 0.0f;
@@ -556,69 +593,89 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                     flip = ((double)dx * Rf.v[0] + (double)dy * Rf.v[1] + (double)dz * Rf.v[2]) > 0.0;
                 }
             }
-            if (In.flags & FF_FAST_REFL) {
-                // UpdateVelocity with full accommodation and Maxwell speeds, then a diffuse direction
-                if (kFP32) vel = (R)(M.phys_f[fo].sqrtT * interp_x_f((float)rng.next(), s_cdf_vf, s_cdf_pf, MFG_MAXWELL_N));
-                else vel = (R)(M.phys_d[fo].sqrtT * interp_x_d((double)rng.next(), s_cdf_v, s_cdf_p, MFG_MAXWELL_N));
-                R r1 = (R)rng.next(), r2 = (R)rng.next();
-                polar_dir<kFP32>(M, fo, (R)sqrt(r1), r2, flip, dx, dy, dz);
-            } else {
-                reflect_general<kFP32>(M, fo, flip, rng, P.time, vel, dx, dy, dz, s_cdf_v, s_cdf_p, s_cdf_vf, s_cdf_pf);
-            }
-            const FacetIsectD& Rr = M.isect_d[fo];
-            double cosn = kFP32 ? (double)fabsf(dx * M.phys_f[fo].N[0] + dy * M.phys_f[fo].N[1] + dz * M.phys_f[fo].N[2])
-                                : fabs((double)dx * Rr.v[0] + (double)dy * Rr.v[1] + (double)dz * Rr.v[2]);
-            R ort = vel * (R)cosn;
+            law = (M.info[fo].flags & FF_FAST_REFL) ? 0 : 3;
+        }
+        // speed: Maxwell at the facet temperature (desorption and full-accommodation reflection)
+        if (law < 3) {
+            if (kFP32) vel = (R)(M.phys_f[fo].sqrtT * interp_x_f((float)rng.next(), s_cdf_vf, s_cdf_pf, MFG_MAXWELL_N));
+            else vel = (R)(M.phys_d[fo].sqrtT * interp_x_d((double)rng.next(), s_cdf_v, s_cdf_p, MFG_MAXWELL_N));
+        } else if (law & 4) {
+            vel = (R)(145.469 * sqrt(M.info2[fo].temperature / M.gas_mass));
+            law &= 3;
+        }
+        if (des) {
+            P.decay_at = M.enable_decay ? P.time - 1.44269 * M.half_life * log(1.0 - (double)rng.next()) : 1e100;
+            // start point: rejection in the (u,v) rectangle, at most 1000 tries (Particle.cpp:513-570)
+            start_point<kFP32>(M, fo, rng, P.ox, P.oy, P.oz, pu, pv);
+            P.last = fo;
+        }
+        if (law == 3) {
+            reflect_general<kFP32>(M, fo, flip, rng, P.time, vel, dx, dy, dz, s_cdf_v, s_cdf_p, s_cdf_vf, s_cdf_pf);
+        } else {
+            R r1 = (R)rng.next(), r2 = (R)rng.next();
+            R ct = law == 1 ? r1 : (law == 2 ? (R)pow((double)r1, 1.0 / ((double)lexp + 1.0)) : (R)sqrt(r1));
+            polar_dir<kFP32>(M, fo, ct, r2, flip, dx, dy, dz);
+        }
+        {
+            // outgoing tallies; a reflection's incoming half (pending) is added with them (moment 0)
+            const FacetInfo& In = M.info[fo];
+            R cosn;
+            if (kFP32) cosn = fabsf(dx * M.phys_f[fo].N[0] + dy * M.phys_f[fo].N[1] + dz * M.phys_f[fo].N[2]);
+            else cosn = (R)fabs((double)dx * M.isect_d[fo].v[0] + (double)dy * M.isect_d[fo].v[1] + (double)dz * M.isect_d[fo].v[2]);
+            R ort = vel * cosn;
             unsigned long long q1 = kFP32 ? qf(1.0f / (float)ort, (float)MFG_SCALE_INV) : qd(1.0 / (double)ort, MFG_SCALE_INV);
             unsigned long long q2 = kFP32 ? qf((float)ort, (float)MFG_SCALE_V) : qd((double)ort, MFG_SCALE_V);
-            // moment 0: incoming and outgoing halves together
-            pend_s1ov += q1;
-            pend_svort += q2;
-            flush_pending();
-            int cell = -1;
-            if ((In.count & MFG_COUNT_REFL) && In.tex_off >= 0) {
-                double tw = kFP32 ? (double)M.phys_f[fo].texw_p : M.phys_d[fo].texw_p;
-                double th = kFP32 ? (double)M.phys_f[fo].texh_p : M.phys_d[fo].texh_p;
-                int tu = (int)(P.u * tw), tv = (int)(P.v * th);
-                tu = min(max(tu, 0), In.tex_w - 1);
-                tv = min(max(tv, 0), In.tex_h - 1);
-                cell = In.tex_off + tu + tv * In.tex_w;
+            unsigned long long q3 = 0;
+            int cell = pend_cell;
+            if (des) {
+                ++c_des;
+                q3 = kFP32 ? qf(1.0f / (float)vel, (float)MFG_SCALE_INV) : qd(1.0 / (double)vel, MFG_SCALE_INV);
+                cell = (In.count & MFG_COUNT_DES) ? texture_cell<kFP32>(M, fo, pu, pv) : -1;
             }
-            if (In.flags & FF_PROFILE) profile_add(M, T, fo, 0, false, 1, 1, cosn, (double)vel, P.u, P.v, q1, q2);
-            for_moments(M, P.time, [&](int m) {
-                facet_add(M, T, B, fo, m, 0, 0, 0, q1, q2, 0);
-                if (cell >= 0) cell_add(T.texture + ((size_t)m * M.texture_cells + cell) * TT_N, 0, q1, q2);
-                if (In.flags & FF_PROFILE) profile_add(M, T, fo, m, false, 1, 1, cosn, (double)vel, P.u, P.v, q1, q2);
-            });
+            const unsigned long long vf = des ? 2 : 1;   // velocity factor of the 1/v_ort sum
+            const unsigned long long a1 = des ? 2 * q1 : pend_s1ov + q1;
+            const unsigned long long a2 = des ? q2 : pend_svort + q2;
+            const unsigned long long a3 = des ? q3 : pend_s1v;
+            facet_add(M, T, B, fo, 0, des ? 0 : 1, des ? 1 : 0, 0, a1, a2, a3);
+            if (cell >= 0) cell_add(T.texture + (size_t)cell * TT_N, 1, a1, a2);
+            if (In.flags & FF_PROFILE) profile_add(M, T, fo, 0, false, vf, 1, (double)cosn, (double)vel, (double)pu, (double)pv, q1, q2);
+            if (M.nm)
+                tally_moments(M, T, B, fo, P.time, des ? 1 : 0, 0, 0, vf * q1, q2, q3, cell, des ? 1 : 0, false, vf,
+                              (double)cosn, (double)vel, (double)pu, (double)pv, q1, q2);
+            pend = false;
+            pend_cell = -1;
+            pend_s1ov = pend_svort = pend_s1v = 0;
+            need_new = false;
         }
 
         // ---- 2. trace the ray ----
         int root = M.roots[P.structure];
         int hf;
-        double ht, hu, hv;
+        double ht;
+        R hu, hv;
+        const double ddx = (double)dx, ddy = (double)dy, ddz = (double)dz;
         if (kFP32) {
             bool amb = false;
             HitF h = trace_f(M, root, make_ray_f(P.ox, P.oy, P.oz, (float)dx, (float)dy, (float)dz), P.last, amb,
                              T.global + TG_STATUS);
             if (amb || h.f < 0) {
                 ++c_rechk;
-                HitD hd = trace_d(M, root, P.ox, P.oy, P.oz, (double)dx, (double)dy, (double)dz, P.last, T.global + TG_STATUS);
-                hf = hd.f; ht = hd.t; hu = hd.u; hv = hd.v;
+                HitD hd = trace_d(M, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last, T.global + TG_STATUS);
+                hf = hd.f; ht = hd.t; hu = (R)hd.u; hv = (R)hd.v;
             } else {
                 hf = h.f;
                 hu = h.u;
                 hv = h.v;
                 // distance to the FP64 plane of the hit facet: FP32 estimate + FP64 residual
                 const FacetIsectD& Rh = M.isect_d[hf];
-                double ddx = (double)dx, ddy = (double)dy, ddz = (double)dz;
                 double den = Rh.v[0] * ddx + Rh.v[1] * ddy + Rh.v[2] * ddz;
                 double num = Rh.v[3] - (Rh.v[0] * P.ox + Rh.v[1] * P.oy + Rh.v[2] * P.oz);
                 double r = num - (double)h.t * den;
                 ht = (double)h.t + (double)((float)r / (float)den);
             }
         } else {
-            HitD h = trace_d(M, root, P.ox, P.oy, P.oz, (double)dx, (double)dy, (double)dz, P.last, T.global + TG_STATUS);
-            hf = h.f; ht = h.t; hu = h.u; hv = h.v;
+            HitD h = trace_d(M, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last, T.global + TG_STATUS);
+            hf = h.f; ht = h.t; hu = (R)h.u; hv = (R)h.v;
         }
         if (hf < 0) {   // leak (Particle.cpp:387-392)
             ++c_leak;
@@ -636,9 +693,9 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
             double dd = (double)vel * 100.0 * (P.decay_at - P.time);
             if (dd < travel) { travel = dd; event = 2; }
         }
-        P.ox = P.ox + travel * (double)dx;
-        P.oy = P.oy + travel * (double)dy;
-        P.oz = P.oz + travel * (double)dz;
+        P.ox = P.ox + travel * ddx;
+        P.oy = P.oy + travel * ddy;
+        P.oz = P.oz + travel * ddz;
         if (kFP32) P.time += (double)((float)travel * (0.01f / (float)vel));   // cm -> m
         else P.time += travel / 100.0 / (double)vel;
         unsigned long long qdist = kFP32 ? qf((float)travel, (float)MFG_SCALE_DIST) : qd(travel, MFG_SCALE_DIST);
@@ -647,53 +704,41 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
         c_distf += qdist;
         // ---- 4. stick or reflect at facet hf (Particle.cpp:323-357) ----
         const FacetInfo& In = M.info[hf];
-        const FacetIsectD& Rh = M.isect_d[hf];
         bool absorb;
-        double cosn;
+        R cosn;
         if (kFP32) {
             float s = (In.flags & FF_STICK_PARAM) ? (float)param_at(M, M.info2[hf].stick_param, P.time) : M.phys_f[hf].sticking;
             absorb = (s == 1.0f) || (s > 0.0f && (float)rng.next() < s);
-            cosn = (double)fabsf(dx * M.phys_f[hf].N[0] + dy * M.phys_f[hf].N[1] + dz * M.phys_f[hf].N[2]);
+            cosn = fabsf(dx * M.phys_f[hf].N[0] + dy * M.phys_f[hf].N[1] + dz * M.phys_f[hf].N[2]);
         } else {
+            const FacetIsectD& Rh = M.isect_d[hf];
             double s = (In.flags & FF_STICK_PARAM) ? param_at(M, M.info2[hf].stick_param, P.time) : M.phys_d[hf].sticking;
             absorb = (s == 1.0) || (s > 0.0 && (double)rng.next() < s);
-            cosn = fabs((double)dx * Rh.v[0] + (double)dy * Rh.v[1] + (double)dz * Rh.v[2]);
+            cosn = (R)fabs(ddx * Rh.v[0] + ddy * Rh.v[1] + ddz * Rh.v[2]);
         }
-        R ort = vel * (R)cosn;
+        R ort = vel * cosn;
         unsigned long long q1 = kFP32 ? qf(1.0f / (float)ort, (float)MFG_SCALE_INV) : qd(1.0 / (double)ort, MFG_SCALE_INV);
         unsigned long long q2 = kFP32 ? qf((float)ort, (float)MFG_SCALE_V) : qd((double)ort, MFG_SCALE_V);
         unsigned long long q3 = kFP32 ? qf(1.0f / (float)vel, (float)MFG_SCALE_INV) : qd(1.0 / (double)vel, MFG_SCALE_INV);
-        P.u = hu;
-        P.v = hv;
-        int cell = -1;
-        if (In.tex_off >= 0 && (In.count & (absorb ? MFG_COUNT_ABS : MFG_COUNT_REFL))) {
-            double tw = kFP32 ? (double)M.phys_f[hf].texw_p : M.phys_d[hf].texw_p;
-            double th = kFP32 ? (double)M.phys_f[hf].texh_p : M.phys_d[hf].texh_p;
-            int tu = (int)(hu * tw), tv = (int)(hv * th);
-            tu = min(max(tu, 0), In.tex_w - 1);
-            tv = min(max(tv, 0), In.tex_h - 1);
-            cell = In.tex_off + tu + tv * In.tex_w;
-        }
+        pu = hu;
+        pv = hv;
+        int cell = (In.tex_off >= 0 && (In.count & (absorb ? MFG_COUNT_ABS : MFG_COUNT_REFL))) ? texture_cell<kFP32>(M, hf, hu, hv) : -1;
         ++c_hits;
-        if (In.flags & FF_ANGLEMAP) anglemap_add(M, T, hf, (double)dx, (double)dy, (double)dz);
+        if (In.flags & FF_ANGLEMAP) anglemap_add(M, T, hf, ddx, ddy, ddz);
         if (absorb) {   // RecordAbsorb (Particle.cpp:888-924)
             ++c_abs;
             facet_add(M, T, B, hf, 0, 1, 0, 1, 2 * q1, q2, q3);
             if (cell >= 0) cell_add(T.texture + (size_t)cell * TT_N, 1, 2 * q1, q2);
-            if (In.flags & FF_PROFILE) profile_add(M, T, hf, 0, true, 2, 1, cosn, (double)vel, hu, hv, q1, q2);
-            for_moments(M, P.time, [&](int m) {
-                facet_add(M, T, B, hf, m, 1, 0, 1, 2 * q1, q2, q3);
-                if (cell >= 0) cell_add(T.texture + ((size_t)m * M.texture_cells + cell) * TT_N, 1, 2 * q1, q2);
-                if (In.flags & FF_PROFILE) profile_add(M, T, hf, m, true, 2, 1, cosn, (double)vel, hu, hv, q1, q2);
-            });
+            if (In.flags & FF_PROFILE) profile_add(M, T, hf, 0, true, 2, 1, (double)cosn, (double)vel, (double)hu, (double)hv, q1, q2);
+            if (M.nm)
+                tally_moments(M, T, B, hf, P.time, 0, 1, 1, 2 * q1, q2, q3, cell, 1, true, 2,
+                              (double)cosn, (double)vel, (double)hu, (double)hv, q1, q2);
             need_new = true;
         } else {        // incoming half of PerformBounce (Particle.cpp:735-767)
-            if (In.flags & FF_PROFILE) profile_add(M, T, hf, 0, true, 1, 1, cosn, (double)vel, hu, hv, q1, q2);
-            for_moments(M, P.time, [&](int m) {
-                facet_add(M, T, B, hf, m, 1, 0, 0, q1, q2, q3);
-                if (cell >= 0) cell_add(T.texture + ((size_t)m * M.texture_cells + cell) * TT_N, 1, q1, q2);
-                if (In.flags & FF_PROFILE) profile_add(M, T, hf, m, true, 1, 1, cosn, (double)vel, hu, hv, q1, q2);
-            });
+            if (In.flags & FF_PROFILE) profile_add(M, T, hf, 0, true, 1, 1, (double)cosn, (double)vel, (double)hu, (double)hv, q1, q2);
+            if (M.nm)
+                tally_moments(M, T, B, hf, P.time, 0, 1, 0, q1, q2, q3, cell, 1, true, 1,
+                              (double)cosn, (double)vel, (double)hu, (double)hv, q1, q2);
             P.last = hf;
             pend = true;
             pend_s1ov = q1;
@@ -701,7 +746,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
             pend_s1v = q3;
             pend_cell = cell;
             need_new = false;
-            if (++P.bounces > C.max_steps) {   // step cap: count the hit, drop the particle
+            if (++P.bounces > max_steps) {   // step cap: count the hit, drop the particle
                 flush_pending();
                 ++c_drop;
                 need_new = true;

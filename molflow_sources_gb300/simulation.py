@@ -75,6 +75,13 @@ def load_library(build_if_missing=True):
         L.mfg_wait.argtypes = [vp, C.c_int64, C.POINTER(A.RunStats)]
         L.mfg_abort.argtypes = [vp]
         L.mfg_fetch.argtypes = [vp, C.POINTER(A.StateView)]
+        L.mfg_model_merge.argtypes = [C.POINTER(vp), C.c_int32, C.POINTER(vp)]
+        L.mfg_model_instances.argtypes = [vp]
+        L.mfg_model_instances.restype = C.c_int32
+        L.mfg_instance_layout.argtypes = [vp, C.c_int32, C.POINTER(A.StateLayout)]
+        L.mfg_fetch_instance.argtypes = [vp, C.c_int32, C.POINTER(A.StateView)]
+        L.mfg_run_batch.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(A.RunOptions), C.POINTER(A.RunStats)]
+        L.mfg_run_batch_async.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(A.RunOptions)]
         L.mfg_autotune.argtypes = [vp, C.c_uint64, C.c_int32, C.c_uint64, C.POINTER(A.RunOptions)]
         L.mfg_replay.argtypes = [vp, C.c_int32, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                  C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_double),
@@ -249,6 +256,72 @@ class GpuSimulation:
         if getattr(self, "gmodel", None) is not None:
             self.gmodel.close()
             self.gmodel = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GpuBatch:
+    """Many independent models traced in one persistent launch (mfg_model_merge + mfg_run_batch).
+
+    Each instance keeps its geometry, BVH, sources and tallies; particles of all instances
+    share one work queue, so instances of different cost balance across the GPU."""
+
+    def __init__(self, models, device=0):
+        L = load_library()
+        self.models = list(models)
+        self.parts = [GpuModel(m) for m in self.models]
+        arr = (C.c_void_p * len(self.parts))(*[p.h.value for p in self.parts])
+        h = C.c_void_p()
+        _check(L.mfg_model_merge(arr, len(self.parts), C.byref(h)))
+        self.merged = h
+        s = C.c_void_p()
+        _check(L.mfg_sim_create(self.merged, device, C.byref(s)))
+        self.h = s
+        self.last_stats = None
+
+    def run(self, counts, precision=A.PREC_FP32R, seed=0x4D6F6C66, use_graph=False, time_limit_s=0.0,
+            block_size=0, blocks_per_sm=0):
+        """counts: particles per instance (int applies to all)."""
+        if np.isscalar(counts):
+            counts = [int(counts)] * len(self.models)
+        c = np.ascontiguousarray(counts, dtype=np.uint64)
+        if not time_limit_s:
+            time_limit_s = float(os.environ.get("MFG_TIME_LIMIT_S", "0"))
+        o = A.RunOptions(precision=precision, seed=seed, block_size=block_size, blocks_per_sm=blocks_per_sm,
+                         smem_bvh_nodes=-1, time_limit_s=time_limit_s, use_graph=int(bool(use_graph)))
+        st = A.RunStats()
+        rc = load_library().mfg_run_batch(self.h, A.ptr(c, C.c_uint64), C.byref(o), C.byref(st))
+        self.last_stats = {f: getattr(st, f) for f, _ in A.RunStats._fields_}
+        _check(rc)
+        return self.last_stats
+
+    def fetch_instance(self, i):
+        st = SimuState(self.models[i])
+        v = st.view()
+        _check(load_library().mfg_fetch_instance(self.h, i, C.byref(v)))
+        return st
+
+    def reset(self):
+        _check(load_library().mfg_reset(self.h))
+
+    def set_particle_offset(self, first_particle):
+        _check(load_library().mfg_set_particle_offset(self.h, int(first_particle)))
+
+    def close(self):
+        L = load_library()
+        if getattr(self, "h", None):
+            L.mfg_sim_destroy(self.h)
+            self.h = None
+        if getattr(self, "merged", None):
+            L.mfg_model_destroy(self.merged)
+            self.merged = None
+        for p in getattr(self, "parts", []):
+            p.close()
+        self.parts = []
 
     def __del__(self):
         try:

@@ -80,6 +80,7 @@ typedef struct {
     int mode;
     uint32_t key[2];
     uint64_t pid;
+    uint32_t inst;
     uint32_t ctr;
     int have;
     double cache;
@@ -95,7 +96,7 @@ static double rnd(rng_t* r) {
         return u01_from(a, b);
     }
     if (r->have) { r->have = 0; return r->cache; }
-    uint32_t c[4] = {(uint32_t)r->pid, (uint32_t)(r->pid >> 32), r->ctr++, 0u}, o[4];
+    uint32_t c[4] = {(uint32_t)r->pid, (uint32_t)(r->pid >> 32), r->ctr++, r->inst}, o[4];
     orc_philox4x32(c, r->key, o);
     r->cache = u01_from(o[2], o[3]);
     r->have = 1;
@@ -105,7 +106,8 @@ static double rnd(rng_t* r) {
 static double rnd_opacity(rng_t* r, uint64_t step, int f) {
     if (r->mode == ORC_RNG_MT) return rnd(r);
     uint32_t c[4] = {(uint32_t)r->pid, (uint32_t)(r->pid >> 32), (uint32_t)step, (uint32_t)f + 1u}, o[4];
-    orc_philox4x32(c, r->key, o);
+    uint32_t k[2] = {r->key[0] ^ (r->inst * 0x9E3779B9u), r->key[1] ^ 0xA5A5A5A5u};   /* separate stream */
+    orc_philox4x32(c, k, o);
     return u01_from(o[0], o[1]);
 }
 
@@ -1217,6 +1219,7 @@ int orc_run(orc_model* M, uint64_t n_des, const orc_run_opts* o, mfg_state_view*
         rng_t r; memset(&r, 0, sizeof r);
         r.mode = o->rng_mode;
         r.key[0] = (uint32_t)o->seed; r.key[1] = (uint32_t)(o->seed >> 32);
+        r.inst = o->instance;
         if (r.mode == ORC_RNG_MT) mt_seed(&r.mt, 42424242u + (uint32_t)tid);
 #pragma omp for schedule(dynamic, 256)
         for (long long i = 0; i < (long long)n_des; ++i) {

@@ -42,6 +42,7 @@ typedef struct orc_run_opts {
     int32_t  n_threads;        /* 0 = all cores */
     int32_t  rng_mode;         /* ORC_RNG_* */
     uint64_t max_steps;        /* bounce cap per particle, 0 = 2^40 */
+    uint32_t instance;         /* batch instance id: word 3 of the Philox counter */
 } orc_run_opts;
 
 typedef struct orc_stats {

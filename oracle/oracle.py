@@ -37,7 +37,7 @@ def build(force=False):
 
 class OrcRunOpts(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("first_particle", C.c_uint64), ("n_threads", C.c_int32),
-                ("rng_mode", C.c_int32), ("max_steps", C.c_uint64)]
+                ("rng_mode", C.c_int32), ("max_steps", C.c_uint64), ("instance", C.c_uint32)]
 
 
 class OrcStats(C.Structure):
@@ -105,10 +105,11 @@ class Oracle:
         return o, area
 
     def run(self, n_des, seed=0x4D6F6C66, first_particle=0, threads=0, rng=ORC_RNG_PHILOX, state=None,
-            max_steps=0):
+            max_steps=0, instance=0):
         """Trace n_des particles; tallies are added into `state` (new one if None)."""
         st = state if state is not None else SimuState(self.model)
-        o = OrcRunOpts(seed=seed, first_particle=first_particle, n_threads=threads, rng_mode=rng, max_steps=max_steps)
+        o = OrcRunOpts(seed=seed, first_particle=first_particle, n_threads=threads, rng_mode=rng, max_steps=max_steps,
+                       instance=instance)
         s = OrcStats()
         v = st.view()
         rc = lib().orc_run(self.h, n_des, C.byref(o), C.byref(v), C.byref(s))

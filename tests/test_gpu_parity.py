@@ -99,11 +99,12 @@ def test_fp32r_agrees_with_oracle_within_3_sigma(tube):
     zz = zscores(gh, np.sqrt(gh / g.n_desorbed), m[:, A.FC_NBMCHIT], s[:, A.FC_NBMCHIT])
     assert np.abs(zz).max() < z_threshold(66), np.abs(zz).max()
     # texture counts on the 64x64 wall texture, family of 4096 cells
-    # (Poisson sigma of each cell count: a particle rarely hits the same cell twice)
+    # (Poisson counts per cell: a particle rarely hits the same cell twice)
     n_o = sum(b.n_desorbed for b in batches)
     co = sum(b.texture[0, :, 0] for b in batches)
     cg = g.texture[0, :, 0]
-    zt = zscores(cg / g.n_desorbed, np.sqrt(cg) / g.n_desorbed, co / n_o, np.sqrt(co) / n_o)
+    pool = (cg + co) / (g.n_desorbed + n_o)   # pooled rate per cell under the null hypothesis
+    zt = (cg / g.n_desorbed - co / n_o) / np.sqrt(np.maximum(pool, 1e-300) * (1.0 / g.n_desorbed + 1.0 / n_o))
     assert np.abs(zt).max() < z_threshold(4096) + 0.5, np.abs(zt).max()
     assert abs(np.mean(zt ** 2) - 1.0) < 0.1, np.mean(zt ** 2)
     # pressure-like sums per hit on the walls (Maxwell speeds)
