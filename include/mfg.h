@@ -283,6 +283,24 @@ int mfg_autotune(mfg_sim* sim, uint64_t n_trial, int32_t precision, uint64_t see
 /* Tallies of one instance of a batch, in that instance's own layout (overwrites). */
 int mfg_fetch_instance(mfg_sim* sim, int32_t instance, mfg_state_view* view);
 
+/* Change sticking coefficients of facets between runs (parameter sweeps, finite differences).
+ * Replaces editing sh.sticking and reloading (ParameterParser.cpp:240-248). */
+int mfg_update_sticking(mfg_sim* sim, int32_t n, const int32_t* facets, const double* values);
+
+/* Score-function sensitivities, an autograd-Function-shaped pair (no reference counterpart).
+ * Outputs y[9]: Sum v_ort per desorbed particle on up to 8 gauge facets (pressure up to
+ * MolPerTP/area) and absorptions per desorbed particle on the pump facets (pumped flux).
+ * Parameters: sticking of param_facets (each in (0,1)) and the outgassing of every source.
+ * mfg_sens_forward traces n particles with the sensitivity kernel and stores the Jacobian;
+ * mfg_sens_backward returns dL/dsticking[P] and dL/doutgassing[S] for a given dL/dy[9]. */
+int mfg_sens_setup(mfg_sim* sim, int32_t n_params, const int32_t* param_facets, int32_t n_gauges,
+                   const int32_t* gauge_facets, int32_t n_pumps, const int32_t* pump_facets);
+int32_t mfg_sens_sources(const mfg_sim* sim);
+int mfg_sens_forward(mfg_sim* sim, uint64_t n, const mfg_run_options* opt, double* outputs, mfg_run_stats* stats);
+/* d y / d sticking [P x 9], d y / d outgassing [S x 9] (per molecule/s of source s), source facet ids [S] */
+int mfg_sens_jacobian(mfg_sim* sim, double* d_sticking, double* d_outgassing, int32_t* source_facets);
+int mfg_sens_backward(mfg_sim* sim, const double* dl_dy, double* dl_dsticking, double* dl_doutgassing);
+
 /* Replay mode: intersect caller-given rays (no physics).  For ray i:
  * origin[3i..], direction[3i..], last_facet[i] (facet to skip, -1 none).
  * Out: hit_facet[i] (-1 = no hit), hit_t[i] (distance in |direction| units).

@@ -9,6 +9,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -85,6 +86,14 @@ struct mfg_sim {
     int launches = 0;
     int tuned_block[2] = {0, 0};     // per precision, from mfg_autotune
     int tuned_bps[2] = {0, 0};
+    std::vector<double> sticking;    // current sticking per facet (mfg_update_sticking)
+    // sensitivity state (mfg_sens_*)
+    bool sens_ready = false;
+    std::vector<int32_t> sens_params, sens_src;
+    SensCtl sens{};
+    size_t sens_bytes = 0;
+    void* sens_block = nullptr;
+    std::vector<double> js, jq, jy;
 };
 
 extern "C" {
@@ -293,6 +302,8 @@ int mfg_sim_create(const mfg_model* model, int device, mfg_sim** out) {
     if ((e = cudaHostGetDevicePointer(&s->d_abort, s->h_abort, 0)) != cudaSuccess) return bail(cuda_fail(e, "mapped pointer"));
     int rc = sim_upload(s);
     if (rc != MFG_OK) return bail(rc);
+    s->sticking.resize(model->h.nf);
+    for (int i = 0; i < model->h.nf; ++i) s->sticking[i] = model->h.phys_d[i].sticking;
     rc = mfg_reset(s);
     if (rc != MFG_OK) return bail(rc);
     *out = s;
@@ -307,6 +318,7 @@ void mfg_sim_destroy(mfg_sim* s) {
     if (s->h_abort) cudaFreeHost(s->h_abort);
     if (s->h_run) cudaFreeHost(s->h_run);
     if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+    if (s->sens_block) cudaFree(s->sens_block);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -320,7 +332,7 @@ static int read_global(mfg_sim* s, std::vector<unsigned long long>& g) {
     return MFG_OK;
 }
 
-static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options* opt) {
+static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options* opt, bool sens = false) {
     const mfg::HostModel& h = s->model->h;
     if (!h.gpu_supported) return fail(MFG_ERR_UNSUPPORTED_FEATURE, "not traced on the GPU: " + h.gpu_unsupported_reason);
     const int ni = int(h.instances.size());
@@ -358,6 +370,7 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     C.inst_prefix = reinterpret_cast<const unsigned long long*>(s->d_run + sizeof(RunDesc));
     C.inst_first = C.inst_prefix + ni + 1;
     C.abort_flag = s->d_abort;
+    if (sens) C.sens = s->sens;
     size_t fac_bytes = size_t(h.nf) * SF_N * 8;
     C.smem_facets = fac_bytes <= 64 * 1024 ? 1 : 0;
     size_t dyn = (TG_N + (C.smem_facets ? size_t(h.nf) * SF_N : 0)) * 8;
@@ -371,7 +384,10 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     // (register budgets 128, 85, 64); blocks_per_sm selects the FP32R variant
     int variant = 0;
     const void* fn = (const void*)mfgk::trace_kernel<false, 2>;
-    if (o.precision == MFG_PREC_FP32R) {
+    if (sens) {
+        variant = o.precision == MFG_PREC_FP32R ? 13 : 12;
+        fn = variant == 13 ? (const void*)mfgk::trace_kernel<true, 3, true> : (const void*)mfgk::trace_kernel<false, 2, true>;
+    } else if (o.precision == MFG_PREC_FP32R) {
         variant = (o.blocks_per_sm == 3) ? 3 : (o.blocks_per_sm == 4 ? 4 : 2);
         fn = variant == 3 ? (const void*)mfgk::trace_kernel<true, 3>
            : variant == 4 ? (const void*)mfgk::trace_kernel<true, 4> : (const void*)mfgk::trace_kernel<true, 2>;
@@ -387,14 +403,16 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
         cudaError_t e = cudaMemcpyAsync(s->d_run, s->h_run, s->run_bytes, cudaMemcpyHostToDevice, s->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(s->d_counter, 0, 8, s->stream);
         if (e != cudaSuccess) return e;
-        if (variant == 3) mfgk::trace_kernel<true, 3><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
+        if (variant == 13) mfgk::trace_kernel<true, 3, true><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
+        else if (variant == 12) mfgk::trace_kernel<false, 2, true><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
+        else if (variant == 3) mfgk::trace_kernel<true, 3><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
         else if (variant == 4) mfgk::trace_kernel<true, 4><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
         else if (variant == 2) mfgk::trace_kernel<true, 2><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
         else mfgk::trace_kernel<false, 2><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
         return cudaGetLastError();
     };
     s->t_start = std::chrono::steady_clock::now();
-    if (o.use_graph) {
+    if (o.use_graph && !sens) {
         // one captured graph per launch shape: [run descriptor copy, counter reset, tracer]
         long long key = (long long)variant * 1000003LL + block * 1009LL + grid;
         if (!s->graph_exec || s->graph_key != key) {
@@ -672,6 +690,159 @@ int32_t mfg_model_instances(const mfg_model* m) { return m ? int32_t(m->h.instan
 int mfg_instance_layout(const mfg_model* m, int32_t i, mfg_state_layout* out) {
     if (!m || !out || i < 0 || i >= int(m->h.instances.size())) return fail(MFG_ERR_INVALID_ARGUMENT, "bad argument");
     *out = m->h.instances[i].layout;
+    return MFG_OK;
+}
+
+int mfg_update_sticking(mfg_sim* s, int32_t n, const int32_t* facets, const double* values) {
+    if (!s || n < 0 || (n && (!facets || !values))) return fail(MFG_ERR_INVALID_ARGUMENT, "bad argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
+    const mfg::HostModel& h = s->model->h;
+    CK(cudaSetDevice(s->device));
+    for (int i = 0; i < n; ++i) {
+        int f = facets[i];
+        if (f < 0 || f >= h.nf || !(values[i] >= 0.0 && values[i] <= 1.0)) return fail(MFG_ERR_INVALID_ARGUMENT, "bad facet or sticking value");
+        s->sticking[f] = values[i];
+        double d = values[i];
+        float fl = float(values[i]);
+        CK(cudaMemcpyAsync((char*)s->dm.phys_d + sizeof(FacetPhysD) * size_t(f) + offsetof(FacetPhysD, sticking), &d, sizeof d,
+                           cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync((char*)s->dm.phys_f + sizeof(FacetPhysF) * size_t(f) + offsetof(FacetPhysF, sticking), &fl, sizeof fl,
+                           cudaMemcpyHostToDevice, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    return MFG_OK;
+}
+
+int mfg_sens_setup(mfg_sim* s, int32_t n_params, const int32_t* param_facets, int32_t n_gauges, const int32_t* gauge_facets,
+                   int32_t n_pumps, const int32_t* pump_facets) {
+    if (!s || n_params < 0 || n_gauges < 0 || n_gauges > MFG_SENS_NOUT - 1 || n_pumps < 0)
+        return fail(MFG_ERR_INVALID_ARGUMENT, "bad argument (at most 8 gauges)");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
+    const mfg::HostModel& h = s->model->h;
+    if (h.instances.size() != 1) return fail(MFG_ERR_INVALID_ARGUMENT, "sensitivities are for single models");
+    std::vector<int32_t> pof(h.nf, -1), gof(h.nf, -1), sof(h.nf, -1);
+    std::vector<uint8_t> pump(h.nf, 0);
+    for (int i = 0; i < n_params; ++i) {
+        int f = param_facets[i];
+        if (f < 0 || f >= h.nf || pof[f] >= 0) return fail(MFG_ERR_INVALID_ARGUMENT, "bad or repeated parameter facet");
+        if (!(s->sticking[f] > 0.0 && s->sticking[f] < 1.0)) return fail(MFG_ERR_INVALID_ARGUMENT, "parameter sticking must be in (0,1)");
+        pof[f] = i;
+    }
+    for (int i = 0; i < n_gauges; ++i) {
+        int f = gauge_facets[i];
+        if (f < 0 || f >= h.nf) return fail(MFG_ERR_INVALID_ARGUMENT, "bad gauge facet");
+        gof[f] = i;
+    }
+    for (int i = 0; i < n_pumps; ++i) {
+        int f = pump_facets[i];
+        if (f < 0 || f >= h.nf) return fail(MFG_ERR_INVALID_ARGUMENT, "bad pump facet");
+        pump[f] = 1;
+    }
+    s->sens_src.clear();
+    for (size_t k = 0; k < h.src_facet.size(); ++k) { sof[h.src_facet[k]] = int32_t(k); s->sens_src.push_back(h.src_facet[k]); }
+    s->sens_params.assign(param_facets, param_facets + n_params);
+    const size_t P = size_t(std::max(n_params, 1)), S = std::max<size_t>(s->sens_src.size(), 1), nf = size_t(h.nf);
+    const size_t off_pof = 0, off_gof = off_pof + 4 * nf, off_sof = off_gof + 4 * nf, off_pump = off_sof + 4 * nf;
+    const size_t off_A = (off_pump + nf + 255) / 256 * 256, off_B = off_A + 8 * P * MFG_SENS_NOUT;
+    const size_t off_C = off_B + 8 * P * MFG_SENS_NOUT, off_Y = off_C + 8 * S * MFG_SENS_NOUT;
+    const size_t off_cnt = off_Y + 8 * MFG_SENS_NOUT, off_ovf = off_cnt + 8 * S, total = off_ovf + 8;
+    CK(cudaSetDevice(s->device));
+    if (s->sens_block) { cudaFree(s->sens_block); s->sens_block = nullptr; }
+    CK(cudaMalloc(&s->sens_block, total));
+    char* b = static_cast<char*>(s->sens_block);
+    CK(cudaMemcpy(b + off_pof, pof.data(), 4 * nf, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b + off_gof, gof.data(), 4 * nf, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b + off_sof, sof.data(), 4 * nf, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b + off_pump, pump.data(), nf, cudaMemcpyHostToDevice));
+    s->sens.param_of_facet = reinterpret_cast<const int32_t*>(b + off_pof);
+    s->sens.gauge_of_facet = reinterpret_cast<const int32_t*>(b + off_gof);
+    s->sens.src_of_facet = reinterpret_cast<const int32_t*>(b + off_sof);
+    s->sens.pump_of_facet = reinterpret_cast<const uint8_t*>(b + off_pump);
+    s->sens.A = reinterpret_cast<double*>(b + off_A);
+    s->sens.B = reinterpret_cast<double*>(b + off_B);
+    s->sens.Cs = reinterpret_cast<double*>(b + off_C);
+    s->sens.Y = reinterpret_cast<double*>(b + off_Y);
+    s->sens.src_count = reinterpret_cast<unsigned long long*>(b + off_cnt);
+    s->sens.overflow = reinterpret_cast<unsigned long long*>(b + off_ovf);
+    s->sens_bytes = total - off_A;
+    s->sens_ready = true;
+    return MFG_OK;
+}
+
+int32_t mfg_sens_sources(const mfg_sim* s) { return s ? int32_t(s->sens_src.size()) : 0; }
+
+int mfg_sens_forward(mfg_sim* s, uint64_t n, const mfg_run_options* opt, double* outputs, mfg_run_stats* stats) {
+    if (!s || !outputs) return fail(MFG_ERR_INVALID_ARGUMENT, "null argument");
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (!s->sens_ready) return fail(MFG_ERR_INVALID_ARGUMENT, "call mfg_sens_setup first");
+        if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
+        CK(cudaSetDevice(s->device));
+        CK(cudaMemsetAsync(reinterpret_cast<char*>(s->sens.A), 0, s->sens_bytes, s->stream));
+        uint64_t counts[1] = {n};
+        int rc = launch_run(s, counts, opt, true);
+        if (rc != MFG_OK) return rc;
+    }
+    int rc = mfg_wait(s, -1, stats);
+    if (rc != MFG_OK) return rc;
+    std::lock_guard<std::mutex> lk(s->mu);
+    const size_t P = s->sens_params.size(), S = s->sens_src.size();
+    std::vector<double> A(P * MFG_SENS_NOUT), B(P * MFG_SENS_NOUT), Cs(S * MFG_SENS_NOUT), Y(MFG_SENS_NOUT);
+    std::vector<unsigned long long> cnt(S);
+    unsigned long long ovf = 0;
+    if (P) {
+        CK(cudaMemcpy(A.data(), s->sens.A, 8 * P * MFG_SENS_NOUT, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(B.data(), s->sens.B, 8 * P * MFG_SENS_NOUT, cudaMemcpyDeviceToHost));
+    }
+    if (S) {
+        CK(cudaMemcpy(Cs.data(), s->sens.Cs, 8 * S * MFG_SENS_NOUT, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(cnt.data(), s->sens.src_count, 8 * S, cudaMemcpyDeviceToHost));
+    }
+    CK(cudaMemcpy(Y.data(), s->sens.Y, 8 * MFG_SENS_NOUT, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&ovf, s->sens.overflow, 8, cudaMemcpyDeviceToHost));
+    const double N = double(n);
+    s->jy.assign(MFG_SENS_NOUT, 0.0);
+    for (int j = 0; j < MFG_SENS_NOUT; ++j) { s->jy[j] = Y[j] / N; outputs[j] = s->jy[j]; }
+    s->js.assign(P * MFG_SENS_NOUT, 0.0);
+    for (size_t k = 0; k < P; ++k) {
+        double st = s->sticking[s->sens_params[k]];
+        for (int j = 0; j < MFG_SENS_NOUT; ++j)
+            s->js[k * MFG_SENS_NOUT + j] = (-A[k * MFG_SENS_NOUT + j] / (1.0 - st) + B[k * MFG_SENS_NOUT + j] / st) / N;
+    }
+    s->jq.assign(S * MFG_SENS_NOUT, 0.0);
+    for (size_t q = 0; q < S; ++q)
+        for (int j = 0; j < MFG_SENS_NOUT; ++j)
+            s->jq[q * MFG_SENS_NOUT + j] = cnt[q] ? Cs[q * MFG_SENS_NOUT + j] / double(cnt[q]) : 0.0;
+    if (ovf) { g_err = "reflection list overflowed for " + std::to_string(ovf) + " particles"; return MFG_ERR_LIMIT; }
+    return MFG_OK;
+}
+
+int mfg_sens_jacobian(mfg_sim* s, double* d_sticking, double* d_outgassing, int32_t* source_facets) {
+    if (!s || s->js.empty() && !s->sens_params.empty()) return fail(MFG_ERR_INVALID_ARGUMENT, "no forward pass yet");
+    if (d_sticking) std::copy(s->js.begin(), s->js.end(), d_sticking);
+    if (d_outgassing) std::copy(s->jq.begin(), s->jq.end(), d_outgassing);
+    if (source_facets) std::copy(s->sens_src.begin(), s->sens_src.end(), source_facets);
+    return MFG_OK;
+}
+
+int mfg_sens_backward(mfg_sim* s, const double* dl_dy, double* dl_dsticking, double* dl_doutgassing) {
+    if (!s || !dl_dy) return fail(MFG_ERR_INVALID_ARGUMENT, "null argument");
+    if (s->jy.empty()) return fail(MFG_ERR_INVALID_ARGUMENT, "no forward pass yet");
+    const size_t P = s->sens_params.size(), S = s->sens_src.size();
+    if (dl_dsticking)
+        for (size_t k = 0; k < P; ++k) {
+            double a = 0;
+            for (int j = 0; j < MFG_SENS_NOUT; ++j) a += dl_dy[j] * s->js[k * MFG_SENS_NOUT + j];
+            dl_dsticking[k] = a;
+        }
+    if (dl_doutgassing)
+        for (size_t q = 0; q < S; ++q) {
+            double a = 0;
+            for (int j = 0; j < MFG_SENS_NOUT; ++j) a += dl_dy[j] * s->jq[q * MFG_SENS_NOUT + j];
+            dl_doutgassing[q] = a;
+        }
     return MFG_OK;
 }
 

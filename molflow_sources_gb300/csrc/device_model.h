@@ -201,6 +201,22 @@ struct RunDesc {
     // followed in memory by inst_prefix[n_inst + 1] and inst_first[n_inst] (u64)
 };
 
+// Score-function sensitivity bookkeeping (sensitivity kernel variant only)
+#define MFG_SENS_NOUT 9          // 8 gauge pressures + pumped flux
+#define MFG_SENS_TRAJ 1024       // reflections remembered per particle
+struct SensCtl {
+    const int32_t* param_of_facet;   // [nf] parameter index, -1 if the facet's sticking is not a parameter
+    const int32_t* gauge_of_facet;   // [nf] gauge index 0..7, -1 otherwise
+    const uint8_t* pump_of_facet;    // [nf] 1 when an absorption counts to the pumped flux
+    const int32_t* src_of_facet;     // [nf] source index for outgassing gradients, -1 otherwise
+    double* A;                       // [P][9] sum over (output event, earlier reflection on parameter k) of y
+    double* B;                       // [P][9] sum over absorptions on parameter k of y
+    double* Cs;                      // [S][9] sum of y per source
+    double* Y;                       // [9] sum of y
+    unsigned long long* src_count;   // [S] desorptions per source
+    unsigned long long* overflow;    // particles whose reflection list overflowed
+};
+
 struct LaunchCtl {
     unsigned long long* next_particle;   // work counter (particles handed out)
     const RunDesc* run;
@@ -208,4 +224,5 @@ struct LaunchCtl {
     const unsigned long long* inst_first;    // Philox counter of each instance's first particle
     const volatile int* abort_flag;          // host-mapped
     int smem_facets;                         // 1: moment-0 facet partials in shared memory
+    SensCtl sens;                            // used by the sensitivity variant
 };

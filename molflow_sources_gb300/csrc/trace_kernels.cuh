@@ -445,7 +445,16 @@ __device__ __noinline__ void reflect_general(const DevModel& M, int fo, bool fli
     }
 }
 
-template <bool kFP32, int kMinBlocks>
+// output event of the sensitivity variant: y adds to output j, to the score sums of every
+// earlier reflection on a parameter facet, and to the particle's source
+__device__ __noinline__ void sens_output(const SensCtl& S, const int* traj, int ntraj, int src, int j, double y) {
+    atomicAdd(S.Y + j, y);
+    const int n = ntraj < MFG_SENS_TRAJ ? ntraj : MFG_SENS_TRAJ;
+    for (int e = 0; e < n; ++e) atomicAdd(S.A + (size_t)traj[e] * MFG_SENS_NOUT + j, y);
+    if (src >= 0) atomicAdd(S.Cs + (size_t)src * MFG_SENS_NOUT + j, y);
+}
+
+template <bool kFP32, int kMinBlocks, bool kSens = false>
 __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_constant__ DevModel M, DevTally T, LaunchCtl C) {
     typedef typename Real_<kFP32>::T R;
     extern __shared__ unsigned long long smem[];
@@ -491,6 +500,8 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
     int pend_cell = -1;
     bool pend = false;
     unsigned iter = 0;
+    int traj[kSens ? MFG_SENS_TRAJ : 1];   // parameters of this particle's reflections (sensitivity variant)
+    int ntraj = 0, src_idx = -1;
     // per-thread global counters (no contended shared atomics on the hot path)
     unsigned long long c_hits = 0, c_des = 0, c_abs = 0, c_leak = 0, c_drop = 0, c_rechk = 0;
     unsigned long long c_dist = 0, c_distf = 0;
@@ -579,6 +590,11 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
             else P.time = (double)rng.next() * M.latest;
             P.structure = I2.structure;
             P.bounces = 0;
+            if (kSens) {
+                ntraj = 0;
+                src_idx = C.sens.src_of_facet[fo];
+                if (src_idx >= 0) atomicAdd(C.sens.src_count + src_idx, 1ull);
+            }
             law = I2.desorb_type == MFG_DES_UNIFORM ? 1 : (I2.desorb_type == MFG_DES_COSINE_N ? 2 : 0);
             lexp = (R)I2.desorb_exp;
             if (!M.use_maxwell) law |= 4;   // fixed speed 145.469 sqrt(T/m) (Particle.cpp:483)
@@ -631,6 +647,10 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                 ++c_des;
                 q3 = kFP32 ? qf(1.0f / (float)vel, (float)MFG_SCALE_INV) : qd(1.0 / (double)vel, MFG_SCALE_INV);
                 cell = (In.count & MFG_COUNT_DES) ? texture_cell<kFP32>(M, fo, pu, pv) : -1;
+            }
+            if (kSens && !des) {
+                int g = C.sens.gauge_of_facet[fo];
+                if (g >= 0) sens_output(C.sens, traj, ntraj, src_idx, g, (double)ort);   // outgoing half at a gauge
             }
             const unsigned long long vf = des ? 2 : 1;   // velocity factor of the 1/v_ort sum
             const unsigned long long a1 = des ? 2 * q1 : pend_s1ov + q1;
@@ -725,6 +745,20 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
         int cell = (In.tex_off >= 0 && (In.count & (absorb ? MFG_COUNT_ABS : MFG_COUNT_REFL))) ? texture_cell<kFP32>(M, hf, hu, hv) : -1;
         ++c_hits;
         if (In.flags & FF_ANGLEMAP) anglemap_add(M, T, hf, ddx, ddy, ddz);
+        if (kSens) {
+            int g = C.sens.gauge_of_facet[hf];
+            if (g >= 0) sens_output(C.sens, traj, ntraj, src_idx, g, (double)ort);   // incoming half / absorption
+            int k = C.sens.param_of_facet[hf];
+            if (absorb) {
+                if (C.sens.pump_of_facet[hf]) {
+                    sens_output(C.sens, traj, ntraj, src_idx, MFG_SENS_NOUT - 1, 1.0);
+                    if (k >= 0) atomicAdd(C.sens.B + (size_t)k * MFG_SENS_NOUT + MFG_SENS_NOUT - 1, 1.0);
+                }
+            } else if (k >= 0) {
+                if (ntraj < MFG_SENS_TRAJ) traj[ntraj++] = k;
+                else if (ntraj == MFG_SENS_TRAJ) { atomicAdd(C.sens.overflow, 1ull); ++ntraj; }
+            }
+        }
         if (absorb) {   // RecordAbsorb (Particle.cpp:888-924)
             ++c_abs;
             facet_add(M, T, B, hf, 0, 1, 0, 1, 2 * q1, q2, q3);

@@ -82,6 +82,14 @@ def load_library(build_if_missing=True):
         L.mfg_fetch_instance.argtypes = [vp, C.c_int32, C.POINTER(A.StateView)]
         L.mfg_run_batch.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(A.RunOptions), C.POINTER(A.RunStats)]
         L.mfg_run_batch_async.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(A.RunOptions)]
+        L.mfg_update_sticking.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+        L.mfg_sens_setup.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int32), C.c_int32,
+                                     C.POINTER(C.c_int32)]
+        L.mfg_sens_sources.argtypes = [vp]
+        L.mfg_sens_sources.restype = C.c_int32
+        L.mfg_sens_forward.argtypes = [vp, C.c_uint64, C.POINTER(A.RunOptions), C.POINTER(C.c_double), C.POINTER(A.RunStats)]
+        L.mfg_sens_jacobian.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int32)]
+        L.mfg_sens_backward.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.mfg_autotune.argtypes = [vp, C.c_uint64, C.c_int32, C.c_uint64, C.POINTER(A.RunOptions)]
         L.mfg_replay.argtypes = [vp, C.c_int32, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                  C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_double),
@@ -191,6 +199,12 @@ class GpuSimulation:
             return MCStepResult.DesorptionError
         _check(rc)
         return MCStepResult.Success
+
+    def update_sticking(self, facets, values):
+        """Change sticking coefficients in place (between runs)."""
+        f = np.ascontiguousarray(facets, np.int32)
+        v = np.ascontiguousarray(values, np.float64)
+        _check(load_library().mfg_update_sticking(self.h, len(f), A.ptr(f, C.c_int32), A.ptr(v, C.c_double)))
 
     def autotune(self, n_trial, precision=A.PREC_FP32R, seed=0x4D6F6C66):
         """Pick the fastest launch shape for this model (clears tallies); returns it as a dict."""

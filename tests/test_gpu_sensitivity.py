@@ -1,0 +1,122 @@
+"""Score-function sticking/outgassing gradients (mfg_sens_*) against central finite differences
+with common random numbers: on the GPU (same Philox particles for s+ds and s-ds) and with the
+CPU oracle."""
+import math
+
+import numpy as np
+import pytest
+
+from molflow_sources_gb300 import _abi as A
+from molflow_sources_gb300.sensitivity import SensitivityFunction, config5_neg_tube
+from molflow_sources_gb300.simulation import GpuSimulation
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+SEED = 0x4D6F6C66
+DS = 1e-3
+
+
+def outputs_from_state(st, m, n):
+    y = np.zeros(9)
+    y[:8] = st.facet_sums[0, m.gauges, A.FS_SUM_V_ORT] / n
+    y[8] = st.facet_counts[0, m.neg, A.FC_NBABSORBED].sum() / n
+    return y
+
+
+@pytest.fixture(scope="module")
+def setup():
+    m = config5_neg_tube()
+    sim = GpuSimulation(m)
+    sf = SensitivityFunction(sim, m.neg, m.gauges, m.neg)
+    return m, sim, sf
+
+
+def test_forward_outputs_equal_plain_run(setup):
+    """The sensitivity kernel traces the same particles as the plain kernel (FP64, same streams)."""
+    m, sim, sf = setup
+    n = 200000
+    sim.ResetSimulation()
+    sim.set_particle_offset(0)
+    y = sf.forward(n, precision=A.PREC_FP64, seed=SEED)
+    plain = outputs_from_state(sim.fetch(), m, n)
+    np.testing.assert_allclose(y, plain, rtol=1e-7, atol=1e-12)
+
+
+def test_gradients_match_central_differences(setup):
+    m, sim, sf = setup
+    nb, n = 8, 4_000_000
+    js = []
+    for b in range(nb):
+        sim.ResetSimulation()
+        sim.set_particle_offset(b * n)
+        sf.forward(n, seed=SEED)
+        js.append(sf.jacobian()[0])
+    js = np.array(js)
+    jm, jse = js.mean(0), js.std(0, ddof=1) / math.sqrt(nb)
+    # parameters with the largest pumped-flux sensitivity, and the one most coupled to gauge 0
+    pick = list(np.argsort(-np.abs(jm[:, 8]))[:3]) + [int(np.argmax(np.abs(jm[:, 0])))]
+    for k in pick:
+        f = int(m.neg[k])
+        s0 = float(m.sticking[f])
+        fd = []
+        for b in range(nb):
+            ys = []
+            for s in (s0 + DS, s0 - DS):
+                sim.update_sticking([f], [s])
+                sim.ResetSimulation()
+                sim.set_particle_offset(b * n)   # common random numbers: the same particles
+                sim.SimulationMCStep(n, precision=A.PREC_FP32R, seed=SEED)
+                ys.append(outputs_from_state(sim.fetch(), m, n))
+            fd.append((ys[0] - ys[1]) / (2 * DS))
+        sim.update_sticking([f], [s0])
+        fd = np.array(fd)
+        fm, fse = fd.mean(0), fd.std(0, ddof=1) / math.sqrt(nb)
+        for j in (0, 8):
+            sig = math.sqrt(jse[k, j] ** 2 + fse[j] ** 2)
+            assert abs(jm[k, j] - fm[j]) < 3.5 * sig + 1e-9, (k, j, jm[k, j], fm[j], sig)
+
+
+def test_outgassing_gradient_is_the_conditional_mean(setup):
+    m, sim, sf = setup
+    sim.ResetSimulation()
+    y = sf.forward(2_000_000, seed=SEED)
+    js, jq, src = sf.jacobian()
+    # the inlet (facet 0) dominates the desorptions: its conditional pumped flux is close to the mean
+    k = int(np.where(src == 0)[0][0])
+    assert abs(jq[k, 8] / y[8] - 1) < 0.05
+    ds, dq = sf.backward(np.eye(9)[8])
+    np.testing.assert_allclose(ds, js[:, 8])
+    np.testing.assert_allclose(dq, jq[:, 8])
+
+
+def test_gradient_cost_over_forward(setup):
+    m, sim, sf = setup
+    n = 4_000_000
+    sim.SimulationMCStep(n, precision=A.PREC_FP32R, seed=SEED)
+    t_fwd = sim.last_stats["kernel_ms"]
+    sf.forward(n, seed=SEED)
+    t_sens = sf.last_stats["kernel_ms"]
+    print("sensitivity / forward kernel time: %.3f" % (t_sens / t_fwd))
+    assert t_sens / t_fwd < 2.0
+
+
+def test_gradient_matches_oracle_finite_difference(setup):
+    """Finite difference of the CPU oracle (common random numbers) for the strongest pumped-flux parameter."""
+    m, sim, sf = setup
+    sim.ResetSimulation()
+    sim.set_particle_offset(0)
+    sf.forward(8_000_000, seed=SEED)
+    js = sf.jacobian()[0]
+    k = int(np.argmax(np.abs(js[:, 8])))
+    f = int(m.neg[k])
+    s0 = float(m.sticking[f])
+    n = 400000
+    vals = []
+    for s in (s0 + 5 * DS, s0 - 5 * DS):
+        mm = config5_neg_tube()
+        mm.sticking[f] = s
+        st, _ = Oracle(mm).run(n, seed=SEED)
+        vals.append(outputs_from_state(st, mm, n)[8])
+    fd = (vals[0] - vals[1]) / (10 * DS)
+    # CRN noise of the oracle difference: flips at facet f only; allow 25 % + 3 sigma
+    assert abs(fd - js[k, 8]) < 0.25 * abs(js[k, 8]) + 3 * math.sqrt(abs(js[k, 8]) * 10 * DS / n) / (10 * DS), (fd, js[k, 8])
