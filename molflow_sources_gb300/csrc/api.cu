@@ -71,7 +71,7 @@ struct mfg_sim {
     int* d_abort = nullptr;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    size_t n_global = TG_N, n_facet = 0, n_texture = 0, n_profile = 0, n_anglemap = 0;
+    size_t n_global = TG_N, n_facet = 0, n_texture = 0, n_profile = 0, n_anglemap = 0, n_dir = 0;
     std::vector<uint64_t> particles_started;   // per instance
     unsigned char* h_run = nullptr;            // pinned RunDesc + prefix + first (staging)
     unsigned char* d_run = nullptr;
@@ -211,7 +211,10 @@ static int sim_upload(mfg_sim* s) {
     M.texture_cells = h.layout.texture_cells;
     M.profile_facets = h.layout.profile_facets;
     M.anglemap_cells = h.layout.anglemap_cells;
+    M.direction_cells = h.layout.direction_cells;
     M.scene_scale = h.scene_scale;
+    M.has_transparent = h.has_transparent;
+    M.pad2 = 0;
     {
         std::vector<int32_t> sb, sc;
         std::vector<double> st;
@@ -234,6 +237,7 @@ static int sim_upload(mfg_sim* s) {
     s->n_texture = B * size_t(h.layout.texture_cells) * TT_N;
     s->n_profile = B * size_t(h.layout.profile_facets) * MFG_PROFILE_SIZE * TT_N;
     s->n_anglemap = size_t(h.layout.anglemap_cells);
+    s->n_dir = B * size_t(h.layout.direction_cells);
     auto alloc = [&](unsigned long long** p, size_t n) -> int {
         *p = nullptr;
         if (!n) return MFG_OK;
@@ -248,6 +252,8 @@ static int sim_upload(mfg_sim* s) {
     if ((rc = alloc(&s->dt.texture, s->n_texture))) return rc;
     if ((rc = alloc(&s->dt.profile, s->n_profile))) return rc;
     if ((rc = alloc(&s->dt.anglemap, s->n_anglemap))) return rc;
+    if ((rc = alloc(&s->dt.dir_count, s->n_dir))) return rc;
+    if ((rc = alloc(reinterpret_cast<unsigned long long**>(&s->dt.direction), 3 * s->n_dir))) return rc;
     if ((rc = alloc(&s->d_counter, 1))) return rc;
     return MFG_OK;
 }
@@ -262,6 +268,10 @@ int mfg_reset(mfg_sim* s) {
     if (s->n_texture) CK(cudaMemsetAsync(s->dt.texture, 0, s->n_texture * 8, s->stream));
     if (s->n_profile) CK(cudaMemsetAsync(s->dt.profile, 0, s->n_profile * 8, s->stream));
     if (s->n_anglemap) CK(cudaMemsetAsync(s->dt.anglemap, 0, s->n_anglemap * 8, s->stream));
+    if (s->n_dir) {
+        CK(cudaMemsetAsync(s->dt.dir_count, 0, s->n_dir * 8, s->stream));
+        CK(cudaMemsetAsync(s->dt.direction, 0, s->n_dir * 24, s->stream));
+    }
     CK(cudaStreamSynchronize(s->stream));
     return MFG_OK;
 }
@@ -332,6 +342,22 @@ static int read_global(mfg_sim* s, std::vector<unsigned long long>& g) {
     return MFG_OK;
 }
 
+// tracer kernel of a launch variant (see launch_run)
+static const void* kernel_of(int variant) {
+    switch (variant) {
+        case 2: return (const void*)mfgk::trace_kernel<true, 2>;
+        case 3: return (const void*)mfgk::trace_kernel<true, 3>;
+        case 4: return (const void*)mfgk::trace_kernel<true, 4>;
+        case 12: return (const void*)mfgk::trace_kernel<false, 2, true>;
+        case 13: return (const void*)mfgk::trace_kernel<true, 3, true>;
+        case 100: return (const void*)mfgk::trace_kernel<false, 2, false, true>;
+        case 102: return (const void*)mfgk::trace_kernel<true, 2, false, true>;
+        case 112: return (const void*)mfgk::trace_kernel<false, 2, true, true>;
+        case 113: return (const void*)mfgk::trace_kernel<true, 3, true, true>;
+        default: return (const void*)mfgk::trace_kernel<false, 2>;
+    }
+}
+
 static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options* opt, bool sens = false) {
     const mfg::HostModel& h = s->model->h;
     if (!h.gpu_supported) return fail(MFG_ERR_UNSUPPORTED_FEATURE, "not traced on the GPU: " + h.gpu_unsupported_reason);
@@ -381,17 +407,16 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     int block = o.block_size > 0 ? o.block_size : 256;
     if (block % 32 || block > 256) return fail(MFG_ERR_INVALID_ARGUMENT, "block_size must be a multiple of 32, at most 256");
     // kernel variant: FP64, or FP32R compiled for at least 2, 3 or 4 resident blocks per SM
-    // (register budgets 128, 85, 64); blocks_per_sm selects the FP32R variant
+    // (register budgets 128, 85, 64); blocks_per_sm selects the FP32R variant.  Models with
+    // transparent or semi-transparent facets use the variants that keep a pass list (+100).
     int variant = 0;
-    const void* fn = (const void*)mfgk::trace_kernel<false, 2>;
     if (sens) {
         variant = o.precision == MFG_PREC_FP32R ? 13 : 12;
-        fn = variant == 13 ? (const void*)mfgk::trace_kernel<true, 3, true> : (const void*)mfgk::trace_kernel<false, 2, true>;
     } else if (o.precision == MFG_PREC_FP32R) {
         variant = (o.blocks_per_sm == 3) ? 3 : (o.blocks_per_sm == 4 ? 4 : 2);
-        fn = variant == 3 ? (const void*)mfgk::trace_kernel<true, 3>
-           : variant == 4 ? (const void*)mfgk::trace_kernel<true, 4> : (const void*)mfgk::trace_kernel<true, 2>;
     }
+    if (h.has_transparent) variant = (variant == 3 || variant == 4) ? 102 : variant + 100;
+    const void* fn = kernel_of(variant);
     CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn)));
     int per_sm = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, dyn));
@@ -403,12 +428,9 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
         cudaError_t e = cudaMemcpyAsync(s->d_run, s->h_run, s->run_bytes, cudaMemcpyHostToDevice, s->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(s->d_counter, 0, 8, s->stream);
         if (e != cudaSuccess) return e;
-        if (variant == 13) mfgk::trace_kernel<true, 3, true><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
-        else if (variant == 12) mfgk::trace_kernel<false, 2, true><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
-        else if (variant == 3) mfgk::trace_kernel<true, 3><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
-        else if (variant == 4) mfgk::trace_kernel<true, 4><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
-        else if (variant == 2) mfgk::trace_kernel<true, 2><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
-        else mfgk::trace_kernel<false, 2><<<unsigned(grid), block, dyn, s->stream>>>(s->dm, s->dt, C);
+        void* args[] = {(void*)&s->dm, (void*)&s->dt, (void*)&C};
+        e = cudaLaunchKernel(fn, dim3(unsigned(grid)), dim3(block), args, dyn, s->stream);
+        if (e != cudaSuccess) return e;
         return cudaGetLastError();
     };
     s->t_start = std::chrono::steady_clock::now();
@@ -508,7 +530,7 @@ int mfg_wait(mfg_sim* s, int64_t timeout_ms, mfg_run_stats* stats) {
     st.kernel_launches = s->launches;
     unsigned long long status = g[TG_STATUS];
     st.status = MFG_OK;
-    if (status & KS_STACK) st.status = MFG_ERR_LIMIT;
+    if (status & (KS_STACK | KS_TRANSP)) st.status = MFG_ERR_LIMIT;
     if (status & KS_TIMEOUT) st.status = MFG_ERR_TIMEOUT;
     if (status & KS_ABORTED) st.status = MFG_ERR_ABORTED;
     if (status) {
@@ -516,7 +538,9 @@ int mfg_wait(mfg_sim* s, int64_t timeout_ms, mfg_run_stats* stats) {
         CK(cudaMemcpyAsync(s->dt.global + TG_STATUS, &zero, 8, cudaMemcpyHostToDevice, s->stream));
         CK(cudaStreamSynchronize(s->stream));
         g_err = st.status == MFG_ERR_TIMEOUT ? "kernel time limit reached; particles in flight were dropped"
-              : st.status == MFG_ERR_ABORTED ? "run aborted" : "BVH traversal stack overflow";
+              : st.status == MFG_ERR_ABORTED ? "run aborted"
+              : (status & KS_TRANSP) ? "a ray crossed more transparent facets than the pass list holds (32)"
+              : "BVH traversal stack overflow";
     }
     if (stats) *stats = st;
     return st.status;
@@ -642,10 +666,27 @@ static int fetch_range(mfg_sim* s, mfg_state_view* v, int fb, int nf, int64_t tb
     if (v->anglemap)
         for (int64_t c = 0; c < na; ++c) v->anglemap[c] = am[ab + c];
     if (v->direction) {
-        int64_t nd = 0;
+        // direction cells of facets [fb, fb+nf): contiguous range starting at the first one's offset
+        int64_t d0 = -1, nd = 0;
         for (int i = 0; i < nf; ++i)
-            if (h.dir_off.size() > size_t(fb + i) && h.dir_off[fb + i] >= 0) nd += int64_t(h.tex_w[fb + i]) * h.tex_h[fb + i];
-        std::fill(v->direction, v->direction + B * size_t(nd) * 4, 0.0);
+            if (h.dir_off[fb + i] >= 0) {
+                if (d0 < 0) d0 = h.dir_off[fb + i];
+                nd += int64_t(h.tex_w[fb + i]) * h.tex_h[fb + i];
+            }
+        const size_t ND = size_t(h.layout.direction_cells);
+        if (nd > 0) {
+            std::vector<double> dv(3 * s->n_dir);
+            std::vector<unsigned long long> dc(s->n_dir);
+            CK(cudaMemcpy(dv.data(), s->dt.direction, 24 * s->n_dir, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(dc.data(), s->dt.dir_count, 8 * s->n_dir, cudaMemcpyDeviceToHost));
+            for (size_t m = 0; m < B; ++m)
+                for (int64_t c = 0; c < nd; ++c) {
+                    size_t k = m * ND + size_t(d0 + c);
+                    double* o = v->direction + (m * size_t(nd) + c) * 4;
+                    o[0] = dv[3 * k]; o[1] = dv[3 * k + 1]; o[2] = dv[3 * k + 2];
+                    o[3] = double(dc[k]);
+                }
+        }
     }
     return MFG_OK;
 }
@@ -888,3 +929,4 @@ int mfg_replay(mfg_sim* s, int32_t precision, int64_t n, const double* origin, c
 }
 
 }  // extern "C"
+

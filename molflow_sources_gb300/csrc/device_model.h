@@ -28,11 +28,12 @@ struct __align__(16) NodeF {
 };
 
 // Facet intersection record FP64 (128 B):
-//  [0..2] N, [3] D = N.O, [4..6] O, [7] two-sided flag (nonzero bits), [8..10] U/|U|^2, [11] pad,
+//  [0..2] N, [3] D = N.O, [4..6] O, [7] flags as integer bits (bit 0 two-sided, bits 1-2 opacity
+//  class: 0 opaque, 1 transparent, 2 partial or time-dependent), [8..10] U/|U|^2, [11] pad,
 //  [12..14] V/|V|^2, [15] pad
 struct __align__(16) FacetIsectD { double v[16]; };
 // FP32 copy (64 B): [0..2] N, [3] Olo.x, [4..6] Ohi, [7] Olo.y, [8..10] U/|U|^2, [11] Olo.z,
-// [12..14] V/|V|^2, [15] two-sided flag (1.0f) — O as a hi+lo float pair for the origin-relative test
+// [12..14] V/|V|^2, [15] the same flags as a float — O as a hi+lo float pair for the origin-relative test
 struct __align__(16) FacetIsectF { float v[16]; };
 
 // Polygon record: circle shortcut + vertex range (64 B / 32 B).
@@ -75,8 +76,10 @@ struct __align__(16) FacetInfo {
 };
 struct __align__(16) FacetInfo2 {
     int32_t structure, desorb_type, stick_param, temp_param;
-    int32_t am_phi, am_lo, am_hi, pad;
+    int32_t am_phi, am_lo, am_hi, dir_off;   // dir_off: direction-cell offset, -1 when not recorded
     double am_limit, max_speed, desorb_exp, temperature;
+    double opacity;
+    int32_t opac_param, pad;
 };
 
 // Device-resident tallies.  Fixed-point scales: velocities (m/s) * 2^20,
@@ -128,6 +131,7 @@ struct __align__(16) FacetInfo2 {
 #define KS_ABORTED 2ull
 #define KS_NO_SOURCE 4ull
 #define KS_STACK 8ull
+#define KS_TRANSP 16ull   // more transparent passes on one ray than the pass list holds
 
 struct DevModel {
     int32_t nf, nstruct;
@@ -174,6 +178,8 @@ struct DevModel {
     int64_t texture_cells;       // per moment block
     int64_t profile_facets;
     int64_t anglemap_cells;
+    int64_t direction_cells;
+    int32_t has_transparent, pad2;   // some facet has opacity < 1 or an opacity parameter
     double scene_scale;          // max |coordinate| of the scene (for FP32 tolerances)
     // instances of a batch (one for a plain model): source-table range and total weight
     int32_t n_inst, pad1;
@@ -188,6 +194,8 @@ struct DevTally {
     unsigned long long* texture;     // (1+M) * texture_cells * TT_N
     unsigned long long* profile;     // (1+M) * profile_facets * 100 * TT_N
     unsigned long long* anglemap;    // anglemap_cells
+    double* direction;               // (1+M) * direction_cells * 3: Sum of velocity vectors (FP64 atomics)
+    unsigned long long* dir_count;   // (1+M) * direction_cells
 };
 
 // Per-run values live in device memory so one captured CUDA graph serves every run:

@@ -495,8 +495,6 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
         if (m.teleport[i]) unsupported(f + "teleport");
         if (m.moving[i]) unsupported(f + "moving facet");
         if (m.desorb_type[i] == MFG_DES_ANGLEMAP) unsupported(f + "angle-map desorption");
-        if (m.opacity[i] < 1.0 || m.p_opac[i] >= 0) unsupported(f + "semi-transparent or transparent facet");
-        if (m.count[i] & MFG_COUNT_DIR) unsupported(f + "direction recording");
         if (m.p_temp[i] >= 0 && m.sojourn[i]) {}
     }
 
@@ -654,10 +652,12 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
             r[12 + a] = F.V[a] / v2;
         }
         r[3] = F.N[0] * F.O[0] + F.N[1] * F.O[1] + F.N[2] * F.O[2];
-        if (m.two_sided[i]) {   // two-sided flag in the record's padding: nonzero bits
-            long long one = 1;
-            std::memcpy(&r[7], &one, sizeof one);
-        }
+        // flags in the record's padding: bit 0 two-sided, bits 1-2 opacity class
+        const long long opac_class = (m.p_opac[i] >= 0 || (m.opacity[i] > 0.0 && m.opacity[i] < 1.0)) ? 2
+                                   : (m.opacity[i] <= 0.0 ? 1 : 0);
+        const long long flags = (m.two_sided[i] ? 1 : 0) | (opac_class << 1);
+        std::memcpy(&r[7], &flags, sizeof flags);
+        if (opac_class) m.has_transparent = 1;
         // FP32 copy: [N | O hi/lo split | U/|U|^2 | V/|V|^2] (origin-relative FP32 facet test)
         float* q = m.isect_f[i].v;
         for (int k = 0; k < 16; ++k) q[k] = 0.0f;
@@ -670,7 +670,7 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
         q[3] = float(F.O[0] - double(q[4]));
         q[7] = float(F.O[1] - double(q[5]));
         q[11] = float(F.O[2] - double(q[6]));
-        q[15] = m.two_sided[i] ? 1.0f : 0.0f;
+        q[15] = float(flags);
         // circle shortcut for the point-in-polygon test
         double su = std::sqrt(u2), sv = std::sqrt(v2);
         const double* pv = &m.v2[2 * size_t(F.vstart)];
@@ -764,6 +764,9 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
         i2.am_phi = m.am_phi[i];
         i2.am_lo = m.am_lo[i];
         i2.am_hi = m.am_hi[i];
+        i2.dir_off = int32_t(m.dir_off[i]);
+        i2.opacity = m.opacity[i];
+        i2.opac_param = m.p_opac[i];
         i2.pad = 0;
         i2.am_limit = m.am_limit[i];
         i2.max_speed = m.max_speed[i];
@@ -847,8 +850,10 @@ int merge_host_models(const std::vector<const HostModel*>& parts, HostModel& out
         }
         for (FacetInfo2 f2 : p.info2) {
             if (f2.structure >= 0) f2.structure += in.struct_base;
+            if (f2.dir_off >= 0) f2.dir_off += int32_t(in.dir_base);
             if (f2.stick_param >= 0) f2.stick_param += par_base;
             if (f2.temp_param >= 0) f2.temp_param += par_base;
+            if (f2.opac_param >= 0) f2.opac_param += par_base;
             out.info2.push_back(f2);
         }
         out.centers.insert(out.centers.end(), p.centers.begin(), p.centers.end());
@@ -864,6 +869,14 @@ int merge_host_models(const std::vector<const HostModel*>& parts, HostModel& out
         out.par_logx.insert(out.par_logx.end(), p.par_logx.begin(), p.par_logx.end());
         out.par_logy.insert(out.par_logy.end(), p.par_logy.begin(), p.par_logy.end());
         out.tex_inc.insert(out.tex_inc.end(), p.tex_inc.begin(), p.tex_inc.end());
+        for (int i = 0; i < p.nf; ++i) {
+            out.tex_off.push_back(p.tex_off[i] >= 0 ? p.tex_off[i] + in.tex_base : -1);
+            out.dir_off.push_back(p.dir_off[i] >= 0 ? p.dir_off[i] + in.dir_base : -1);
+            out.ang_off.push_back(p.ang_off[i] >= 0 ? p.ang_off[i] + in.ang_base : -1);
+            out.prof_idx.push_back(p.prof_idx[i] >= 0 ? p.prof_idx[i] + in.prof_base : -1);
+            out.tex_w.push_back(p.tex_w[i]);
+            out.tex_h.push_back(p.tex_h[i]);
+        }
         out.facets.insert(out.facets.end(), p.facets.begin(), p.facets.end());
         out.nf += p.nf;
         out.nstruct += p.nstruct;
@@ -874,6 +887,7 @@ int merge_host_models(const std::vector<const HostModel*>& parts, HostModel& out
         out.bvh_depth = std::max(out.bvh_depth, p.bvh_depth);
         out.bvh_leaves += p.bvh_leaves;
         out.scene_scale = std::max(out.scene_scale, p.scene_scale);
+        out.has_transparent |= p.has_transparent;
         out.instances.push_back(in);
     }
     mfg_state_layout& L = out.layout;

@@ -75,6 +75,7 @@ struct HostModel {
     std::vector<FacetInfo2> info2;
     std::vector<double> centers;
     double scene_scale = 1;
+    int has_transparent = 0;
     bool gpu_supported = true;
     std::string gpu_unsupported_reason;
     // instances (one for a plain model; several after merge_host_models)

@@ -20,33 +20,11 @@
 #include <type_traits>
 
 #include "device_model.h"
+#include "philox.cuh"
 
 namespace mfgk {
 
 constexpr double kPi = 3.14159265358979323846;
-
-// ------------------------------------------------------------------ Philox --
-__device__ __forceinline__ void philox4x32_10(uint32_t& c0, uint32_t& c1, uint32_t& c2, uint32_t& c3,
-                                              uint32_t k0, uint32_t k1) {
-#pragma unroll
-    for (int r = 0; r < 10; ++r) {
-        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
-        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
-        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
-        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
-        k0 += 0x9E3779B9u;
-        k1 += 0xBB67AE85u;
-    }
-}
-__device__ __forceinline__ double u01d(uint32_t a, uint32_t b) {
-    uint64_t m = ((((uint64_t)a) << 32) | b) >> 12;
-    return __longlong_as_double((long long)(0x3FF0000000000000ull | m)) - 1.0;
-}
-// uniform float in (0,1): (k + 1/2) * 2^-23; never 0, so cos(theta) = sqrt(u) never
-// gives a direction lying in the facet plane
-__device__ __forceinline__ float u01f(uint32_t a) {
-    return (__uint_as_float(0x3F800000u | (a >> 9)) - 1.0f) + 5.9604645e-8f;
-}
 
 // double stream: two uniforms per Philox block (the CPU oracle's order)
 // counter = (particle id lo, hi, draw index, instance)
@@ -143,23 +121,6 @@ __device__ __forceinline__ float interp_x_f(float y, const float* xs, const floa
     float w = (y - ys[i]) / (ys[i + 1] - ys[i]);
     return xs[i] + (xs[i + 1] - xs[i]) * w;
 }
-// InterpolateY (no extrapolation) for time-dependent parameters
-__device__ __noinline__ double param_at(const DevModel& M, int p, double t) {
-    int s = M.par_start[p], e = M.par_start[p + 1], n = e - s;
-    const double* xs = M.par_t + s;
-    const double* ys = M.par_v + s;
-    if (n == 1) return ys[0];
-    int lo = 0, hi = n;
-    while (lo < hi) { int mid = (lo + hi) >> 1; if (xs[mid] <= t) lo = mid + 1; else hi = mid; }
-    int i = lo - 1;
-    if (i < 0) return ys[0];
-    if (i >= n - 1) return ys[n - 1];
-    bool lx = M.par_logx[p], ly = M.par_logy[p];
-    double w = lx ? (log10(t) - log10(xs[i])) / (log10(xs[i + 1]) - log10(xs[i])) : (t - xs[i]) / (xs[i + 1] - xs[i]);
-    if (ly) return exp10(log10(ys[i]) + (log10(ys[i + 1]) - log10(ys[i])) * w);
-    return ys[i] + (ys[i + 1] - ys[i]) * w;
-}
-
 }  // namespace mfgk
 
 #include "traversal.cuh"
@@ -379,19 +340,76 @@ __device__ __forceinline__ int texture_cell(const DevModel& M, int f, R u, R v) 
     return In.tex_off + tu + tv * In.tex_w;
 }
 
+// RecordDirectionVector (Particle.cpp:1006-1023): Sum of v*direction and a count per cell,
+// constant flow and every moment window holding t
+__device__ __noinline__ void direction_add(const DevModel& M, const DevTally& T, int f, double u, double v, double time,
+                                           double vx, double vy, double vz) {
+    const FacetInfo& In = M.info[f];
+    const int off = M.info2[f].dir_off;
+    if (off < 0) return;
+    int tu = (int)(u * M.phys_d[f].texw_p), tv = (int)(v * M.phys_d[f].texh_p);
+    tu = min(max(tu, 0), In.tex_w - 1);
+    tv = min(max(tv, 0), In.tex_h - 1);
+    const size_t c = (size_t)off + tu + (size_t)tv * In.tex_w;
+    auto add = [&](int m) {
+        const size_t k = (size_t)m * M.direction_cells + c;
+        atomicAdd(T.direction + 3 * k, vx);
+        atomicAdd(T.direction + 3 * k + 1, vy);
+        atomicAdd(T.direction + 3 * k + 2, vz);
+        atomicAdd(T.dir_count + k, 1ull);
+    };
+    add(0);
+    for_moments(M, time, add);
+}
+
 // Time-moment tallies of one event (moments >= 1): facet counter, texture cell, profile
 __device__ __noinline__ void tally_moments(const DevModel& M, const DevTally& T, const BlockTally& B, int f, double time,
                                            unsigned long long des, unsigned long long hits, unsigned long long abs_,
                                            unsigned long long s1ov, unsigned long long svort, unsigned long long s1v,
                                            int cell, unsigned long long cell_count, bool count_hit,
-                                           unsigned long long vf, double cosn, double vel, double u, double v,
-                                           unsigned long long q1, unsigned long long q2) {
+                                           unsigned long long vf, unsigned long long of, double cosn, double vel,
+                                           double u, double v, unsigned long long q1, unsigned long long q2) {
     const bool prof = (M.info[f].flags & FF_PROFILE) != 0;
     for_moments(M, time, [&](int m) {
         facet_add(M, T, B, f, m, hits, des, abs_, s1ov, svort, s1v);
         if (cell >= 0) cell_add(T.texture + ((size_t)m * M.texture_cells + cell) * TT_N, cell_count, s1ov, svort);
-        if (prof) profile_add(M, T, f, m, count_hit, vf, 1, cosn, vel, u, v, q1, q2);
+        if (prof) profile_add(M, T, f, m, count_hit, vf, of, cosn, vel, u, v, q1, q2);
     });
+}
+
+// RegisterTransparentPass (Particle.cpp:1232-1257): crossing a transparent facet counts a hit
+// whose 1/v_ort and v_ort sums are doubled (the particle crosses, it does not turn back), on
+// the facet, its texture (countTrans), profile, direction cells and angle map, in the moment
+// windows holding the crossing time.  Returns v_ort.
+template <bool kFP32, class R>
+__device__ __noinline__ double transparent_pass(const DevModel& M, const DevTally& T, const BlockTally& B, int f,
+                                                R t, R u, R v, double time, R vel, R dx, R dy, R dz) {
+    const FacetInfo& In = M.info[f];
+    R cosn;
+    double tp;
+    if (kFP32) {
+        cosn = fabsf(dx * M.phys_f[f].N[0] + dy * M.phys_f[f].N[1] + dz * M.phys_f[f].N[2]);
+        tp = time + (double)((float)t * (0.01f / (float)vel));
+    } else {
+        cosn = (R)fabs((double)dx * M.isect_d[f].v[0] + (double)dy * M.isect_d[f].v[1] + (double)dz * M.isect_d[f].v[2]);
+        tp = time + (double)t / 100.0 / (double)vel;
+    }
+    R ort = vel * cosn;
+    unsigned long long q1 = kFP32 ? qf(1.0f / (float)ort, (float)MFG_SCALE_INV) : qd(1.0 / (double)ort, MFG_SCALE_INV);
+    unsigned long long q2 = kFP32 ? qf((float)ort, (float)MFG_SCALE_V) : qd((double)ort, MFG_SCALE_V);
+    unsigned long long q3 = kFP32 ? qf(1.0f / (float)vel, (float)MFG_SCALE_INV) : qd(1.0 / (double)vel, MFG_SCALE_INV);
+    facet_add(M, T, B, f, 0, 1, 0, 0, 2 * q1, 2 * q2, q3);
+    const int cell = (In.tex_off >= 0 && (In.count & MFG_COUNT_TRANS)) ? texture_cell<kFP32>(M, f, u, v) : -1;
+    if (cell >= 0) cell_add(T.texture + (size_t)cell * TT_N, 1, 2 * q1, 2 * q2);
+    if (In.count & MFG_COUNT_DIR)
+        direction_add(M, T, f, (double)u, (double)v, tp, (double)dx * (double)vel, (double)dy * (double)vel,
+                      (double)dz * (double)vel);
+    if (In.flags & FF_PROFILE) profile_add(M, T, f, 0, true, 2, 2, (double)cosn, (double)vel, (double)u, (double)v, q1, q2);
+    if (In.flags & FF_ANGLEMAP) anglemap_add(M, T, f, (double)dx, (double)dy, (double)dz);
+    if (M.nm)
+        tally_moments(M, T, B, f, tp, 0, 1, 0, 2 * q1, 2 * q2, q3, cell, 1, true, 2, 2, (double)cosn, (double)vel,
+                      (double)u, (double)v, q1, q2);
+    return (double)ort;
 }
 
 // General relaunch (any accommodation, temperature parameter, sojourn time, reflection
@@ -454,7 +472,12 @@ __device__ __noinline__ void sens_output(const SensCtl& S, const int* traj, int 
     if (src >= 0) atomicAdd(S.Cs + (size_t)src * MFG_SENS_NOUT + j, y);
 }
 
-template <bool kFP32, int kMinBlocks, bool kSens = false>
+// stand-in for the pass list in variants built for models without transparent facets
+struct NoTranspList {
+    static constexpr int n = 0;
+};
+
+template <bool kFP32, int kMinBlocks, bool kSens = false, bool kTr = false>
 __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_constant__ DevModel M, DevTally T, LaunchCtl C) {
     typedef typename Real_<kFP32>::T R;
     extern __shared__ unsigned long long smem[];
@@ -660,7 +683,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
             if (cell >= 0) cell_add(T.texture + (size_t)cell * TT_N, 1, a1, a2);
             if (In.flags & FF_PROFILE) profile_add(M, T, fo, 0, false, vf, 1, (double)cosn, (double)vel, (double)pu, (double)pv, q1, q2);
             if (M.nm)
-                tally_moments(M, T, B, fo, P.time, des ? 1 : 0, 0, 0, vf * q1, q2, q3, cell, des ? 1 : 0, false, vf,
+                tally_moments(M, T, B, fo, P.time, des ? 1 : 0, 0, 0, vf * q1, q2, q3, cell, des ? 1 : 0, false, vf, 1,
                               (double)cosn, (double)vel, (double)pu, (double)pv, q1, q2);
             pend = false;
             pend_cell = -1;
@@ -674,13 +697,32 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
         double ht;
         R hu, hv;
         const double ddx = (double)dx, ddy = (double)dy, ddz = (double)dz;
-        if (kFP32) {
+        // transparent and semi-transparent facets: passes of this ray, opacity draws keyed by
+        // (particle, trace step, facet) in a stream of their own
+        typename std::conditional<kTr, TranspList<R>, NoTranspList>::type tl;
+        OpacCtx oc;
+        TranspList<R>* tlp = nullptr;
+        const OpacCtx* ocp = nullptr;
+        if constexpr (kTr) {
+            tl.n = 0;
+            oc.k0 = rng.k0 ^ (rng.inst * 0x9E3779B9u);
+            oc.k1 = rng.k1 ^ 0xA5A5A5A5u;
+            oc.p0 = rng.p0;
+            oc.p1 = rng.p1;
+            oc.step = (uint32_t)P.bounces;
+            oc.time = P.time;
+            tlp = &tl;
+            ocp = &oc;
+        }
+        if constexpr (kFP32) {
             bool amb = false;
-            HitF h = trace_f(M, root, make_ray_f(P.ox, P.oy, P.oz, (float)dx, (float)dy, (float)dz), P.last, amb,
-                             T.global + TG_STATUS);
+            HitF h = trace_f<kTr>(M, root, make_ray_f(P.ox, P.oy, P.oz, (float)dx, (float)dy, (float)dz), P.last, amb,
+                                  T.global + TG_STATUS, tlp, ocp);
             if (amb || h.f < 0) {
                 ++c_rechk;
-                HitD hd = trace_d(M, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last, T.global + TG_STATUS);
+                if constexpr (kTr) tl.n = 0;
+                HitD hd = trace_d<R, kTr>(M, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last, T.global + TG_STATUS, tlp,
+                                          ocp);
                 hf = hd.f; ht = hd.t; hu = (R)hd.u; hv = (R)hd.v;
             } else {
                 hf = h.f;
@@ -694,7 +736,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                 ht = (double)h.t + (double)((float)r / (float)den);
             }
         } else {
-            HitD h = trace_d(M, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last, T.global + TG_STATUS);
+            HitD h = trace_d<R, kTr>(M, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last, T.global + TG_STATUS, tlp, ocp);
             hf = h.f; ht = h.t; hu = (R)h.u; hv = (R)h.v;
         }
         if (hf < 0) {   // leak (Particle.cpp:387-392)
@@ -712,6 +754,16 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
         if (M.enable_decay) {
             double dd = (double)vel * 100.0 * (P.decay_at - P.time);
             if (dd < travel) { travel = dd; event = 2; }
+        }
+        if constexpr (kTr) {
+            for (int k = 0; k < tl.n; ++k) {
+                if (!((double)tl.t[k] < travel)) continue;
+                double ort_t = transparent_pass<kFP32>(M, T, B, tl.f[k], tl.t[k], tl.u[k], tl.v[k], P.time, vel, dx, dy, dz);
+                if (kSens) {
+                    int g = C.sens.gauge_of_facet[tl.f[k]];
+                    if (g >= 0) sens_output(C.sens, traj, ntraj, src_idx, g, 2.0 * ort_t);
+                }
+            }
         }
         P.ox = P.ox + travel * ddx;
         P.oy = P.oy + travel * ddy;
@@ -745,6 +797,8 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
         int cell = (In.tex_off >= 0 && (In.count & (absorb ? MFG_COUNT_ABS : MFG_COUNT_REFL))) ? texture_cell<kFP32>(M, hf, hu, hv) : -1;
         ++c_hits;
         if (In.flags & FF_ANGLEMAP) anglemap_add(M, T, hf, ddx, ddy, ddz);
+        if (In.count & MFG_COUNT_DIR)
+            direction_add(M, T, hf, (double)hu, (double)hv, P.time, ddx * (double)vel, ddy * (double)vel, ddz * (double)vel);
         if (kSens) {
             int g = C.sens.gauge_of_facet[hf];
             if (g >= 0) sens_output(C.sens, traj, ntraj, src_idx, g, (double)ort);   // incoming half / absorption
@@ -765,13 +819,13 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
             if (cell >= 0) cell_add(T.texture + (size_t)cell * TT_N, 1, 2 * q1, q2);
             if (In.flags & FF_PROFILE) profile_add(M, T, hf, 0, true, 2, 1, (double)cosn, (double)vel, (double)hu, (double)hv, q1, q2);
             if (M.nm)
-                tally_moments(M, T, B, hf, P.time, 0, 1, 1, 2 * q1, q2, q3, cell, 1, true, 2,
+                tally_moments(M, T, B, hf, P.time, 0, 1, 1, 2 * q1, q2, q3, cell, 1, true, 2, 1,
                               (double)cosn, (double)vel, (double)hu, (double)hv, q1, q2);
             need_new = true;
         } else {        // incoming half of PerformBounce (Particle.cpp:735-767)
             if (In.flags & FF_PROFILE) profile_add(M, T, hf, 0, true, 1, 1, (double)cosn, (double)vel, (double)hu, (double)hv, q1, q2);
             if (M.nm)
-                tally_moments(M, T, B, hf, P.time, 0, 1, 0, q1, q2, q3, cell, 1, true, 1,
+                tally_moments(M, T, B, hf, P.time, 0, 1, 0, q1, q2, q3, cell, 1, true, 1, 1,
                               (double)cosn, (double)vel, (double)hu, (double)hv, q1, q2);
             P.last = hf;
             pend = true;
@@ -828,16 +882,19 @@ __global__ void replay_kernel(const __grid_constant__ DevModel M, int precision,
     double ox = origin[3 * i], oy = origin[3 * i + 1], oz = origin[3 * i + 2];
     double dx = dir[3 * i], dy = dir[3 * i + 1], dz = dir[3 * i + 2];
     int root = M.roots[0];
+    const OpacCtx oc = replay_opacity();
+    const OpacCtx* ocp = M.has_transparent ? &oc : nullptr;
     if (precision == 0) {
-        HitD h = trace_d(M, root, ox, oy, oz, dx, dy, dz, last[i], status);
+        HitD h = trace_d<double>(M, root, ox, oy, oz, dx, dy, dz, last[i], status, nullptr, ocp);
         hit_f[i] = h.f;
         hit_t[i] = h.f >= 0 ? h.t : -1.0;
     } else {
         bool amb = false;
-        HitF h = trace_f(M, root, make_ray_f(ox, oy, oz, (float)dx, (float)dy, (float)dz), last[i], amb, status);
+        HitF h = trace_f(M, root, make_ray_f(ox, oy, oz, (float)dx, (float)dy, (float)dz), last[i], amb, status,
+                         nullptr, ocp);
         if (amb || h.f < 0) {
             atomicAdd(rechecks, 1ull);
-            HitD hd = trace_d(M, root, ox, oy, oz, dx, dy, dz, last[i], status);
+            HitD hd = trace_d<double>(M, root, ox, oy, oz, dx, dy, dz, last[i], status, nullptr, ocp);
             hit_f[i] = hd.f;
             hit_t[i] = hd.f >= 0 ? hd.t : -1.0;
         } else {

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include "device_model.h"
+#include "philox.cuh"
 
 #ifndef MFG_AMB_HOOK
 #define MFG_AMB_HOOK(reason)
@@ -13,6 +14,71 @@
 namespace mfgk {
 
 constexpr int kStack = 64;
+
+// InterpolateY (no extrapolation) for time-dependent parameters
+__device__ __noinline__ double param_at(const DevModel& M, int p, double t) {
+    int s = M.par_start[p], e = M.par_start[p + 1], n = e - s;
+    const double* xs = M.par_t + s;
+    const double* ys = M.par_v + s;
+    if (n == 1) return ys[0];
+    int lo = 0, hi = n;
+    while (lo < hi) { int mid = (lo + hi) >> 1; if (xs[mid] <= t) lo = mid + 1; else hi = mid; }
+    int i = lo - 1;
+    if (i < 0) return ys[0];
+    if (i >= n - 1) return ys[n - 1];
+    bool lx = M.par_logx[p], ly = M.par_logy[p];
+    double w = lx ? (log10(t) - log10(xs[i])) / (log10(xs[i + 1]) - log10(xs[i])) : (t - xs[i]) / (xs[i + 1] - xs[i]);
+    if (ly) return exp10(log10(ys[i]) + (log10(ys[i + 1]) - log10(ys[i])) * w);
+    return ys[i] + (ys[i + 1] - ys[i]) * w;
+}
+
+
+// ---------------------------------------------------------- opacity ----
+#define MFG_MAX_TRANSP 32
+// Transparent passes found during one trace (candidates of RegisterTransparentPass)
+template <class T>
+struct TranspList {
+    int n;
+    int f[MFG_MAX_TRANSP];
+    T t[MFG_MAX_TRANSP], u[MFG_MAX_TRANSP], v[MFG_MAX_TRANSP];
+};
+// A partial-opacity decision is an order-independent draw per (particle, trace step, facet)
+// from a Philox stream keyed apart from the particle's own stream.
+struct OpacCtx {
+    uint32_t k0, k1, p0, p1, step;
+    double time;
+};
+__device__ __forceinline__ bool is_hard(const DevModel& M, int f, int cls, const OpacCtx* oc) {
+    if (cls == 0) return true;
+    if (cls == 1 || !oc) return false;
+    const FacetInfo2& I2 = M.info2[f];
+    double op = I2.opac_param >= 0 ? param_at(M, I2.opac_param, oc->time) : I2.opacity;
+    if (op >= 1.0) return true;
+    if (op <= 0.0) return false;
+    uint32_t c0 = oc->p0, c1 = oc->p1, c2 = oc->step, c3 = (uint32_t)f + 1u;
+    philox4x32_10(c0, c1, c2, c3, oc->k0, oc->k1);
+    return u01d(c0, c1) < op;
+}
+// opacity draws of a ray replayed on its own: particle 0, step 0, time 0, seed 0
+__device__ __forceinline__ OpacCtx replay_opacity() {
+    OpacCtx oc;
+    oc.k0 = 0u;
+    oc.k1 = 0xA5A5A5A5u;
+    oc.p0 = oc.p1 = oc.step = 0u;
+    oc.time = 0.0;
+    return oc;
+}
+template <class T>
+__device__ __forceinline__ void add_transp(TranspList<T>* tl, int f, double t, double u, double v,
+                                           unsigned long long* status) {
+    if (!tl) return;
+    if (tl->n < MFG_MAX_TRANSP) {
+        tl->f[tl->n] = f; tl->t[tl->n] = (T)t; tl->u[tl->n] = (T)u; tl->v[tl->n] = (T)v;
+        ++tl->n;
+    } else {
+        atomicOr(status, KS_TRANSP);
+    }
+}
 
 // -------------------------------------------------- point in polygon ----
 __device__ __forceinline__ bool crossing_d(const double2* v2, int vs, int nv, double u, double v) {
@@ -43,9 +109,12 @@ struct HitD {
     double t, u, v;
 };
 
-// closest hard hit of the ray (skipping facet `last`); BVH of structure `root`
+// closest hard hit of the ray (skipping facet `last`); BVH of structure `root`.  Transparent
+// candidates (opacity 0, or a partial-opacity draw above the opacity) go to `tl`.
+template <class LT = double, bool kTr = true>
 __device__ __noinline__ HitD trace_d(const DevModel& M, int root, double ox, double oy, double oz,
-                                     double dx, double dy, double dz, int last, unsigned long long* status) {
+                                     double dx, double dy, double dz, int last, unsigned long long* status,
+                                     TranspList<LT>* tl = nullptr, const OpacCtx* oc = nullptr) {
     HitD h;
     h.f = -1;
     h.t = 1.0e99;
@@ -79,7 +148,8 @@ __device__ __noinline__ HitD trace_d(const DevModel& M, int root, double ox, dou
                 const FacetIsectD& R = M.isect_d[f];
                 double Nx = R.v[0], Ny = R.v[1], Nz = R.v[2], D = R.v[3];
                 double den = Nx * dx + Ny * dy + Nz * dz;
-                bool two = __double_as_longlong(R.v[7]) != 0;   // two-sided flag kept in the record
+                const long long fl = __double_as_longlong(R.v[7]);   // bit 0 two-sided, bits 1-2 opacity class
+                const bool two = (fl & 1) != 0;
                 if (!two && den >= 0.0) continue;
                 if (den == 0.0) continue;
                 double t = (D - (Nx * ox + Ny * oy + Nz * oz)) / den;
@@ -90,6 +160,10 @@ __device__ __noinline__ HitD trace_d(const DevModel& M, int root, double ox, dou
                 double v = px * R.v[12] + py * R.v[13] + pz * R.v[14];
                 if (v < 0.0 || v > 1.0) continue;
                 if (!in_facet_d(M, f, u, v)) continue;
+                if constexpr (kTr) {
+                    const int cls = (int)((fl >> 1) & 3);
+                    if (cls != 0 && !is_hard(M, f, cls, oc)) { add_transp(tl, f, t, u, v, status); continue; }
+                }
                 if (t < h.t || f < h.f) { h.f = f; h.t = t; h.u = u; h.v = v; }
             }
         }
@@ -150,9 +224,11 @@ __device__ __forceinline__ RayF make_ray_f(double ox, double oy, double oz, floa
     return r;
 }
 
-// FacetIsectF layout: [N0 N1 N2 Olo0 | Ohi0 Ohi1 Ohi2 Olo1 | Us0 Us1 Us2 Olo2 | Vs0 Vs1 Vs2 -]
+// FacetIsectF layout: [N0 N1 N2 Olo0 | Ohi0 Ohi1 Ohi2 Olo1 | Us0 Us1 Us2 Olo2 | Vs0 Vs1 Vs2 flags]
+template <bool kTr = true>
 __device__ __noinline__ HitF trace_f(const DevModel& M, int root, const RayF& ray, int last, bool& ambiguous,
-                                     unsigned long long* status) {
+                                     unsigned long long* status, TranspList<float>* tl = nullptr,
+                                     const OpacCtx* oc = nullptr) {
     HitF h;
     h.f = -1;
     h.t = 3.0e38f;
@@ -189,7 +265,8 @@ __device__ __noinline__ HitF trace_f(const DevModel& M, int root, const RayF& ra
                 const FacetIsectF& R = M.isect_f[f];
                 float Nx = R.v[0], Ny = R.v[1], Nz = R.v[2];
                 float den = Nx * dx + Ny * dy + Nz * dz;
-                bool two = R.v[15] != 0.0f;                      // two-sided flag kept in the record
+                const int fl = (int)R.v[15];                     // bit 0 two-sided, bits 1-2 opacity class
+                const bool two = (fl & 1) != 0;
                 float aden = fabsf(den);
                 // back-face culling is exact when N.d is well above its rounding error
                 if (!two && den > 1e-6f) continue;
@@ -235,6 +312,10 @@ __device__ __noinline__ HitF trace_f(const DevModel& M, int root, const RayF& ra
                     continue;
                 }
                 if (!inside) continue;
+                if constexpr (kTr) {
+                    const int cls = (fl >> 1) & 3;
+                    if (cls != 0 && !is_hard(M, f, cls, oc)) { add_transp(tl, f, t, u, v, status); continue; }
+                }
                 // certain hit; ambiguous ordering when it is within error bounds of the best
                 if (h.f >= 0 && fabsf(t - h.t) <= tol + htol) { ambiguous = true; MFG_AMB_HOOK(5); }
                 if (t < h.t) { h.f = f; h.t = t; h.u = u; h.v = v; htol = tol; }

@@ -13,7 +13,7 @@ import math
 import numpy as np
 
 from . import _abi as A
-from .model import Model, build_pipe
+from .model import FACET_FIELDS, Model, build_pipe
 
 
 def config1_tube(texture_facet=2, tex=64):
@@ -158,4 +158,51 @@ def config2_beam_chamber(n_around=50, n_rings=2000, length=500.0, a=3.0, b=1.5, 
     m.anglemap_theta_higher_res[p1] = 0
     m.anglemap_theta_limit[p1] = math.pi / 2
     m.kind = kind
+    return m
+
+
+def transparent_tube(transient=False, n_disk=48):
+    """Config-1 tube with three two-sided disks across it: z = 2.5 cm fully transparent
+    (opacity 0), z = 5 cm semi-transparent (opacity 0.5), z = 7.5 cm with a time-dependent
+    opacity parameter (0.2 -> 0.8 over 1 ms).  Each disk has an 8x8 texture counting
+    transparent passes, a U profile, and the middle one direction vectors and an angle map.
+    With `transient`, the 1 ms inlet pulse and 40 log-spaced moments of config 3 are added."""
+    base = config1_tube()
+    V = [base.vertices]
+    facets = [list(f) for f in base.facets]
+    r = 1.0 * math.cos(math.pi / 64) * 0.999          # inside the 64-gon's inscribed circle
+    ang = np.arange(n_disk) / n_disk * 2 * math.pi
+    nv = len(base.vertices)
+    disks = []
+    for z in (2.5, 5.0, 7.5):
+        ring = np.stack([r * np.cos(ang), r * np.sin(ang), np.full(n_disk, z)], axis=1)
+        V.append(ring)
+        disks.append(len(facets))
+        facets.append(list(range(nv, nv + n_disk)))
+        nv += n_disk
+    m = Model(np.concatenate(V), facets)
+    for k in FACET_FIELDS:
+        getattr(m, k)[:base.n_facets] = getattr(base, k)
+    d0, d1, d2 = disks
+    for d in disks:
+        m.is_2sided[d] = 1
+        m.sticking[d] = 0.0
+        m.tex_width[d] = 8.0
+        m.tex_height[d] = 8.0
+        m.count_flags[d] = A.COUNT_TRANS | A.COUNT_REFL | A.COUNT_ABS
+        m.profile_type[d] = A.PROFILE_U
+    m.opacity[d0] = 0.0
+    m.opacity[d1] = 0.5
+    m.count_flags[d1] |= A.COUNT_DIR
+    m.anglemap_record[d1] = 1
+    m.anglemap_phi_width[d1] = 36
+    m.anglemap_theta_limit[d1] = math.pi / 4
+    m.anglemap_theta_lower_res[d1] = 9
+    m.anglemap_theta_higher_res[d1] = 9
+    m.opacity_param[d2] = m.add_param([0.0, 1e-3], [0.2, 0.8])
+    m.disks = disks
+    if transient:
+        m.constant_flow = 0
+        m.set_moments(np.logspace(-5, -1, 40), 1e-5)
+        m.outgassing_param[0] = m.add_param([0.0, 1e-3, 1e-3 * (1 + 1e-9), 10.0], [10.0, 10.0, 0.0, 0.0])
     return m

@@ -66,8 +66,37 @@ def _parse_user_moments(um_node):
     return times, windows
 
 
-def load(path_or_bytes, with_state=True):
-    """Return (model, state or None, info dict)."""
+def load_catalog(folder):
+    """Parameters of a parameter-catalog folder: one parameter per .csv file of 't,value'
+    rows, named "[catalog] <file name>", pairs kept sorted by t, linear interpolation
+    (TimeDependentParameters::LoadParameterCatalog, MolflowSimGeom.cpp:1250-1319).
+    Returns a list of (name, t, v)."""
+    import os
+    out = []
+    if folder is None or not os.path.isdir(folder):
+        return out
+    for fn in sorted(os.listdir(folder)):
+        if not fn.endswith(".csv"):
+            continue
+        pairs = []
+        with open(os.path.join(folder, fn), encoding="utf-8-sig") as f:
+            for line in f:
+                row = [c.strip() for c in line.strip().split(",")]
+                if row == [""]:
+                    continue
+                if len(row) != 2:
+                    break
+                pairs.append((float(row[0]), float(row[1])))
+        pairs.sort(key=lambda p: p[0])
+        out.append(("[catalog] " + fn, np.array([p[0] for p in pairs]), np.array([p[1] for p in pairs])))
+    return out
+
+
+def load(path_or_bytes, with_state=True, catalog=()):
+    """Return (model, state or None, info dict).
+
+    `catalog`: parameters of a parameter catalog (see load_catalog); they follow the file's
+    own parameters, as in the reference (InsertParametersBeforeCatalog)."""
     r = _root(path_or_bytes)
     g = r.find("Geometry")
     vnode = g.find("Vertices")
@@ -85,13 +114,19 @@ def load(path_or_bytes, with_state=True):
             v = [float(x.get("value")) for x in p.findall("Moment")]
             m.add_param(t, v, logx=_i(p, "logXinterp"), logy=_i(p, "logYinterp"))
             names.append(p.get("name"))
+    for nm, t, v in catalog:
+        m.add_param(t, v)
+        names.append(nm)
 
     def param_ref(node, name_attr):
+        # by name (2.9.15+ files), else by index into file + catalog parameters (LoaderXML.cpp:847-925)
         if node is None:
             return -1
         if node.get(name_attr):
             nm = node.get(name_attr)
-            return names.index(nm) if nm in names else -1
+            if nm not in names:
+                raise ValueError("parameter %r not found" % nm)
+            return names.index(nm)
         return _i(node, "parameterId", -1)
 
     for k, f in enumerate(fnodes):

@@ -14,6 +14,9 @@
 static int64_t g_reasons[8];
 #define MFG_AMB_HOOK(r) (++g_reasons[(r)])
 static inline long long __double_as_longlong(double x) { long long i; std::memcpy(&i, &x, sizeof i); return i; }
+static inline double __longlong_as_double(long long i) { double x; std::memcpy(&x, &i, sizeof x); return x; }
+static inline float __uint_as_float(unsigned u) { float x; std::memcpy(&x, &u, sizeof x); return x; }
+static inline unsigned __umulhi(unsigned a, unsigned b) { return (unsigned)(((unsigned long long)a * b) >> 32); }
 static inline unsigned long long atomicOr(unsigned long long* p, unsigned long long v) {
     unsigned long long o = *p; *p |= v; return o;
 }

@@ -27,6 +27,7 @@ CASES = {
     "B01-lr1000_pipe": {"tex": [], "prof": "all"},
     "B02-lr10_pipe_tex": {"tex": [2, 252, 502, 752, 1001], "prof": []},
     "B03-lr10_pipe_prof": {"tex": [], "prof": [2, 252, 502, 752, 1001]},
+    "B04-lr10_pipe_trans": {"tex": [0, 1, 2, 500, 1001, 1002, 1003, 1004], "prof": []},
 }
 
 
@@ -61,5 +62,7 @@ def save_case(src_dir, name, keep):
 
 if __name__ == "__main__":
     src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/tests/TestCases"
+    only = sys.argv[2:]
     for name, keep in CASES.items():
-        save_case(src, name, keep)
+        if not only or name in only:
+            save_case(src, name, keep)

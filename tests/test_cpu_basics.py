@@ -103,6 +103,39 @@ def test_oracle_pinned_to_b01_long_tube():
     assert abs(p - p_ref) < 3 * math.hypot(binom_sigma(p, n), binom_sigma(p_ref, n_ref))
 
 
+def b04_compare(st, n, ref):
+    """Per-desorption hits on B04's transparent and opaque facets against the stored state.
+
+    B04 stacks three identical L/R=10 tubes: the first two are transparent (opacity 0),
+    the third opaque.  Transparent passes are counted as hits (RegisterTransparentPass)."""
+    n_ref = ref["ref_global"][A.G_NBDESORBED]
+    fc_ref = ref["ref_facet_counts"]
+    fc = st.facet_counts[0]
+    groups = {"in1": [0], "out1": [1], "in2": [1002], "out2": [1003], "in3": [2004], "out3": [2005],
+              "walls1": list(range(2, 1002)), "walls2": list(range(1004, 2004))}
+    z = {}
+    for name, fs in groups.items():
+        a = fc[fs, A.FC_NBMCHIT].sum() / n
+        b = fc_ref[fs, A.FC_NBMCHIT].sum() / n_ref
+        z[name] = (a - b) / math.sqrt(a / n + b / n_ref)
+    # texture of a transparent facet counts the passes (countTrans)
+    for f in (0, 1002):
+        a = st.texture_of(f)[..., 0].sum() / n
+        b = ref["ref_tex_%d" % f][..., 0].sum() / n_ref
+        z["tex%d" % f] = (a - b) / math.sqrt(a / n + b / n_ref)
+    return z
+
+
+def test_oracle_pinned_to_b04_transparent_tubes():
+    m, ref, _ = golden_util.load("B04-lr10_pipe_trans")
+    assert (m.opacity[:2004] == 0).all() and (m.opacity[2004:] == 1).all()
+    n = 200000
+    st, s = O.Oracle(m).run(n, seed=SEED)
+    assert s["leaks"] == 0
+    z = b04_compare(st, n, ref)
+    assert max(abs(v) for v in z.values()) < z_threshold(len(z)), z
+
+
 def test_oracle_negative_control_detects_wrong_sticking():
     """The comparator must reject a wrong model (cf. the reference's ResultsWrong test)."""
     m, ref, _ = golden_util.load("01-quick_pipe_profiles_textures_2sided")

@@ -152,7 +152,6 @@ def test_golden_b02_transmission_and_wall_texture():
 
 def test_golden_quick_pipe_profile_and_two_sided():
     m, ref, meta = golden_util.load("01-quick_pipe_profiles_textures_2sided")
-    m.count_flags[:] &= ~np.uint32(A.COUNT_DIR)   # direction cells are not traced on the GPU
     n = 4_000_000
     sim = GpuSimulation(m)
     sim.SimulationMCStep(n, precision=A.PREC_FP32R, seed=SEED)
@@ -167,6 +166,24 @@ def test_golden_quick_pipe_profile_and_two_sided():
     pr = ref["ref_prof_4"][:, 0] / n_ref
     zp = (pu - pr) / np.sqrt(pu / n + pr / n_ref)
     assert np.abs(zp).max() < z_threshold(100) + 1.0
+
+
+def test_fp64_quick_pipe_all_tallies_equal_oracle():
+    """Fixture 01 geometry (5-gon tube, 2-sided facet, U profile, 50x12 texture with direction
+    cells): FP64 kernel and oracle on the same particles give the same integer tallies."""
+    m, ref, meta = golden_util.load("01-quick_pipe_profiles_textures_2sided")
+    n = 50000
+    sim = GpuSimulation(m)
+    sim.SimulationMCStep(n, precision=A.PREC_FP64, seed=SEED)
+    g = sim.fetch()
+    r, _ = Oracle(m).run(n, seed=SEED)
+    assert np.array_equal(g.facet_counts, r.facet_counts)
+    assert np.array_equal(g.texture[..., 0], r.texture[..., 0])
+    assert np.array_equal(g.profile[..., 0], r.profile[..., 0])
+    assert np.array_equal(g.direction[..., 3], r.direction[..., 3])
+    np.testing.assert_allclose(g.direction[..., :3], r.direction[..., :3], rtol=1e-9, atol=1e-6)
+    np.testing.assert_allclose(g.profile, r.profile, rtol=1e-8, atol=1e-6)
+    np.testing.assert_allclose(g.texture, r.texture, rtol=1e-8, atol=1e-6)
 
 
 def clausing_santeler(l_over_r):
@@ -251,7 +268,7 @@ def test_autotune_and_occupancy_variants_agree(tube):
 
 def test_unsupported_feature_is_reported():
     m = config1_tube()
-    m.opacity[5] = 0.5
+    m.teleport_dest[5] = 3
     sim = GpuSimulation(m)
     with pytest.raises(MfgError) as e:
         sim.SimulationMCStep(10)

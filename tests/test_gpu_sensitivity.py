@@ -52,9 +52,11 @@ def test_gradients_match_central_differences(setup):
         sf.forward(n, seed=SEED)
         js.append(sf.jacobian()[0])
     js = np.array(js)
-    jm, jse = js.mean(0), js.std(0, ddof=1) / math.sqrt(nb)
-    # parameters with the largest pumped-flux sensitivity, and the one most coupled to gauge 0
-    pick = list(np.argsort(-np.abs(jm[:, 8]))[:3]) + [int(np.argmax(np.abs(jm[:, 0])))]
+    # parameters with the largest pumped-flux sensitivity, and the one most coupled to gauge 0,
+    # chosen on batch 0 and estimated on the other batches (the largest of 1000 noisy
+    # estimates is biased upwards)
+    pick = list(np.argsort(-np.abs(js[0, :, 8]))[:3]) + [int(np.argmax(np.abs(js[0, :, 0])))]
+    jm, jse = js[1:].mean(0), js[1:].std(0, ddof=1) / math.sqrt(nb - 1)
     for k in pick:
         f = int(m.neg[k])
         s0 = float(m.sticking[f])
@@ -103,20 +105,29 @@ def test_gradient_cost_over_forward(setup):
 def test_gradient_matches_oracle_finite_difference(setup):
     """Finite difference of the CPU oracle (common random numbers) for the strongest pumped-flux parameter."""
     m, sim, sf = setup
-    sim.ResetSimulation()
-    sim.set_particle_offset(0)
-    sf.forward(8_000_000, seed=SEED)
-    js = sf.jacobian()[0]
-    k = int(np.argmax(np.abs(js[:, 8])))
+    nb, nj = 4, 4_000_000
+    est = []
+    for b in range(nb + 1):
+        sim.ResetSimulation()
+        sim.set_particle_offset(b * nj)
+        sf.forward(nj, seed=SEED)
+        est.append(sf.jacobian()[0][:, 8])
+    # parameter chosen on the first batch, gradient estimated on the others (no selection bias)
+    k = int(np.argmax(np.abs(est[0])))
+    jk = np.array([e[k] for e in est[1:]])
+    jm, jse = jk.mean(), jk.std(ddof=1) / math.sqrt(nb)
     f = int(m.neg[k])
     s0 = float(m.sticking[f])
-    n = 400000
+    n = 4_000_000
     vals = []
     for s in (s0 + 5 * DS, s0 - 5 * DS):
         mm = config5_neg_tube()
         mm.sticking[f] = s
         st, _ = Oracle(mm).run(n, seed=SEED)
         vals.append(outputs_from_state(st, mm, n)[8])
+        hits_f = st.facet_counts[0, f, A.FC_NBMCHIT] / n
     fd = (vals[0] - vals[1]) / (10 * DS)
-    # CRN noise of the oracle difference: flips at facet f only; allow 25 % + 3 sigma
-    assert abs(fd - js[k, 8]) < 0.25 * abs(js[k, 8]) + 3 * math.sqrt(abs(js[k, 8]) * 10 * DS / n) / (10 * DS), (fd, js[k, 8])
+    # common random numbers: only particles whose stick/reflect decision at facet f flips
+    # (about hits_f * 10 DS per desorption) can change the output, each by at most one
+    sigma = math.sqrt(hits_f * 10 * DS * n) / (n * 10 * DS)
+    assert abs(fd - jm) < 0.1 * abs(jm) + 3 * math.hypot(sigma, jse), (fd, jm, sigma, jse)
