@@ -309,6 +309,19 @@ int mfg_replay(mfg_sim* sim, int32_t precision, int64_t n_rays,
                const double* origin, const double* direction, const int32_t* last_facet,
                int32_t* hit_facet, double* hit_t, uint64_t* n_rechecks);
 
+/* Replay that allocates no device memory.  No counterpart in the reference.
+ * For callers that cannot allocate on the device during a query: a process whose device memory
+ * belongs to another framework's pool allocator, or a loop that must not block in cudaMalloc or
+ * cudaFree (they can synchronise the device).  d_origin, d_direction, d_last, d_hit_facet and
+ * d_hit_t are device pointers with the meaning of mfg_replay's host buffers.  The FP64 recheck
+ * queue lives in a fixed 8 MiB array in the library, so n may not exceed 1,048,576 rays
+ * (MFG_ERR_LIMIT otherwise).  The first call on a device looks up that array's device address;
+ * make it before any stream capture.  The array is shared by all calls and keeps the last
+ * call's contents: each call clears the counters it needs, and calls that overlap on the GPU
+ * race.  Runs on the handle's stream and returns when the results are written. */
+int mfg_replay_noalloc(mfg_sim* sim, int32_t precision, int64_t n, const double* d_origin, const double* d_direction,
+                       const int32_t* d_last, int32_t* d_hit_facet, double* d_hit_t, uint64_t* n_rechecks);
+
 #ifdef __cplusplus
 }
 #endif

@@ -930,3 +930,116 @@ int mfg_replay(mfg_sim* s, int32_t precision, int64_t n, const double* origin, c
 
 }  // extern "C"
 
+// ---------------------------------------------------------------------------
+// Replay without device allocations.
+//
+// For callers that cannot allocate device memory during a query: a process whose device
+// memory belongs to another framework's pool allocator (a stray cudaMalloc would fall outside
+// that pool's budget), or a control loop that must not block in cudaMalloc/cudaFree, which can
+// synchronise the whole device.  The caller passes device-resident inputs and outputs; the
+// FP64 recheck queue lives in the fixed array below.
+//
+// The array is shared by every call in the process and keeps the last call's contents: each
+// call clears the queue counter and status word before its first kernel, and calls that
+// overlap on the GPU (different streams or threads at the same time) race on it.
+// ---------------------------------------------------------------------------
+#define MFG_NOALLOC_MAX_RAYS (1 << 20)
+// [0] rays queued for the FP64 pass, [1] status bits, [2 ..] queued ray indices  (8 MiB + 16 B)
+static __device__ __align__(256) unsigned long long g_noalloc_scratch[2 + MFG_NOALLOC_MAX_RAYS];
+
+namespace {
+std::mutex g_noalloc_mu;
+unsigned long long* g_noalloc_addr[256];   // device address of g_noalloc_scratch, per device
+
+__global__ void noalloc_pass1(const __grid_constant__ DevModel M, int precision, long long n, const double* origin,
+                              const double* dir, const int* last, int* hit_f, double* hit_t,
+                              unsigned long long* scratch) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double ox = origin[3 * i], oy = origin[3 * i + 1], oz = origin[3 * i + 2];
+    double dx = dir[3 * i], dy = dir[3 * i + 1], dz = dir[3 * i + 2];
+    int root = M.roots[0];
+    const mfgk::OpacCtx oc = mfgk::replay_opacity();
+    const mfgk::OpacCtx* ocp = M.has_transparent ? &oc : nullptr;
+    if (precision == MFG_PREC_FP64) {
+        mfgk::HitD h = mfgk::trace_d<double>(M, root, ox, oy, oz, dx, dy, dz, last[i], scratch + 1, nullptr, ocp);
+        hit_f[i] = h.f;
+        hit_t[i] = h.f >= 0 ? h.t : -1.0;
+        return;
+    }
+    bool amb = false;
+    mfgk::HitF h = mfgk::trace_f(M, root, mfgk::make_ray_f(ox, oy, oz, (float)dx, (float)dy, (float)dz), last[i], amb,
+                                 scratch + 1, nullptr, ocp);
+    if (amb || h.f < 0) {   // queue the ray for the FP64 pass
+        unsigned long long k = atomicAdd(scratch, 1ull);
+        scratch[2 + k] = (unsigned long long)i;
+        return;
+    }
+    const FacetIsectD& Rh = M.isect_d[h.f];
+    double den = Rh.v[0] * dx + Rh.v[1] * dy + Rh.v[2] * dz;
+    double num = Rh.v[3] - (Rh.v[0] * ox + Rh.v[1] * oy + Rh.v[2] * oz);
+    double r = num - (double)h.t * den;
+    hit_f[i] = h.f;
+    hit_t[i] = (double)h.t + (double)((float)r / (float)den);
+}
+
+__global__ void noalloc_pass2(const __grid_constant__ DevModel M, const double* origin, const double* dir,
+                              const int* last, int* hit_f, double* hit_t, unsigned long long* scratch) {
+    unsigned long long k = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= scratch[0]) return;
+    long long i = (long long)scratch[2 + k];
+    const mfgk::OpacCtx oc = mfgk::replay_opacity();
+    mfgk::HitD h = mfgk::trace_d<double>(M, M.roots[0], origin[3 * i], origin[3 * i + 1], origin[3 * i + 2], dir[3 * i],
+                                         dir[3 * i + 1], dir[3 * i + 2], last[i], scratch + 1, nullptr,
+                                         M.has_transparent ? &oc : nullptr);
+    hit_f[i] = h.f;
+    hit_t[i] = h.f >= 0 ? h.t : -1.0;
+}
+}  // namespace
+
+extern "C" int mfg_replay_noalloc(mfg_sim* s, int32_t precision, int64_t n, const double* d_origin,
+                                  const double* d_direction, const int32_t* d_last, int32_t* d_hit_facet,
+                                  double* d_hit_t, uint64_t* n_rechecks) {
+    if (!s || n < 0) return fail(MFG_ERR_INVALID_ARGUMENT, "null simulation or negative ray count");
+    if (precision != MFG_PREC_FP64 && precision != MFG_PREC_FP32R) return fail(MFG_ERR_INVALID_ARGUMENT, "unknown precision");
+    if (n > MFG_NOALLOC_MAX_RAYS)
+        return fail(MFG_ERR_LIMIT, "mfg_replay_noalloc takes at most " + std::to_string(MFG_NOALLOC_MAX_RAYS) +
+                                       " rays per call (" + std::to_string(n) + " given); split the batch");
+    if (n > 0 && (!d_origin || !d_direction || !d_last || !d_hit_facet || !d_hit_t))
+        return fail(MFG_ERR_INVALID_ARGUMENT, "null buffer");
+    if (n_rechecks) *n_rechecks = 0;
+    if (n == 0) return MFG_OK;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
+    if (s->device < 0 || s->device >= 256) return fail(MFG_ERR_NO_DEVICE, "device index out of range");
+    CK(cudaSetDevice(s->device));
+    unsigned long long* scratch;
+    {
+        // set-up, once per device, with that device current: the host-side name of the array is
+        // not a device address, so ask the runtime for the device address
+        std::lock_guard<std::mutex> g(g_noalloc_mu);
+        if (!g_noalloc_addr[s->device]) {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+            g_noalloc_addr[s->device] = static_cast<unsigned long long*>(p);
+        }
+        scratch = g_noalloc_addr[s->device];
+    }
+    CK(cudaMemsetAsync(scratch, 0, 2 * sizeof(unsigned long long), s->stream));   // queue counter and status
+    const int block = 128;
+    const unsigned grid = unsigned((n + block - 1) / block);
+    noalloc_pass1<<<grid, block, 0, s->stream>>>(s->dm, precision, n, d_origin, d_direction, d_last, d_hit_facet,
+                                                  d_hit_t, scratch);
+    CK(cudaGetLastError());
+    if (precision == MFG_PREC_FP32R) {
+        noalloc_pass2<<<grid, block, 0, s->stream>>>(s->dm, d_origin, d_direction, d_last, d_hit_facet, d_hit_t, scratch);
+        CK(cudaGetLastError());
+    }
+    unsigned long long head[2] = {0, 0};
+    CK(cudaMemcpyAsync(head, scratch, sizeof head, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if (head[1] & KS_STACK) return fail(MFG_ERR_LIMIT, "BVH traversal stack overflow");
+    if (n_rechecks) *n_rechecks = head[0];
+    return MFG_OK;
+}
