@@ -25,7 +25,9 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     "c1": dict(name="config1_tube_L10cm_R1cm_64gon_tex64x64_maxwell_N2_293K", step=100_000_000, fp64_step=5_000_000),
     "c2": dict(name="config2_beam_chamber_200k_triangles", step=10_000_000, fp64_step=500_000),
+    "c3": dict(name="config3_tube_1ms_pulse_100_logspaced_moments", step=20_000_000, fp64_step=2_000_000),
     "c4": dict(name="config4_batch_256_instances_1k-50k_facets", step=1_000_000, fp64_step=0),
+    "c5": dict(name="config5_neg_tube_1000_sticking_parameters_8_gauges", step=20_000_000, fp64_step=0),
 }
 
 
@@ -33,6 +35,8 @@ def make_model(workload):
     from molflow_sources_gb300 import workloads
     if workload == "c1":
         return workloads.config1_tube()
+    if workload == "c3":
+        return workloads.config3_transient()
     return workloads.config2_beam_chamber()
 
 
@@ -112,11 +116,20 @@ def bytes_per_hit(model, nodes, prims):
     return nodes * 32 + prims * 64 + 160 + 2 * (4 * 8 + textured * 3 * 8)
 
 
-def cpu_baseline(model, target_s=10.0):
+def calibrate(orc, seed, min_s=0.5):
+    """Desorptions per second of the oracle on all host threads, from a run of at least min_s."""
+    n = 2000
+    while True:
+        st, s = orc.run(n, seed=seed)
+        if s["seconds"] >= min_s or n >= 10 ** 8:
+            return s["desorbed"] / max(s["seconds"], 1e-6)
+        n *= 4
+
+
+def cpu_baseline(model, target_s=12.0):
     from oracle.oracle import Oracle
     orc = Oracle(model)
-    st, s = orc.run(2000, seed=11)
-    rate_des = s["desorbed"] / max(s["seconds"], 1e-6)
+    rate_des = calibrate(orc, 11)
     n = int(max(1000, min(rate_des * target_s, 5e8)))
     st, s = orc.run(n, seed=12, first_particle=10 ** 12)
     return {"value": s["hits"] / s["seconds"], "unit": "hits/s", "cores": s["threads"], "kind": "port",
@@ -136,8 +149,7 @@ def run_reference(args, rank, world):
     orc = Oracle(model)
     for _ in range(args.warmup):
         orc.run(500, seed=3)
-    st, s = orc.run(2000, seed=4)
-    rate_des = s["desorbed"] / max(s["seconds"], 1e-6)
+    rate_des = calibrate(orc, 4)
     n = int(max(500, min(rate_des * args.ref_step_s, 5e8)))
     for k in range(args.steps):
         st, s = orc.run(n, seed=5, first_particle=k * n)
@@ -213,6 +225,56 @@ def run_batch(args, torch, dist, rank, world, local, W, n_step):
     return 0
 
 
+def run_sensitivity(args, torch, dist, rank, world, local, W, n_step):
+    """Config 5: forward run with score-function gradients of 9 outputs with respect to 1000
+    sticking coefficients and every source's outgassing, against the plain forward run."""
+    from molflow_sources_gb300 import _abi as A
+    from molflow_sources_gb300.sensitivity import SensitivityFunction, config5_neg_tube
+    from molflow_sources_gb300.simulation import GpuSimulation
+    m = config5_neg_tube()
+    sim = GpuSimulation(m, device=local)
+    sim.set_particle_offset(rank * (1 << 48))
+    sf = SensitivityFunction(sim, m.neg, m.gauges, m.neg)
+    seed = 0x4D6F6C66
+    for _ in range(args.warmup):
+        sim.SimulationMCStep(n_step // 10, precision=A.PREC_FP32R, seed=seed)
+        sf.forward(n_step // 10, seed=seed)
+    sampler = ClockSampler(local)
+    sampler.start()
+    torch.cuda.synchronize()
+    f_ms = f_hits = s_ms = s_hits = 0.0
+    launches = 0
+    for k in range(args.steps):
+        sim.SimulationMCStep(n_step, precision=A.PREC_FP32R, seed=seed)
+        f_ms += sim.last_stats["kernel_ms"]
+        f_hits += sim.last_stats["hits"]
+        sf.forward(n_step, seed=seed)
+        s_ms += sf.last_stats["kernel_ms"]
+        s_hits += sf.last_stats["hits"]
+        launches += sim.last_stats["kernel_launches"] + sf.last_stats["kernel_launches"]
+    clocks = sampler.stop()
+    # end to end: forward with gradients, then the Jacobian read back to host memory
+    t1 = time.perf_counter()
+    sf.forward(n_step, seed=seed)
+    js, jq, src = sf.jacobian()
+    e2e_s = time.perf_counter() - t1
+    rate = s_hits / (s_ms / 1e3)
+    line = {"metric": "hits/s per GB300 with sticking and outgassing gradients (score function)", "value": rate,
+            "unit": "hits/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": s_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": W["name"], "desorptions_per_step": n_step, "parameters": int(len(m.neg)),
+                       "outputs": 9, "facets": int(m.n_facets)},
+            "forward_hits_per_s": f_hits / (f_ms / 1e3), "gradient_cost_over_forward": (s_ms / s_hits) / (f_ms / f_hits),
+            "gpu_launches": launches, "clocks": clocks,
+            "e2e": {"value": sf.last_stats["hits"] / e2e_s, "unit": "hits/s", "h2d_bytes_per_step": 96,
+                    "d2h_bytes_per_step": int(js.nbytes + jq.nbytes + src.nbytes)},
+            "cpu_baseline": None}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -224,6 +286,10 @@ def main():
     ap.add_argument("--fp64-step", type=int, default=0)
     ap.add_argument("--ref-step-s", type=float, default=6.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--launch", default="",
+                    help="fixed FP32R launch shape BLOCK,BLOCKS_PER_SM instead of the autotuner's choice")
+    ap.add_argument("--profile-steps", action="store_true",
+                    help="bracket the timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -244,6 +310,8 @@ def main():
     n_step = args.step_desorptions or W["step"]
     if args.workload == "c4":
         return run_batch(args, torch, dist, rank, world, local, W, n_step)
+    if args.workload == "c5":
+        return run_sensitivity(args, torch, dist, rank, world, local, W, n_step)
     model = make_model(args.workload)
     t0 = time.time()
     sim = GpuSimulation(model, device=local)
@@ -268,9 +336,14 @@ def main():
         f64_hits += sim.last_stats["hits"]
     fp64_rate = f64_hits / (f64_ms / 1e3)
 
-    tuned = sim.autotune(max(n_step // 20, 10000), precision=A.PREC_FP32R, seed=seed)   # launch shape
+    if args.launch:
+        b_, k_ = (int(x) for x in args.launch.split(","))
+        tuned = {"block_size": b_, "blocks_per_sm": k_}
+    else:
+        tuned = sim.autotune(max(n_step // 20, 10000), precision=A.PREC_FP32R, seed=seed)   # launch shape
+    shape = dict(tuned) if args.launch else {}
     for _ in range(args.warmup):
-        sim.SimulationMCStep(n_step, precision=A.PREC_FP32R, seed=seed)
+        sim.SimulationMCStep(n_step, precision=A.PREC_FP32R, seed=seed, **shape)
     sim.ResetSimulation()
     sampler = ClockSampler(local)
     sampler.start()
@@ -280,15 +353,19 @@ def main():
     rechecks = 0
     launches = 0
     des = 0
+    if args.profile_steps:
+        torch.cuda.profiler.start()
     for k in range(args.steps):
         flush.fill_(k & 0xFF)   # L2 flush between steps (outside the kernel's event pair)
-        sim.SimulationMCStep(n_step, precision=A.PREC_FP32R, seed=seed)
+        sim.SimulationMCStep(n_step, precision=A.PREC_FP32R, seed=seed, **shape)
         st = sim.last_stats
         kernel_ms.append(st["kernel_ms"])
         hits += st["hits"]
         rechecks += st["rechecks"]
         launches += st["kernel_launches"]
         des += st["desorbed"]
+    if args.profile_steps:
+        torch.cuda.profiler.stop()
     barrier()
     # end to end: public API call + tallies copied to host memory every step
     from molflow_sources_gb300.model import SimuState
@@ -297,7 +374,7 @@ def main():
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     for k in range(max(1, args.steps // 2)):
-        sim.SimulationMCStep(n_step, precision=A.PREC_FP32R, seed=seed)
+        sim.SimulationMCStep(n_step, precision=A.PREC_FP32R, seed=seed, **shape)
         e2e_hits += sim.last_stats["hits"]
         sim.UpdateHitsAndLog(gstate)
     torch.cuda.synchronize()

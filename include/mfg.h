@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define MFG_ABI_VERSION 1u
+#define MFG_ABI_VERSION 2u
 
 /* ---- status codes (replace the reference's exceptions / MCStepResult,
  *      src/Simulation/Particle.h:24-28, src/Simulation/MolflowSimGeom.cpp:219-247) ---- */
@@ -86,6 +86,21 @@ extern "C" {
 #define MFG_G_DIST_TOTAL   5
 #define MFG_G_DIST_FULLHITS 6
 #define MFG_G_N            8
+
+/* Histogram settings (HistogramParams): which of the number of bounces, the flight distance
+ * (cm) and the flight time (s) since desorption an absorption is binned by.  Bin counts: bounces
+ * bounce_max/bounce_binsize + 2 (integer division), distance and time (size_t)(max/binsize) + 1;
+ * the last bin takes every larger value. */
+#define MFG_HIST_BOUNCE   1u
+#define MFG_HIST_DISTANCE 2u
+#define MFG_HIST_TIME     4u
+typedef struct mfg_histogram_params {
+    uint32_t record;                   /* MFG_HIST_* bits */
+    uint32_t pad;
+    uint64_t bounce_binsize, bounce_max;
+    double   distance_binsize, distance_max;
+    double   time_binsize, time_max;
+} mfg_histogram_params;
 
 /*
  * Model descriptor: the fields of MolflowSimulationModel that the tracer reads
@@ -157,6 +172,10 @@ typedef struct mfg_model_desc {
     const double*  param_v;
     const uint8_t* param_log_x;        /* logXinterp [0] */
     const uint8_t* param_log_y;        /* logYinterp [0] */
+
+    /* histograms recorded at each absorption (RecordHistograms, Particle.cpp:926-975) */
+    mfg_histogram_params global_histogram;          /* sp.globalHistogramParams */
+    const mfg_histogram_params* facet_histogram;    /* sh.facetHistogramParams [n_facets] or NULL */
 } mfg_model_desc;
 
 /*
@@ -180,6 +199,9 @@ typedef struct mfg_state_layout {
     int64_t n_profile;             /* (1+M)*profile_facets*PROFILE_SIZE*3 (countEquiv, sum_v_ort, sum_1_per_ort_velocity) */
     int64_t n_direction;           /* (1+M)*direction_cells*4 (dir.x, dir.y, dir.z, count) */
     int64_t n_anglemap;            /* anglemap_cells */
+    int64_t histogram_bins;        /* bins of one moment block: the global histograms (bounce,
+                                      distance, time, those recorded), then each facet's in id order */
+    int64_t n_histogram;           /* (1+M)*histogram_bins */
 } mfg_state_layout;
 
 typedef struct mfg_state_view {
@@ -190,6 +212,7 @@ typedef struct mfg_state_view {
     double*   profile;       /* [n_profile] */
     double*   direction;     /* [n_direction] */
     uint64_t* anglemap;      /* [n_anglemap] */
+    double*   histogram;     /* [n_histogram] */
 } mfg_state_view;
 
 /* Run options (precision, RNG, launch shape). */

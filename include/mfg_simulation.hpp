@@ -44,6 +44,7 @@ struct HostState {
     std::vector<uint64_t> facet_counts;
     std::vector<double> facet_sums, texture, profile, direction;
     std::vector<uint64_t> anglemap;
+    std::vector<double> histogram;
     std::timed_mutex mutex;   // simuStateMutex
 
     void resize(const mfg_state_layout& L) {
@@ -55,10 +56,11 @@ struct HostState {
         profile.assign(size_t(L.n_profile), 0.0);
         direction.assign(size_t(L.n_direction), 0.0);
         anglemap.assign(size_t(L.n_anglemap), 0);
+        histogram.assign(size_t(L.n_histogram), 0.0);
     }
     mfg_state_view view() {
         return mfg_state_view{global.data(), facet_counts.data(), facet_sums.data(), texture.data(),
-                              profile.data(), direction.data(), anglemap.data()};
+                              profile.data(), direction.data(), anglemap.data(), histogram.data()};
     }
     // GlobalSimuState::operator+= (src/Simulation/MolflowSimGeom.cpp:452-458)
     HostState& operator+=(const HostState& o) {
@@ -69,6 +71,7 @@ struct HostState {
         for (size_t i = 0; i < profile.size(); ++i) profile[i] += o.profile[i];
         for (size_t i = 0; i < direction.size(); ++i) direction[i] += o.direction[i];
         for (size_t i = 0; i < anglemap.size(); ++i) anglemap[i] += o.anglemap[i];
+        for (size_t i = 0; i < histogram.size(); ++i) histogram[i] += o.histogram[i];
         return *this;
     }
 };

@@ -1,7 +1,7 @@
 """ctypes mirrors of the C structs declared in include/mfg.h (ABI version 1)."""
 import ctypes as C
 
-MFG_ABI_VERSION = 1
+MFG_ABI_VERSION = 2
 
 MFG_OK = 0
 MFG_ERR_INVALID_MODEL = 1
@@ -38,6 +38,23 @@ _i32 = C.POINTER(C.c_int32)
 _u8 = C.POINTER(C.c_uint8)
 _u32 = C.POINTER(C.c_uint32)
 _u64 = C.POINTER(C.c_uint64)
+
+HIST_BOUNCE, HIST_DISTANCE, HIST_TIME = 1, 2, 4
+
+
+class HistogramParams(C.Structure):
+    _fields_ = [("record", C.c_uint32), ("pad", C.c_uint32), ("bounce_binsize", C.c_uint64),
+                ("bounce_max", C.c_uint64), ("distance_binsize", C.c_double), ("distance_max", C.c_double),
+                ("time_binsize", C.c_double), ("time_max", C.c_double)]
+
+
+def histogram_sizes(h):
+    """(bounce, distance, time) bin counts of a HistogramParams-like object, 0 when not recorded."""
+    b = int(h.bounce_max) // max(int(h.bounce_binsize), 1) + 2 if h.record & HIST_BOUNCE else 0
+    d = int(h.distance_max / h.distance_binsize) + 1 if h.record & HIST_DISTANCE else 0
+    t = int(h.time_max / h.time_binsize) + 1 if h.record & HIST_TIME else 0
+    return b, d, t
+
 
 # (field name, ctypes type) in declaration order of mfg_model_desc
 MODEL_DESC_FIELDS = [
@@ -97,6 +114,8 @@ MODEL_DESC_FIELDS = [
     ("param_v", _d),
     ("param_log_x", _u8),
     ("param_log_y", _u8),
+    ("global_histogram", HistogramParams),
+    ("facet_histogram", C.POINTER(HistogramParams)),
 ]
 
 
@@ -107,7 +126,8 @@ class ModelDesc(C.Structure):
 class StateLayout(C.Structure):
     _fields_ = [(n, C.c_int64) for n in (
         "n_facets", "n_moments", "texture_cells", "profile_facets", "direction_cells", "anglemap_cells",
-        "n_global", "n_facet_counts", "n_facet_sums", "n_texture", "n_profile", "n_direction", "n_anglemap")]
+        "n_global", "n_facet_counts", "n_facet_sums", "n_texture", "n_profile", "n_direction", "n_anglemap",
+        "histogram_bins", "n_histogram")]
 
 
 class StateView(C.Structure):
@@ -119,6 +139,7 @@ class StateView(C.Structure):
         ("profile", _d),
         ("direction", _d),
         ("anglemap", _u64),
+        ("histogram", _d),
     ]
 
 

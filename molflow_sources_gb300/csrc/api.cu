@@ -71,7 +71,8 @@ struct mfg_sim {
     int* d_abort = nullptr;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    size_t n_global = TG_N, n_facet = 0, n_texture = 0, n_profile = 0, n_anglemap = 0, n_dir = 0;
+    size_t n_global = TG_N, n_facet = 0, n_texture = 0, n_profile = 0, n_anglemap = 0, n_dir = 0, n_hist = 0;
+    size_t n_lf = 0;   // low-flux equivalent counts: 2 global + facet pairs + texture cells + profile bins
     std::vector<uint64_t> particles_started;   // per instance
     unsigned char* h_run = nullptr;            // pinned RunDesc + prefix + first (staging)
     unsigned char* d_run = nullptr;
@@ -197,6 +198,7 @@ static int sim_upload(mfg_sim* s) {
     UP(h.par_v, par_v);
     UP(h.par_logx, par_logx);
     UP(h.par_logy, par_logy);
+    UP(h.fhist, fhist);
 #undef UP
     M.src_total = h.src_total;
     M.latest = h.latest;
@@ -214,7 +216,12 @@ static int sim_upload(mfg_sim* s) {
     M.direction_cells = h.layout.direction_cells;
     M.scene_scale = h.scene_scale;
     M.has_transparent = h.has_transparent;
-    M.pad2 = 0;
+    M.has_ext = h.has_ext;
+    M.low_flux = h.low_flux;
+    M.pad4 = 0;
+    M.low_flux_cutoff = h.low_flux_cutoff;
+    M.ghist = h.ghist;
+    M.hist_bins = h.layout.histogram_bins;
     {
         std::vector<int32_t> sb, sc;
         std::vector<double> st;
@@ -238,6 +245,7 @@ static int sim_upload(mfg_sim* s) {
     s->n_profile = B * size_t(h.layout.profile_facets) * MFG_PROFILE_SIZE * TT_N;
     s->n_anglemap = size_t(h.layout.anglemap_cells);
     s->n_dir = B * size_t(h.layout.direction_cells);
+    s->n_hist = B * size_t(h.layout.histogram_bins);
     auto alloc = [&](unsigned long long** p, size_t n) -> int {
         *p = nullptr;
         if (!n) return MFG_OK;
@@ -254,6 +262,18 @@ static int sim_upload(mfg_sim* s) {
     if ((rc = alloc(&s->dt.anglemap, s->n_anglemap))) return rc;
     if ((rc = alloc(&s->dt.dir_count, s->n_dir))) return rc;
     if ((rc = alloc(reinterpret_cast<unsigned long long**>(&s->dt.direction), 3 * s->n_dir))) return rc;
+    if ((rc = alloc(reinterpret_cast<unsigned long long**>(&s->dt.histogram), s->n_hist))) return rc;
+    if (h.low_flux) {
+        const size_t nfc = B * size_t(h.nf) * 2, ntx = B * size_t(h.layout.texture_cells),
+                     npr = B * size_t(h.layout.profile_facets) * MFG_PROFILE_SIZE;
+        s->n_lf = 2 + nfc + ntx + npr;
+        double* base = nullptr;
+        if ((rc = alloc(reinterpret_cast<unsigned long long**>(&base), s->n_lf))) return rc;
+        s->dt.lf_glob = base;
+        s->dt.lf_facet = base + 2;
+        s->dt.lf_tex = base + 2 + nfc;
+        s->dt.lf_prof = base + 2 + nfc + ntx;
+    }
     if ((rc = alloc(&s->d_counter, 1))) return rc;
     return MFG_OK;
 }
@@ -272,6 +292,8 @@ int mfg_reset(mfg_sim* s) {
         CK(cudaMemsetAsync(s->dt.dir_count, 0, s->n_dir * 8, s->stream));
         CK(cudaMemsetAsync(s->dt.direction, 0, s->n_dir * 24, s->stream));
     }
+    if (s->n_hist) CK(cudaMemsetAsync(s->dt.histogram, 0, s->n_hist * 8, s->stream));
+    if (s->n_lf) CK(cudaMemsetAsync(s->dt.lf_glob, 0, s->n_lf * 8, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return MFG_OK;
 }
@@ -415,7 +437,7 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     } else if (o.precision == MFG_PREC_FP32R) {
         variant = (o.blocks_per_sm == 3) ? 3 : (o.blocks_per_sm == 4 ? 4 : 2);
     }
-    if (h.has_transparent) variant = (variant == 3 || variant == 4) ? 102 : variant + 100;
+    if (h.has_ext) variant = (variant == 3 || variant == 4) ? 102 : variant + 100;
     const void* fn = kernel_of(variant);
     CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn)));
     int per_sm = 0;
@@ -665,6 +687,34 @@ static int fetch_range(mfg_sim* s, mfg_state_view* v, int fb, int nf, int64_t tb
             }
     if (v->anglemap)
         for (int64_t c = 0; c < na; ++c) v->anglemap[c] = am[ab + c];
+    if (v->histogram && s->n_hist && whole)
+        CK(cudaMemcpy(v->histogram, s->dt.histogram, s->n_hist * 8, cudaMemcpyDeviceToHost));
+    if (s->n_lf && whole) {
+        // low-flux mode: equivalent (weighted) hits, absorptions and texture / profile counts
+        std::vector<double> lf(s->n_lf);
+        CK(cudaMemcpy(lf.data(), s->dt.lf_glob, s->n_lf * 8, cudaMemcpyDeviceToHost));
+        const double* lfc = lf.data() + 2;
+        const double* lft = lfc + B * NF * 2;
+        const double* lfp = lft + B * NT;
+        if (v->global) {
+            v->global[MFG_G_NBHITEQUIV] = lf[0];
+            v->global[MFG_G_NBABSEQUIV] = lf[1];
+        }
+        if (v->facet_sums)
+            for (size_t m = 0; m < B; ++m)
+                for (int i = 0; i < nf; ++i) {
+                    double* o = v->facet_sums + (m * size_t(nf) + i) * MFG_FS_N;
+                    o[MFG_FS_NBHITEQUIV] = lfc[(m * NF + fb + i) * 2];
+                    o[MFG_FS_NBABSEQUIV] = lfc[(m * NF + fb + i) * 2 + 1];
+                }
+        if (v->texture)
+            for (size_t m = 0; m < B; ++m)
+                for (int64_t c = 0; c < nt; ++c) v->texture[(m * size_t(nt) + c) * 3] = lft[m * NT + tb + c];
+        if (v->profile)
+            for (size_t m = 0; m < B; ++m)
+                for (int64_t c = 0; c < np * MFG_PROFILE_SIZE; ++c)
+                    v->profile[(m * size_t(np) * MFG_PROFILE_SIZE + c) * 3] = lfp[m * NP + pb * MFG_PROFILE_SIZE + c];
+    }
     if (v->direction) {
         // direction cells of facets [fb, fb+nf): contiguous range starting at the first one's offset
         int64_t d0 = -1, nd = 0;

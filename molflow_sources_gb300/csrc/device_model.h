@@ -52,6 +52,7 @@ struct __align__(16) PolyF { float cu, cv, su, sv, rin2, rout2; int32_t vstart, 
 #define FF_PROFILE     64u
 #define FF_DIFFUSE_ONLY 128u
 #define FF_FAST_REFL   256u   // diffuse, full accommodation, Maxwell speeds, no sojourn, constant temperature
+#define FF_LINK        512u   // structure link: the particle passes into structure FacetInfo2::link
 
 // Per-facet physics record (FP64, 128 B).
 struct __align__(16) FacetPhysD {
@@ -79,7 +80,7 @@ struct __align__(16) FacetInfo2 {
     int32_t am_phi, am_lo, am_hi, dir_off;   // dir_off: direction-cell offset, -1 when not recorded
     double am_limit, max_speed, desorb_exp, temperature;
     double opacity;
-    int32_t opac_param, pad;
+    int32_t opac_param, link;   // link: destination structure of a link facet, -1 none
 };
 
 // Device-resident tallies.  Fixed-point scales: velocities (m/s) * 2^20,
@@ -133,6 +134,16 @@ struct __align__(16) FacetInfo2 {
 #define KS_STACK 8ull
 #define KS_TRANSP 16ull   // more transparent passes on one ray than the pass list holds
 
+// one histogram set (RecordHistograms, Particle.cpp:926-975): bin sizes, bin counts (0 = not
+// recorded) and offset of the set in a moment block (-1 = none)
+struct HistDev {
+    uint32_t record;
+    int32_t off;
+    uint64_t bounce_bin;
+    double dist_bin, time_bin;
+    int32_t nb, nd, nt, pad;
+};
+
 struct DevModel {
     int32_t nf, nstruct;
     int32_t n_src, nm;
@@ -179,7 +190,14 @@ struct DevModel {
     int64_t profile_facets;
     int64_t anglemap_cells;
     int64_t direction_cells;
-    int32_t has_transparent, pad2;   // some facet has opacity < 1 or an opacity parameter
+    int32_t has_transparent;     // some facet has opacity < 1 or an opacity parameter
+    int32_t has_ext;             // traced by the extended kernel variants (transparency, histograms, low flux)
+    int32_t low_flux, pad4;      // low-flux mode (otfParams.lowFluxMode) and its cutoff weight
+    double low_flux_cutoff;
+    // histograms recorded at absorptions: global set and per-facet sets, hist_bins per moment block
+    HistDev ghist;
+    const HistDev* fhist;        // [nf] or null
+    int64_t hist_bins;
     double scene_scale;          // max |coordinate| of the scene (for FP32 tolerances)
     // instances of a batch (one for a plain model): source-table range and total weight
     int32_t n_inst, pad1;
@@ -189,6 +207,12 @@ struct DevModel {
 };
 
 struct DevTally {
+    double* histogram;               // (1+M) * hist_bins (FP64 atomics)
+    // low-flux mode: weighted ("equivalent") counts, FP64 atomics; null otherwise
+    double* lf_glob;                 // [2] nbHitEquiv, nbAbsEquiv
+    double* lf_facet;                // (1+M) * nf * 2 (nbHitEquiv, nbAbsEquiv)
+    double* lf_tex;                  // (1+M) * texture_cells (countEquiv)
+    double* lf_prof;                 // (1+M) * profile_facets * 100 (countEquiv)
     unsigned long long* global;      // TG_N
     unsigned long long* facet;       // (1+M) * nf * TF_N
     unsigned long long* texture;     // (1+M) * texture_cells * TT_N

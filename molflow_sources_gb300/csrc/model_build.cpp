@@ -400,8 +400,27 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     m.low_flux = d->low_flux_mode;
     m.low_flux_cutoff = d->low_flux_cutoff;
     if (!(m.gas_mass > 0)) { err = "gas mass must be positive"; return MFG_ERR_INVALID_MODEL; }
+    {
+        const mfg_histogram_params& hp = d->global_histogram;
+        if (((hp.record & MFG_HIST_DISTANCE) && !(hp.distance_binsize > 0 && hp.distance_max >= 0 && hp.distance_max / hp.distance_binsize < 1e8)) ||
+            ((hp.record & MFG_HIST_TIME) && !(hp.time_binsize > 0 && hp.time_max >= 0 && hp.time_max / hp.time_binsize < 1e8)) ||
+            ((hp.record & MFG_HIST_BOUNCE) && hp.bounce_max / (hp.bounce_binsize ? hp.bounce_binsize : 1) > 100000000ull)) {
+            err = "bad global histogram settings";
+            return MFG_ERR_INVALID_MODEL;
+        }
+    }
     for (int i = 0; i < nf; ++i) {
         if (m.structure[i] < -1 || m.structure[i] >= m.nstruct) { err = "structure index out of range on facet " + std::to_string(i + 1); return MFG_ERR_INVALID_MODEL; }
+        if (m.link[i] < 0 || m.link[i] > m.nstruct) { err = "structure link destination out of range on facet " + std::to_string(i + 1); return MFG_ERR_INVALID_MODEL; }
+        if (d->facet_histogram) {
+            const mfg_histogram_params& hp = d->facet_histogram[i];
+            if (((hp.record & MFG_HIST_DISTANCE) && !(hp.distance_binsize > 0 && hp.distance_max >= 0 && hp.distance_max / hp.distance_binsize < 1e8)) ||
+                ((hp.record & MFG_HIST_TIME) && !(hp.time_binsize > 0 && hp.time_max >= 0 && hp.time_max / hp.time_binsize < 1e8)) ||
+                ((hp.record & MFG_HIST_BOUNCE) && hp.bounce_max / (hp.bounce_binsize ? hp.bounce_binsize : 1) > 100000000ull)) {
+                err = "bad histogram settings on facet " + std::to_string(i + 1);
+                return MFG_ERR_INVALID_MODEL;
+            }
+        }
         if (!(m.temperature[i] > 0)) { err = "temperature must be positive on facet " + std::to_string(i + 1); return MFG_ERR_INVALID_MODEL; }
     }
 
@@ -488,10 +507,8 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     auto unsupported = [&](const std::string& why) {
         if (m.gpu_supported) { m.gpu_supported = false; m.gpu_unsupported_reason = why; }
     };
-    if (m.low_flux) unsupported("low flux mode");
     for (int i = 0; i < nf; ++i) {
         std::string f = "facet " + std::to_string(i + 1) + ": ";
-        if (m.link[i]) unsupported(f + "structure link");
         if (m.teleport[i]) unsupported(f + "teleport");
         if (m.moving[i]) unsupported(f + "moving facet");
         if (m.desorb_type[i] == MFG_DES_ANGLEMAP) unsupported(f + "angle-map desorption");
@@ -529,6 +546,33 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     L.n_profile = B * L.profile_facets * MFG_PROFILE_SIZE * 3;
     L.n_direction = B * L.direction_cells * 4;
     L.n_anglemap = L.anglemap_cells;
+    // histograms: global set at offset 0, then each recording facet's (bounce, distance, time);
+    // bin counts restated from the sizes the reference stores with its histograms
+    auto hist_of = [](const mfg_histogram_params& p, HistDev& h) {
+        h = HistDev{};
+        h.off = -1;
+        h.record = p.record;
+        if (!p.record) return;
+        h.bounce_bin = p.bounce_binsize ? p.bounce_binsize : 1;
+        h.dist_bin = p.distance_binsize;
+        h.time_bin = p.time_binsize;
+        if (p.record & MFG_HIST_BOUNCE) h.nb = int32_t(p.bounce_max / h.bounce_bin + 2);
+        if (p.record & MFG_HIST_DISTANCE) h.nd = int32_t(size_t(p.distance_max / p.distance_binsize) + 1);
+        if (p.record & MFG_HIST_TIME) h.nt = int32_t(size_t(p.time_max / p.time_binsize) + 1);
+    };
+    int64_t hb = 0;
+    hist_of(d->global_histogram, m.ghist);
+    if (m.ghist.record) { m.ghist.off = 0; hb = m.ghist.nb + m.ghist.nd + m.ghist.nt; }
+    m.fhist.clear();
+    if (d->facet_histogram) {
+        m.fhist.resize(nf);
+        for (int i = 0; i < nf; ++i) {
+            hist_of(d->facet_histogram[i], m.fhist[i]);
+            if (m.fhist[i].record) { m.fhist[i].off = int32_t(hb); hb += m.fhist[i].nb + m.fhist[i].nd + m.fhist[i].nt; }
+        }
+    }
+    L.histogram_bins = hb;
+    L.n_histogram = B * hb;
     m.tex_inc.assign(size_t(L.texture_cells), 0.0);
     for (int i = 0; i < nf; ++i) {
         if (m.tex_off[i] < 0) continue;
@@ -746,7 +790,8 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
         in.flags = (m.two_sided[i] ? FF_TWO_SIDED : 0) | (m.tex_off[i] >= 0 ? FF_TEXTURED : 0) |
                    (m.p_stick[i] >= 0 ? FF_STICK_PARAM : 0) | (m.p_temp[i] >= 0 ? FF_TEMP_PARAM : 0) |
                    (m.sojourn[i] ? FF_SOJOURN : 0) | (m.ang_off[i] >= 0 ? FF_ANGLEMAP : 0) |
-                   (m.prof_idx[i] >= 0 ? FF_PROFILE : 0) | (m.diffuse[i] > 0.999999 ? FF_DIFFUSE_ONLY : 0);
+                   (m.prof_idx[i] >= 0 ? FF_PROFILE : 0) | (m.diffuse[i] > 0.999999 ? FF_DIFFUSE_ONLY : 0) |
+                   (m.link[i] ? FF_LINK : 0);
         if (m.diffuse[i] > 0.999999 && m.accommodation[i] > 0.9999 && m.use_maxwell && !m.sojourn[i] && m.p_temp[i] < 0)
             in.flags |= FF_FAST_REFL;
         in.count = m.count[i];
@@ -767,7 +812,7 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
         i2.dir_off = int32_t(m.dir_off[i]);
         i2.opacity = m.opacity[i];
         i2.opac_param = m.p_opac[i];
-        i2.pad = 0;
+        i2.link = m.link[i] ? m.link[i] - 1 : -1;
         i2.am_limit = m.am_limit[i];
         i2.max_speed = m.max_speed[i];
         i2.desorb_exp = m.desorb_exp[i];
@@ -781,6 +826,7 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     inst.src_total = m.src_total;
     inst.layout = m.layout;
     m.instances.assign(1, inst);
+    m.has_ext = m.has_transparent || m.layout.histogram_bins > 0 || m.low_flux;
     return MFG_OK;
 }
 
@@ -795,6 +841,10 @@ int merge_host_models(const std::vector<const HostModel*>& parts, HostModel& out
             err = "batched models must share gas, speed law, flow mode, decay and moments";
             return MFG_ERR_INVALID_ARGUMENT;
         }
+    }
+    for (const HostModel* p : parts) {
+        if (p->layout.histogram_bins > 0) { err = "histograms are not recorded in batched instances"; return MFG_ERR_UNSUPPORTED_FEATURE; }
+        if (p->low_flux) { err = "low-flux mode is not traced in batched instances"; return MFG_ERR_UNSUPPORTED_FEATURE; }
     }
     out = HostModel();
     out.nm = p0.nm;
@@ -854,6 +904,7 @@ int merge_host_models(const std::vector<const HostModel*>& parts, HostModel& out
             if (f2.stick_param >= 0) f2.stick_param += par_base;
             if (f2.temp_param >= 0) f2.temp_param += par_base;
             if (f2.opac_param >= 0) f2.opac_param += par_base;
+            if (f2.link >= 0) f2.link += in.struct_base;
             out.info2.push_back(f2);
         }
         out.centers.insert(out.centers.end(), p.centers.begin(), p.centers.end());
@@ -888,6 +939,7 @@ int merge_host_models(const std::vector<const HostModel*>& parts, HostModel& out
         out.bvh_leaves += p.bvh_leaves;
         out.scene_scale = std::max(out.scene_scale, p.scene_scale);
         out.has_transparent |= p.has_transparent;
+        out.has_ext |= p.has_ext;
         out.instances.push_back(in);
     }
     mfg_state_layout& L = out.layout;

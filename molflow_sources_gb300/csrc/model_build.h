@@ -76,6 +76,9 @@ struct HostModel {
     std::vector<double> centers;
     double scene_scale = 1;
     int has_transparent = 0;
+    int has_ext = 0;                      // needs the extended kernel variants
+    HistDev ghist{};                      // histograms (off -1: none)
+    std::vector<HistDev> fhist;           // per facet, empty when no facet records
     bool gpu_supported = true;
     std::string gpu_unsupported_reason;
     // instances (one for a plain model; several after merge_host_models)

@@ -176,41 +176,73 @@ struct Real_<true> {
 struct ParticleState {
     double ox, oy, oz;
     double time, decay_at;
-    uint64_t bounces;
+    uint64_t bounces;      // trace steps since desorption (reflections and link passes)
     int last, structure;
+    // extended variants: flight distance (cm), desorption time and reflections since desorption,
+    // and the low-flux weight (oriRatio)
+    double dist, gen_time;
+    uint64_t refl;
+    double ori;
 };
 
 // ProfileFacet (Particle.cpp:1026-1085); profiles are tallied in global memory
-__device__ __noinline__ void profile_add(const DevModel& M, const DevTally& T, int f, int m, bool count_hit,
-                                            unsigned long long vfac, unsigned long long ofac, double cosn, double vel,
-                                            double u, double v, unsigned long long q1, unsigned long long q2) {
-    const FacetInfo& In = M.info[f];
-    int pt = In.profile_type;
-    int pos = -1;
-    bool full = false;
+// profile bin of a hit: -1 when outside; `full` for U/V profiles, which also take the sums
+__device__ __forceinline__ int profile_bin(const DevModel& M, int f, bool count_hit, double cosn, double vel, double u,
+                                           double v, bool& full) {
+    const int pt = M.info[f].profile_type;
+    full = false;
     if (count_hit && pt == MFG_PROFILE_ANGULAR) {
         double th = acos(fmin(cosn, 1.0));
-        pos = (int)(th / (kPi / 2) * (double)MFG_PROFILE_SIZE);
-        pos = min(max(pos, 0), MFG_PROFILE_SIZE - 1);
+        int pos = (int)(th / (kPi / 2) * (double)MFG_PROFILE_SIZE);
+        return min(max(pos, 0), MFG_PROFILE_SIZE - 1);
     } else if (pt == MFG_PROFILE_U || pt == MFG_PROFILE_V) {
         double x = (pt == MFG_PROFILE_U ? u : v) * (double)MFG_PROFILE_SIZE;
-        if (!(x >= 0.0) || x >= (double)MFG_PROFILE_SIZE) return;
-        pos = (int)x;
+        if (!(x >= 0.0) || x >= (double)MFG_PROFILE_SIZE) return -1;
         full = true;
+        return (int)x;
     } else if (count_hit && pt >= MFG_PROFILE_VELOCITY && pt <= MFG_PROFILE_TAN_VELOCITY) {
         double dd = (pt == MFG_PROFILE_VELOCITY) ? 1.0 : (pt == MFG_PROFILE_ORT_VELOCITY ? cosn : sqrt(fmax(0.0, 1.0 - cosn * cosn)));
         double x = dd * vel / M.info2[f].max_speed * (double)MFG_PROFILE_SIZE;
-        if (!(x >= 0.0) || x >= (double)MFG_PROFILE_SIZE) return;
-        pos = (int)x;
-    } else {
-        return;
+        if (!(x >= 0.0) || x >= (double)MFG_PROFILE_SIZE) return -1;
+        return (int)x;
     }
-    unsigned long long* g = T.profile + (((size_t)m * M.profile_facets + In.prof_idx) * MFG_PROFILE_SIZE + pos) * TT_N;
+    return -1;
+}
+__device__ __noinline__ void profile_add(const DevModel& M, const DevTally& T, int f, int m, bool count_hit,
+                                            unsigned long long vfac, unsigned long long ofac, double cosn, double vel,
+                                            double u, double v, unsigned long long q1, unsigned long long q2) {
+    bool full;
+    const int pos = profile_bin(M, f, count_hit, cosn, vel, u, v, full);
+    if (pos < 0) return;
+    unsigned long long* g = T.profile + (((size_t)m * M.profile_facets + M.info[f].prof_idx) * MFG_PROFILE_SIZE + pos) * TT_N;
     if (count_hit) atomicAdd(g + TT_COUNT, 1ull);
     if (full) {
         add128(g + TT_S1OV, vfac * q1);
         add128(g + TT_SVORT, ofac * q2);
     }
+}
+
+// Low-flux mode (Particle.cpp:338-356): the counters keep Monte Carlo counts; the weighted
+// ("equivalent") counts of one tally event go to FP64 arrays, in moment 0 and every window
+// holding `time`: facet nbHitEquiv/nbAbsEquiv (he, ae), texture countEquiv (cell, cw), profile
+// countEquiv (pw), and the global nbHitEquiv/nbAbsEquiv (ghe, gae)
+__device__ __noinline__ void lf_counts(const DevModel& M, const DevTally& T, int f, double time, double he, double ae,
+                                       int cell, double cw, double pw, double cosn, double vel, double u, double v,
+                                       double ghe, double gae) {
+    if (ghe != 0.0) atomicAdd(T.lf_glob, ghe);
+    if (gae != 0.0) atomicAdd(T.lf_glob + 1, gae);
+    bool full = false;
+    const int pos = (pw != 0.0 && (M.info[f].flags & FF_PROFILE)) ? profile_bin(M, f, true, cosn, vel, u, v, full) : -1;
+    auto add = [&](int m) {
+        double* fc = T.lf_facet + ((size_t)m * M.nf + f) * 2;
+        if (he != 0.0) atomicAdd(fc, he);
+        if (ae != 0.0) atomicAdd(fc + 1, ae);
+        if (cell >= 0 && cw != 0.0) atomicAdd(T.lf_tex + (size_t)m * M.texture_cells + cell, cw);
+        if (pos >= 0)
+            atomicAdd(T.lf_prof + ((size_t)m * M.profile_facets + M.info[f].prof_idx) * MFG_PROFILE_SIZE + pos, pw);
+    };
+    add(0);
+    for_moments(M, time, add);
 }
 
 // RecordAngleMap (Particle.cpp:1104-1136): incident (theta, phi) histogram, not time resolved
@@ -366,24 +398,67 @@ __device__ __noinline__ void direction_add(const DevModel& M, const DevTally& T,
 __device__ __noinline__ void tally_moments(const DevModel& M, const DevTally& T, const BlockTally& B, int f, double time,
                                            unsigned long long des, unsigned long long hits, unsigned long long abs_,
                                            unsigned long long s1ov, unsigned long long svort, unsigned long long s1v,
-                                           int cell, unsigned long long cell_count, bool count_hit,
+                                           int cell, unsigned long long cell_count, unsigned long long cell_s1ov,
+                                           unsigned long long cell_svort, bool count_hit,
                                            unsigned long long vf, unsigned long long of, double cosn, double vel,
                                            double u, double v, unsigned long long q1, unsigned long long q2) {
     const bool prof = (M.info[f].flags & FF_PROFILE) != 0;
     for_moments(M, time, [&](int m) {
         facet_add(M, T, B, f, m, hits, des, abs_, s1ov, svort, s1v);
-        if (cell >= 0) cell_add(T.texture + ((size_t)m * M.texture_cells + cell) * TT_N, cell_count, s1ov, svort);
+        if (cell >= 0) cell_add(T.texture + ((size_t)m * M.texture_cells + cell) * TT_N, cell_count, cell_s1ov, cell_svort);
         if (prof) profile_add(M, T, f, m, count_hit, vf, of, cosn, vel, u, v, q1, q2);
     });
+}
+
+// RecordHistograms (Particle.cpp:926-975): bounces, flight distance and flight time of an
+// absorbed particle, in moment 0 and every moment window holding the absorption time
+__device__ __forceinline__ void hist_add(const HistDev& h, double* block, uint64_t refl, double dist, double flight,
+                                         double w) {
+    if (h.off < 0) return;
+    double* b = block + h.off;
+    if (h.nb) {
+        uint64_t k = refl / h.bounce_bin;
+        if (k > (uint64_t)(h.nb - 1)) k = (uint64_t)(h.nb - 1);
+        atomicAdd(b + k, w);
+        b += h.nb;
+    }
+    if (h.nd) {
+        unsigned long long k = (unsigned long long)(dist / h.dist_bin);
+        if (k > (unsigned long long)(h.nd - 1)) k = (unsigned long long)(h.nd - 1);
+        atomicAdd(b + k, w);
+        b += h.nd;
+    }
+    if (h.nt) {
+        unsigned long long k = (unsigned long long)(flight / h.time_bin);
+        if (k > (unsigned long long)(h.nt - 1)) k = (unsigned long long)(h.nt - 1);
+        atomicAdd(b + k, w);
+    }
+}
+__device__ __noinline__ void record_histograms(const DevModel& M, const DevTally& T, int f, double time, uint64_t refl,
+                                               double dist, double gen_time, double w) {
+    const double flight = time - gen_time;
+    auto add = [&](int m) {
+        double* block = T.histogram + (size_t)m * M.hist_bins;
+        hist_add(M.ghist, block, refl, dist, flight, w);
+        if (M.fhist) hist_add(M.fhist[f], block, refl, dist, flight, w);
+    };
+    add(0);
+    for_moments(M, time, add);
 }
 
 // RegisterTransparentPass (Particle.cpp:1232-1257): crossing a transparent facet counts a hit
 // whose 1/v_ort and v_ort sums are doubled (the particle crosses, it does not turn back), on
 // the facet, its texture (countTrans), profile, direction cells and angle map, in the moment
 // windows holding the crossing time.  Returns v_ort.
+//
+// A structure link (PerformBounce, Particle.cpp:698-724) is tallied the same way at t = 0, except
+// that the facet counter gets no velocity sums (`link`).
+// In low-flux mode the sums carry the particle's weight `w` and the equivalent counts go to the
+// low-flux arrays.
 template <bool kFP32, class R>
 __device__ __noinline__ double transparent_pass(const DevModel& M, const DevTally& T, const BlockTally& B, int f,
-                                                R t, R u, R v, double time, R vel, R dx, R dy, R dz) {
+                                                R t, R u, R v, double time, R vel, R dx, R dy, R dz,
+                                                bool link = false, double w = 1.0) {
     const FacetInfo& In = M.info[f];
     R cosn;
     double tp;
@@ -395,20 +470,23 @@ __device__ __noinline__ double transparent_pass(const DevModel& M, const DevTall
         tp = time + (double)t / 100.0 / (double)vel;
     }
     R ort = vel * cosn;
-    unsigned long long q1 = kFP32 ? qf(1.0f / (float)ort, (float)MFG_SCALE_INV) : qd(1.0 / (double)ort, MFG_SCALE_INV);
-    unsigned long long q2 = kFP32 ? qf((float)ort, (float)MFG_SCALE_V) : qd((double)ort, MFG_SCALE_V);
-    unsigned long long q3 = kFP32 ? qf(1.0f / (float)vel, (float)MFG_SCALE_INV) : qd(1.0 / (double)vel, MFG_SCALE_INV);
-    facet_add(M, T, B, f, 0, 1, 0, 0, 2 * q1, 2 * q2, q3);
+    unsigned long long q1 = kFP32 ? qf((float)w * (1.0f / (float)ort), (float)MFG_SCALE_INV) : qd(w * (1.0 / (double)ort), MFG_SCALE_INV);
+    unsigned long long q2 = kFP32 ? qf((float)w * (float)ort, (float)MFG_SCALE_V) : qd(w * (double)ort, MFG_SCALE_V);
+    unsigned long long q3 = kFP32 ? qf((float)w * (1.0f / (float)vel), (float)MFG_SCALE_INV) : qd(w * (1.0 / (double)vel), MFG_SCALE_INV);
+    const unsigned long long f1 = link ? 0ull : 2 * q1, f2 = link ? 0ull : 2 * q2;
+    facet_add(M, T, B, f, 0, 1, 0, 0, f1, f2, q3);
     const int cell = (In.tex_off >= 0 && (In.count & MFG_COUNT_TRANS)) ? texture_cell<kFP32>(M, f, u, v) : -1;
     if (cell >= 0) cell_add(T.texture + (size_t)cell * TT_N, 1, 2 * q1, 2 * q2);
     if (In.count & MFG_COUNT_DIR)
-        direction_add(M, T, f, (double)u, (double)v, tp, (double)dx * (double)vel, (double)dy * (double)vel,
-                      (double)dz * (double)vel);
+        direction_add(M, T, f, (double)u, (double)v, tp, w * (double)dx * (double)vel, w * (double)dy * (double)vel,
+                      w * (double)dz * (double)vel);
+    if (T.lf_glob)
+        lf_counts(M, T, f, tp, w, 0.0, cell, w, w, (double)cosn, (double)vel, (double)u, (double)v, link ? w : 0.0, 0.0);
     if (In.flags & FF_PROFILE) profile_add(M, T, f, 0, true, 2, 2, (double)cosn, (double)vel, (double)u, (double)v, q1, q2);
     if (In.flags & FF_ANGLEMAP) anglemap_add(M, T, f, (double)dx, (double)dy, (double)dz);
     if (M.nm)
-        tally_moments(M, T, B, f, tp, 0, 1, 0, 2 * q1, 2 * q2, q3, cell, 1, true, 2, 2, (double)cosn, (double)vel,
-                      (double)u, (double)v, q1, q2);
+        tally_moments(M, T, B, f, tp, 0, 1, 0, f1, f2, q3, cell, 1, 2 * q1, 2 * q2, true, 2, 2, (double)cosn,
+                      (double)vel, (double)u, (double)v, q1, q2);
     return (double)ort;
 }
 
@@ -477,7 +555,9 @@ struct NoTranspList {
     static constexpr int n = 0;
 };
 
-template <bool kFP32, int kMinBlocks, bool kSens = false, bool kTr = false>
+// kExt: variant for models with transparent facets or histograms (pass list, flight distance,
+// desorption time and reflection count per particle)
+template <bool kFP32, int kMinBlocks, bool kSens = false, bool kExt = false>
 __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_constant__ DevModel M, DevTally T, LaunchCtl C) {
     typedef typename Real_<kFP32>::T R;
     extern __shared__ unsigned long long smem[];
@@ -518,6 +598,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
     R pu = 0, pv = 0;         // (u,v) on the current facet (facetHitDetails)
     bool active = true;       // lane still has particles to trace
     bool need_new = true;     // lane must desorb a new particle
+    bool relink = false;      // lane crossed a structure link: trace on without a new direction
     // incoming half of the last reflection, added together with the outgoing half (moment 0)
     unsigned long long pend_s1ov = 0, pend_svort = 0, pend_s1v = 0;
     int pend_cell = -1;
@@ -586,110 +667,127 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
         //      direction and tally code; only short prologues differ.  Random numbers are drawn in
         //      the reference's order: desorption = source, [reverse], time, speed, [decay], (u,v)..., theta,
         //      phi (Particle.cpp:418-625); reflection = speed, [sojourn], [type], theta, phi (:769-802).
-        const bool des = want;
-        int fo, law;              // law: 0 cosine, 1 uniform, 2 cos^N, 3 general reflection
-        bool flip = false;
-        R lexp = 0;
-        if (des) {
-            int inst = 0;
-            if (n_inst > 1) {
-                int a = 0, b = n_inst;   // last instance whose prefix <= id
-                while (b - a > 1) { int mid = (a + b) >> 1; if (C.inst_prefix[mid] <= P.bounces) a = mid; else b = mid; }
-                inst = a;
-            }
-            rng.start(C.inst_first[inst] + (P.bounces - C.inst_prefix[inst]), (uint32_t)inst);
-            // source facet by cumulative outgassing (Particle.cpp:418-464)
-            const int sbase = M.inst_src_base[inst], scount = M.inst_src_count[inst];
-            double sr = (double)rng.next() * M.inst_src_total[inst];
-            int lo = 0, hi = scount;
-            while (lo < hi) { int mid = (lo + hi) >> 1; if (M.src_cdf[sbase + mid] > sr) hi = mid; else lo = mid + 1; }
-            if (lo >= scount) lo = scount - 1;
-            lo += sbase;
-            fo = M.src_facet[lo];
-            const FacetInfo2& I2 = M.info2[fo];
-            if (M.info[fo].flags & FF_TWO_SIDED) flip = (double)rng.next() > 0.5;
-            int idt = M.src_id[lo];
-            if (idt >= 0) P.time = desorption_time(M, idt, (double)rng.next());
-            else P.time = (double)rng.next() * M.latest;
-            P.structure = I2.structure;
-            P.bounces = 0;
-            if (kSens) {
-                ntraj = 0;
-                src_idx = C.sens.src_of_facet[fo];
-                if (src_idx >= 0) atomicAdd(C.sens.src_count + src_idx, 1ull);
-            }
-            law = I2.desorb_type == MFG_DES_UNIFORM ? 1 : (I2.desorb_type == MFG_DES_COSINE_N ? 2 : 0);
-            lexp = (R)I2.desorb_exp;
-            if (!M.use_maxwell) law |= 4;   // fixed speed 145.469 sqrt(T/m) (Particle.cpp:483)
-        } else {
-            fo = P.last;
-            if (M.info[fo].flags & FF_TWO_SIDED) {
-                if (kFP32) {
-                    const FacetPhysF& Pf = M.phys_f[fo];
-                    flip = (dx * Pf.N[0] + dy * Pf.N[1] + dz * Pf.N[2]) > 0.0f;
-                } else {
-                    const FacetIsectD& Rf = M.isect_d[fo];
-                    flip = ((double)dx * Rf.v[0] + (double)dy * Rf.v[1] + (double)dz * Rf.v[2]) > 0.0;
-                }
-            }
-            law = (M.info[fo].flags & FF_FAST_REFL) ? 0 : 3;
-        }
-        // speed: Maxwell at the facet temperature (desorption and full-accommodation reflection)
-        if (law < 3) {
-            if (kFP32) vel = (R)(M.phys_f[fo].sqrtT * interp_x_f((float)rng.next(), s_cdf_vf, s_cdf_pf, MFG_MAXWELL_N));
-            else vel = (R)(M.phys_d[fo].sqrtT * interp_x_d((double)rng.next(), s_cdf_v, s_cdf_p, MFG_MAXWELL_N));
-        } else if (law & 4) {
-            vel = (R)(145.469 * sqrt(M.info2[fo].temperature / M.gas_mass));
-            law &= 3;
-        }
-        if (des) {
-            P.decay_at = M.enable_decay ? P.time - 1.44269 * M.half_life * log(1.0 - (double)rng.next()) : 1e100;
-            // start point: rejection in the (u,v) rectangle, at most 1000 tries (Particle.cpp:513-570)
-            start_point<kFP32>(M, fo, rng, P.ox, P.oy, P.oz, pu, pv);
-            P.last = fo;
-        }
-        if (law == 3) {
-            reflect_general<kFP32>(M, fo, flip, rng, P.time, vel, dx, dy, dz, s_cdf_v, s_cdf_p, s_cdf_vf, s_cdf_pf);
-        } else {
-            R r1 = (R)rng.next(), r2 = (R)rng.next();
-            R ct = law == 1 ? r1 : (law == 2 ? (R)pow((double)r1, 1.0 / ((double)lexp + 1.0)) : (R)sqrt(r1));
-            polar_dir<kFP32>(M, fo, ct, r2, flip, dx, dy, dz);
-        }
-        {
-            // outgoing tallies; a reflection's incoming half (pending) is added with them (moment 0)
-            const FacetInfo& In = M.info[fo];
-            R cosn;
-            if (kFP32) cosn = fabsf(dx * M.phys_f[fo].N[0] + dy * M.phys_f[fo].N[1] + dz * M.phys_f[fo].N[2]);
-            else cosn = (R)fabs((double)dx * M.isect_d[fo].v[0] + (double)dy * M.isect_d[fo].v[1] + (double)dz * M.isect_d[fo].v[2]);
-            R ort = vel * cosn;
-            unsigned long long q1 = kFP32 ? qf(1.0f / (float)ort, (float)MFG_SCALE_INV) : qd(1.0 / (double)ort, MFG_SCALE_INV);
-            unsigned long long q2 = kFP32 ? qf((float)ort, (float)MFG_SCALE_V) : qd((double)ort, MFG_SCALE_V);
-            unsigned long long q3 = 0;
-            int cell = pend_cell;
+        if (!relink) {
+            const bool des = want;
+            int fo, law;              // law: 0 cosine, 1 uniform, 2 cos^N, 3 general reflection
+            bool flip = false;
+            R lexp = 0;
             if (des) {
-                ++c_des;
-                q3 = kFP32 ? qf(1.0f / (float)vel, (float)MFG_SCALE_INV) : qd(1.0 / (double)vel, MFG_SCALE_INV);
-                cell = (In.count & MFG_COUNT_DES) ? texture_cell<kFP32>(M, fo, pu, pv) : -1;
+                int inst = 0;
+                if (n_inst > 1) {
+                    int a = 0, b = n_inst;   // last instance whose prefix <= id
+                    while (b - a > 1) { int mid = (a + b) >> 1; if (C.inst_prefix[mid] <= P.bounces) a = mid; else b = mid; }
+                    inst = a;
+                }
+                rng.start(C.inst_first[inst] + (P.bounces - C.inst_prefix[inst]), (uint32_t)inst);
+                // source facet by cumulative outgassing (Particle.cpp:418-464)
+                const int sbase = M.inst_src_base[inst], scount = M.inst_src_count[inst];
+                double sr = (double)rng.next() * M.inst_src_total[inst];
+                int lo = 0, hi = scount;
+                while (lo < hi) { int mid = (lo + hi) >> 1; if (M.src_cdf[sbase + mid] > sr) hi = mid; else lo = mid + 1; }
+                if (lo >= scount) lo = scount - 1;
+                lo += sbase;
+                fo = M.src_facet[lo];
+                const FacetInfo2& I2 = M.info2[fo];
+                if (M.info[fo].flags & FF_TWO_SIDED) flip = (double)rng.next() > 0.5;
+                int idt = M.src_id[lo];
+                if (idt >= 0) P.time = desorption_time(M, idt, (double)rng.next());
+                else P.time = (double)rng.next() * M.latest;
+                P.structure = I2.structure;
+                P.bounces = 0;
+                if constexpr (kExt) {
+                    P.dist = 0.0;
+                    P.gen_time = P.time;
+                    P.refl = 0;
+                    P.ori = 1.0;
+                }
+                if (kSens) {
+                    ntraj = 0;
+                    src_idx = C.sens.src_of_facet[fo];
+                    if (src_idx >= 0) atomicAdd(C.sens.src_count + src_idx, 1ull);
+                }
+                law = I2.desorb_type == MFG_DES_UNIFORM ? 1 : (I2.desorb_type == MFG_DES_COSINE_N ? 2 : 0);
+                lexp = (R)I2.desorb_exp;
+                if (!M.use_maxwell) law |= 4;   // fixed speed 145.469 sqrt(T/m) (Particle.cpp:483)
+            } else {
+                fo = P.last;
+                if (M.info[fo].flags & FF_TWO_SIDED) {
+                    if (kFP32) {
+                        const FacetPhysF& Pf = M.phys_f[fo];
+                        flip = (dx * Pf.N[0] + dy * Pf.N[1] + dz * Pf.N[2]) > 0.0f;
+                    } else {
+                        const FacetIsectD& Rf = M.isect_d[fo];
+                        flip = ((double)dx * Rf.v[0] + (double)dy * Rf.v[1] + (double)dz * Rf.v[2]) > 0.0;
+                    }
+                }
+                law = (M.info[fo].flags & FF_FAST_REFL) ? 0 : 3;
             }
-            if (kSens && !des) {
-                int g = C.sens.gauge_of_facet[fo];
-                if (g >= 0) sens_output(C.sens, traj, ntraj, src_idx, g, (double)ort);   // outgoing half at a gauge
+            // speed: Maxwell at the facet temperature (desorption and full-accommodation reflection)
+            if (law < 3) {
+                if (kFP32) vel = (R)(M.phys_f[fo].sqrtT * interp_x_f((float)rng.next(), s_cdf_vf, s_cdf_pf, MFG_MAXWELL_N));
+                else vel = (R)(M.phys_d[fo].sqrtT * interp_x_d((double)rng.next(), s_cdf_v, s_cdf_p, MFG_MAXWELL_N));
+            } else if (law & 4) {
+                vel = (R)(145.469 * sqrt(M.info2[fo].temperature / M.gas_mass));
+                law &= 3;
             }
-            const unsigned long long vf = des ? 2 : 1;   // velocity factor of the 1/v_ort sum
-            const unsigned long long a1 = des ? 2 * q1 : pend_s1ov + q1;
-            const unsigned long long a2 = des ? q2 : pend_svort + q2;
-            const unsigned long long a3 = des ? q3 : pend_s1v;
-            facet_add(M, T, B, fo, 0, des ? 0 : 1, des ? 1 : 0, 0, a1, a2, a3);
-            if (cell >= 0) cell_add(T.texture + (size_t)cell * TT_N, 1, a1, a2);
-            if (In.flags & FF_PROFILE) profile_add(M, T, fo, 0, false, vf, 1, (double)cosn, (double)vel, (double)pu, (double)pv, q1, q2);
-            if (M.nm)
-                tally_moments(M, T, B, fo, P.time, des ? 1 : 0, 0, 0, vf * q1, q2, q3, cell, des ? 1 : 0, false, vf, 1,
-                              (double)cosn, (double)vel, (double)pu, (double)pv, q1, q2);
-            pend = false;
-            pend_cell = -1;
-            pend_s1ov = pend_svort = pend_s1v = 0;
-            need_new = false;
+            if (des) {
+                P.decay_at = M.enable_decay ? P.time - 1.44269 * M.half_life * log(1.0 - (double)rng.next()) : 1e100;
+                // start point: rejection in the (u,v) rectangle, at most 1000 tries (Particle.cpp:513-570)
+                start_point<kFP32>(M, fo, rng, P.ox, P.oy, P.oz, pu, pv);
+                P.last = fo;
+            }
+            if (law == 3) {
+                reflect_general<kFP32>(M, fo, flip, rng, P.time, vel, dx, dy, dz, s_cdf_v, s_cdf_p, s_cdf_vf, s_cdf_pf);
+            } else {
+                R r1 = (R)rng.next(), r2 = (R)rng.next();
+                R ct = law == 1 ? r1 : (law == 2 ? (R)pow((double)r1, 1.0 / ((double)lexp + 1.0)) : (R)sqrt(r1));
+                polar_dir<kFP32>(M, fo, ct, r2, flip, dx, dy, dz);
+            }
+            {
+                // outgoing tallies; a reflection's incoming half (pending) is added with them (moment 0)
+                const FacetInfo& In = M.info[fo];
+                R cosn;
+                if (kFP32) cosn = fabsf(dx * M.phys_f[fo].N[0] + dy * M.phys_f[fo].N[1] + dz * M.phys_f[fo].N[2]);
+                else cosn = (R)fabs((double)dx * M.isect_d[fo].v[0] + (double)dy * M.isect_d[fo].v[1] + (double)dz * M.isect_d[fo].v[2]);
+                R ort = vel * cosn;
+                double W = 1.0;   // low-flux weight of the outgoing half
+                if constexpr (kExt) {
+                    if (M.low_flux) W = P.ori;
+                }
+                unsigned long long q1 = kFP32 ? qf((float)W * (1.0f / (float)ort), (float)MFG_SCALE_INV) : qd(W * (1.0 / (double)ort), MFG_SCALE_INV);
+                unsigned long long q2 = kFP32 ? qf((float)W * (float)ort, (float)MFG_SCALE_V) : qd(W * (double)ort, MFG_SCALE_V);
+                unsigned long long q3 = 0;
+                int cell = pend_cell;
+                if (des) {
+                    ++c_des;
+                    q3 = kFP32 ? qf(1.0f / (float)vel, (float)MFG_SCALE_INV) : qd(1.0 / (double)vel, MFG_SCALE_INV);
+                    cell = (In.count & MFG_COUNT_DES) ? texture_cell<kFP32>(M, fo, pu, pv) : -1;
+                    if constexpr (kExt) {
+                        if (M.low_flux && cell >= 0)
+                            lf_counts(M, T, fo, P.time, 0.0, 0.0, cell, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0);
+                    }
+                }
+                if (kSens && !des) {
+                    int g = C.sens.gauge_of_facet[fo];
+                    if (g >= 0) sens_output(C.sens, traj, ntraj, src_idx, g, (double)ort);   // outgoing half at a gauge
+                }
+                const unsigned long long vf = des ? 2 : 1;   // velocity factor of the 1/v_ort sum
+                const unsigned long long a1 = des ? 2 * q1 : pend_s1ov + q1;
+                const unsigned long long a2 = des ? q2 : pend_svort + q2;
+                const unsigned long long a3 = des ? q3 : pend_s1v;
+                facet_add(M, T, B, fo, 0, des ? 0 : 1, des ? 1 : 0, 0, a1, a2, a3);
+                if (cell >= 0) cell_add(T.texture + (size_t)cell * TT_N, 1, a1, a2);
+                if (In.flags & FF_PROFILE) profile_add(M, T, fo, 0, false, vf, 1, (double)cosn, (double)vel, (double)pu, (double)pv, q1, q2);
+                if (M.nm)
+                    tally_moments(M, T, B, fo, P.time, des ? 1 : 0, 0, 0, vf * q1, q2, q3, cell, des ? 1 : 0, vf * q1, q2, false, vf, 1,
+                                  (double)cosn, (double)vel, (double)pu, (double)pv, q1, q2);
+                pend = false;
+                pend_cell = -1;
+                pend_s1ov = pend_svort = pend_s1v = 0;
+                need_new = false;
+            }
         }
+        relink = false;
 
         // ---- 2. trace the ray ----
         int root = M.roots[P.structure];
@@ -699,11 +797,11 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
         const double ddx = (double)dx, ddy = (double)dy, ddz = (double)dz;
         // transparent and semi-transparent facets: passes of this ray, opacity draws keyed by
         // (particle, trace step, facet) in a stream of their own
-        typename std::conditional<kTr, TranspList<R>, NoTranspList>::type tl;
+        typename std::conditional<kExt, TranspList<R>, NoTranspList>::type tl;
         OpacCtx oc;
         TranspList<R>* tlp = nullptr;
         const OpacCtx* ocp = nullptr;
-        if constexpr (kTr) {
+        if constexpr (kExt) {
             tl.n = 0;
             oc.k0 = rng.k0 ^ (rng.inst * 0x9E3779B9u);
             oc.k1 = rng.k1 ^ 0xA5A5A5A5u;
@@ -716,12 +814,12 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
         }
         if constexpr (kFP32) {
             bool amb = false;
-            HitF h = trace_f<kTr>(M, root, make_ray_f(P.ox, P.oy, P.oz, (float)dx, (float)dy, (float)dz), P.last, amb,
+            HitF h = trace_f<kExt>(M, root, make_ray_f(P.ox, P.oy, P.oz, (float)dx, (float)dy, (float)dz), P.last, amb,
                                   T.global + TG_STATUS, tlp, ocp);
             if (amb || h.f < 0) {
                 ++c_rechk;
-                if constexpr (kTr) tl.n = 0;
-                HitD hd = trace_d<R, kTr>(M, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last, T.global + TG_STATUS, tlp,
+                if constexpr (kExt) tl.n = 0;
+                HitD hd = trace_d<R, kExt>(M, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last, T.global + TG_STATUS, tlp,
                                           ocp);
                 hf = hd.f; ht = hd.t; hu = (R)hd.u; hv = (R)hd.v;
             } else {
@@ -736,7 +834,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                 ht = (double)h.t + (double)((float)r / (float)den);
             }
         } else {
-            HitD h = trace_d<R, kTr>(M, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last, T.global + TG_STATUS, tlp, ocp);
+            HitD h = trace_d<R, kExt>(M, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last, T.global + TG_STATUS, tlp, ocp);
             hf = h.f; ht = h.t; hu = (R)h.u; hv = (R)h.v;
         }
         if (hf < 0) {   // leak (Particle.cpp:387-392)
@@ -755,7 +853,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
             double dd = (double)vel * 100.0 * (P.decay_at - P.time);
             if (dd < travel) { travel = dd; event = 2; }
         }
-        if constexpr (kTr) {
+        if constexpr (kExt) {
             for (int k = 0; k < tl.n; ++k) {
                 if (!((double)tl.t[k] < travel)) continue;
                 double ort_t = transparent_pass<kFP32>(M, T, B, tl.f[k], tl.t[k], tl.u[k], tl.v[k], P.time, vel, dx, dy, dz);
@@ -774,60 +872,129 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
         c_dist += qdist;
         if (event != 0) { need_new = true; continue; }
         c_distf += qdist;
+        if constexpr (kExt) P.dist += travel;
         // ---- 4. stick or reflect at facet hf (Particle.cpp:323-357) ----
         const FacetInfo& In = M.info[hf];
-        bool absorb;
+        // sticking; the regular mode draws stick or reflect (Particle.cpp:323-336), low-flux mode
+        // splits the particle into an absorbed part wa and a reflected part wr (:338-356)
+        bool do_abs, do_refl;
+        double wa = 1.0, wr = 1.0;
         R cosn;
-        if (kFP32) {
-            float s = (In.flags & FF_STICK_PARAM) ? (float)param_at(M, M.info2[hf].stick_param, P.time) : M.phys_f[hf].sticking;
-            absorb = (s == 1.0f) || (s > 0.0f && (float)rng.next() < s);
-            cosn = fabsf(dx * M.phys_f[hf].N[0] + dy * M.phys_f[hf].N[1] + dz * M.phys_f[hf].N[2]);
-        } else {
-            const FacetIsectD& Rh = M.isect_d[hf];
-            double s = (In.flags & FF_STICK_PARAM) ? param_at(M, M.info2[hf].stick_param, P.time) : M.phys_d[hf].sticking;
-            absorb = (s == 1.0) || (s > 0.0 && (double)rng.next() < s);
-            cosn = (R)fabs(ddx * Rh.v[0] + ddy * Rh.v[1] + ddz * Rh.v[2]);
+        {
+            const double s = (In.flags & FF_STICK_PARAM) ? param_at(M, M.info2[hf].stick_param, P.time)
+                                                         : (kFP32 ? (double)M.phys_f[hf].sticking : M.phys_d[hf].sticking);
+            bool lf = false;
+            if constexpr (kExt) lf = M.low_flux != 0;
+            if (lf) {
+                if constexpr (kExt) {
+                    do_abs = s > 0.0;
+                    wa = P.ori * s;
+                    P.ori = do_abs ? P.ori * (1.0 - s) : P.ori * (1.0 - s);
+                    wr = P.ori;
+                    do_refl = P.ori > M.low_flux_cutoff;
+                }
+            } else if (kFP32) {
+                const float sf = (float)s;
+                do_abs = (sf == 1.0f) || (sf > 0.0f && (float)rng.next() < sf);
+                do_refl = !do_abs;
+            } else {
+                do_abs = (s == 1.0) || (s > 0.0 && (double)rng.next() < s);
+                do_refl = !do_abs;
+            }
+            if (kFP32) cosn = fabsf(dx * M.phys_f[hf].N[0] + dy * M.phys_f[hf].N[1] + dz * M.phys_f[hf].N[2]);
+            else cosn = (R)fabs(ddx * M.isect_d[hf].v[0] + ddy * M.isect_d[hf].v[1] + ddz * M.isect_d[hf].v[2]);
         }
-        R ort = vel * cosn;
-        unsigned long long q1 = kFP32 ? qf(1.0f / (float)ort, (float)MFG_SCALE_INV) : qd(1.0 / (double)ort, MFG_SCALE_INV);
-        unsigned long long q2 = kFP32 ? qf((float)ort, (float)MFG_SCALE_V) : qd((double)ort, MFG_SCALE_V);
-        unsigned long long q3 = kFP32 ? qf(1.0f / (float)vel, (float)MFG_SCALE_INV) : qd(1.0 / (double)vel, MFG_SCALE_INV);
+        const R ort = vel * cosn;
+        // fixed-point sums of one part of weight w: 1/v_ort, v_ort, 1/v
+        auto quant = [&](double w, unsigned long long& q1, unsigned long long& q2, unsigned long long& q3) {
+            if (kFP32) {
+                q1 = qf((float)w * (1.0f / (float)ort), (float)MFG_SCALE_INV);
+                q2 = qf((float)w * (float)ort, (float)MFG_SCALE_V);
+                q3 = qf((float)w * (1.0f / (float)vel), (float)MFG_SCALE_INV);
+            } else {
+                q1 = qd(w * (1.0 / (double)ort), MFG_SCALE_INV);
+                q2 = qd(w * (double)ort, MFG_SCALE_V);
+                q3 = qd(w * (1.0 / (double)vel), MFG_SCALE_INV);
+            }
+        };
         pu = hu;
         pv = hv;
-        int cell = (In.tex_off >= 0 && (In.count & (absorb ? MFG_COUNT_ABS : MFG_COUNT_REFL))) ? texture_cell<kFP32>(M, hf, hu, hv) : -1;
-        ++c_hits;
-        if (In.flags & FF_ANGLEMAP) anglemap_add(M, T, hf, ddx, ddy, ddz);
-        if (In.count & MFG_COUNT_DIR)
-            direction_add(M, T, hf, (double)hu, (double)hv, P.time, ddx * (double)vel, ddy * (double)vel, ddz * (double)vel);
+        c_hits += (do_abs ? 1 : 0) + (do_refl ? 1 : 0);
         if (kSens) {
             int g = C.sens.gauge_of_facet[hf];
             if (g >= 0) sens_output(C.sens, traj, ntraj, src_idx, g, (double)ort);   // incoming half / absorption
-            int k = C.sens.param_of_facet[hf];
-            if (absorb) {
+        }
+        if (do_abs) {   // RecordAbsorb (Particle.cpp:888-924)
+            unsigned long long q1, q2, q3;
+            quant(wa, q1, q2, q3);
+            ++c_abs;
+            const int cell = (In.tex_off >= 0 && (In.count & MFG_COUNT_ABS)) ? texture_cell<kFP32>(M, hf, hu, hv) : -1;
+            if (In.flags & FF_ANGLEMAP) anglemap_add(M, T, hf, ddx, ddy, ddz);
+            if (In.count & MFG_COUNT_DIR)
+                direction_add(M, T, hf, (double)hu, (double)hv, P.time, wa * ddx * (double)vel, wa * ddy * (double)vel,
+                              wa * ddz * (double)vel);
+            if (kSens) {
+                int k = C.sens.param_of_facet[hf];
                 if (C.sens.pump_of_facet[hf]) {
                     sens_output(C.sens, traj, ntraj, src_idx, MFG_SENS_NOUT - 1, 1.0);
                     if (k >= 0) atomicAdd(C.sens.B + (size_t)k * MFG_SENS_NOUT + MFG_SENS_NOUT - 1, 1.0);
                 }
-            } else if (k >= 0) {
-                if (ntraj < MFG_SENS_TRAJ) traj[ntraj++] = k;
-                else if (ntraj == MFG_SENS_TRAJ) { atomicAdd(C.sens.overflow, 1ull); ++ntraj; }
             }
-        }
-        if (absorb) {   // RecordAbsorb (Particle.cpp:888-924)
-            ++c_abs;
+            if constexpr (kExt) {
+                if (M.hist_bins) record_histograms(M, T, hf, P.time, P.refl, P.dist, P.gen_time, wa);
+                if (M.low_flux)
+                    lf_counts(M, T, hf, P.time, wa, wa, cell, wa, wa, (double)cosn, (double)vel, (double)hu, (double)hv, wa, wa);
+            }
             facet_add(M, T, B, hf, 0, 1, 0, 1, 2 * q1, q2, q3);
             if (cell >= 0) cell_add(T.texture + (size_t)cell * TT_N, 1, 2 * q1, q2);
             if (In.flags & FF_PROFILE) profile_add(M, T, hf, 0, true, 2, 1, (double)cosn, (double)vel, (double)hu, (double)hv, q1, q2);
             if (M.nm)
-                tally_moments(M, T, B, hf, P.time, 0, 1, 1, 2 * q1, q2, q3, cell, 1, true, 2, 1,
+                tally_moments(M, T, B, hf, P.time, 0, 1, 1, 2 * q1, q2, q3, cell, 1, 2 * q1, q2, true, 2, 1,
                               (double)cosn, (double)vel, (double)hu, (double)hv, q1, q2);
+        }
+        if (!do_refl) {
             need_new = true;
-        } else {        // incoming half of PerformBounce (Particle.cpp:735-767)
+            continue;
+        }
+        if (In.flags & FF_LINK) {
+            // structure link: counted as a pass, the particle goes on into the linked structure
+            // with its direction, speed and last-hit facet (PerformBounce, Particle.cpp:698-724)
+            transparent_pass<kFP32>(M, T, B, hf, (R)0, hu, hv, P.time, vel, dx, dy, dz, true, wr);
+            P.structure = M.info2[hf].link;
+            relink = true;
+            need_new = false;
+            if (++P.bounces > max_steps) {   // step cap
+                ++c_drop;
+                relink = false;
+                need_new = true;
+            }
+            continue;
+        }
+        {   // incoming half of PerformBounce (Particle.cpp:735-767)
+            unsigned long long q1, q2, q3;
+            quant(wr, q1, q2, q3);
+            const int cell = (In.tex_off >= 0 && (In.count & MFG_COUNT_REFL)) ? texture_cell<kFP32>(M, hf, hu, hv) : -1;
+            if (In.flags & FF_ANGLEMAP) anglemap_add(M, T, hf, ddx, ddy, ddz);
+            if (In.count & MFG_COUNT_DIR)
+                direction_add(M, T, hf, (double)hu, (double)hv, P.time, wr * ddx * (double)vel, wr * ddy * (double)vel,
+                              wr * ddz * (double)vel);
+            if (kSens) {
+                int k = C.sens.param_of_facet[hf];
+                if (k >= 0) {
+                    if (ntraj < MFG_SENS_TRAJ) traj[ntraj++] = k;
+                    else if (ntraj == MFG_SENS_TRAJ) { atomicAdd(C.sens.overflow, 1ull); ++ntraj; }
+                }
+            }
+            if constexpr (kExt) {
+                if (M.low_flux)
+                    lf_counts(M, T, hf, P.time, wr, 0.0, cell, wr, wr, (double)cosn, (double)vel, (double)hu, (double)hv, wr, 0.0);
+            }
             if (In.flags & FF_PROFILE) profile_add(M, T, hf, 0, true, 1, 1, (double)cosn, (double)vel, (double)hu, (double)hv, q1, q2);
             if (M.nm)
-                tally_moments(M, T, B, hf, P.time, 0, 1, 0, q1, q2, q3, cell, 1, true, 1, 1,
+                tally_moments(M, T, B, hf, P.time, 0, 1, 0, q1, q2, q3, cell, 1, q1, q2, true, 1, 1,
                               (double)cosn, (double)vel, (double)hu, (double)hv, q1, q2);
             P.last = hf;
+            if constexpr (kExt) ++P.refl;
             pend = true;
             pend_s1ov = q1;
             pend_svort = q2;

@@ -46,7 +46,19 @@ FACET_FIELDS = {
     "sojourn_freq": (np.float64, 0.0),
     "sojourn_e": (np.float64, 0.0),
     "is_moving": (np.uint8, 0),
+    # facet histogram settings (sh.facetHistogramParams): MFG_HIST_* bits and bin sizes / limits
+    "hist_record": (np.uint32, 0),
+    "hist_bounce_binsize": (np.uint64, 1),
+    "hist_bounce_max": (np.uint64, 0),
+    "hist_distance_binsize": (np.float64, 1.0),
+    "hist_distance_max": (np.float64, 0.0),
+    "hist_time_binsize": (np.float64, 1.0),
+    "hist_time_max": (np.float64, 0.0),
 }
+HIST_FIELDS = ("record", "bounce_binsize", "bounce_max", "distance_binsize", "distance_max", "time_binsize", "time_max")
+HIST_DTYPE = np.dtype([("record", np.uint32), ("pad", np.uint32), ("bounce_binsize", np.uint64),
+                       ("bounce_max", np.uint64), ("distance_binsize", np.float64), ("distance_max", np.float64),
+                       ("time_binsize", np.float64), ("time_max", np.float64)])
 
 _CTYPE = {np.float64: C.c_double, np.int32: C.c_int32, np.uint8: C.c_uint8, np.uint32: C.c_uint32}
 
@@ -77,6 +89,9 @@ class Model:
         self.moment_time = np.zeros(0)
         self.moment_window = np.zeros(0)
         self.params = []   # list of (t array, v array, logx, logy)
+        # sp.globalHistogramParams
+        self.global_histogram = dict(record=0, bounce_binsize=1, bounce_max=0, distance_binsize=1.0,
+                                     distance_max=0.0, time_binsize=1.0, time_max=0.0)
         for k, v in kw.items():
             setattr(self, k, v)
 
@@ -110,6 +125,8 @@ class Model:
         d.facet_vertex_start = p(self.facet_vertex_start, C.c_int32)
         d.facet_vertex_index = p(self.facet_vertex_index, C.c_int32)
         for name, (dt, _) in FACET_FIELDS.items():
+            if name.startswith("hist_"):   # packed into facet_histogram below
+                continue
             arr = np.asarray(getattr(self, name), dtype=dt)
             assert arr.shape == (self.n_facets,), name
             setattr(d, name, p(arr, _CTYPE[dt]))
@@ -139,6 +156,16 @@ class Model:
         d.param_v = p(pv, C.c_double)
         d.param_log_x = p(np.array([x[2] for x in self.params] or [0], np.uint8), C.c_uint8)
         d.param_log_y = p(np.array([x[3] for x in self.params] or [0], np.uint8), C.c_uint8)
+        gh = A.HistogramParams()
+        for k in HIST_FIELDS:
+            setattr(gh, k, type(getattr(gh, k))(self.global_histogram[k]))
+        d.global_histogram = gh
+        if self.hist_record.any():
+            fh = np.zeros(self.n_facets, HIST_DTYPE)
+            for k in HIST_FIELDS:
+                fh[k] = getattr(self, "hist_" + k)
+            keep.append(fh)
+            d.facet_histogram = fh.ctypes.data_as(C.POINTER(A.HistogramParams))
         d._keep = keep
         return d
 
@@ -177,9 +204,29 @@ class Model:
                     self.anglemap_theta_lower_res[i] + self.anglemap_theta_higher_res[i] > 0:
                 ang_off[i] = ac
                 ac += int(self.anglemap_phi_width[i]) * int(self.anglemap_theta_lower_res[i] + self.anglemap_theta_higher_res[i])
+        # histograms: the global ones, then each recording facet's, bounce / distance / time
+        class _H:
+            pass
+        hb = 0
+        g = _H()
+        for k in HIST_FIELDS:
+            setattr(g, k, self.global_histogram[k])
+        gsz = A.histogram_sizes(g)
+        hb += sum(gsz)
+        hist_off = np.full(self.n_facets, -1, np.int64)
+        hist_sz = np.zeros((self.n_facets, 3), np.int64)
+        for i in range(self.n_facets):
+            if self.hist_record[i]:
+                f = _H()
+                for k in HIST_FIELDS:
+                    setattr(f, k, getattr(self, "hist_" + k)[i])
+                hist_sz[i] = A.histogram_sizes(f)
+                hist_off[i] = hb
+                hb += int(hist_sz[i].sum())
         return dict(n_facets=self.n_facets, n_moments=nm, blocks=B, texture_cells=int(tc), direction_cells=int(dc),
                     anglemap_cells=int(ac), profile_facets=int(pc), tex_off=tex_off, dir_off=dir_off,
-                    ang_off=ang_off, prof_idx=prof_idx, tex_w=w, tex_h=h)
+                    ang_off=ang_off, prof_idx=prof_idx, tex_w=w, tex_h=h, histogram_bins=int(hb),
+                    global_hist_sizes=gsz, hist_off=hist_off, hist_sizes=hist_sz)
 
 
 class SimuState:
@@ -196,6 +243,7 @@ class SimuState:
         self.profile = np.zeros((B, L["profile_facets"], A.PROFILE_SIZE, 3), np.float64)
         self.direction = np.zeros((B, L["direction_cells"], 4), np.float64)
         self.anglemap = np.zeros(max(L["anglemap_cells"], 0), np.uint64)
+        self.histogram = np.zeros((B, L.get("histogram_bins", 0)), np.float64)
 
     def view(self):
         v = A.StateView()
@@ -206,11 +254,12 @@ class SimuState:
         v.profile = A.ptr(self.profile, C.c_double)
         v.direction = A.ptr(self.direction, C.c_double)
         v.anglemap = A.ptr(self.anglemap, C.c_uint64)
+        v.histogram = A.ptr(self.histogram, C.c_double)
         return v
 
     def __iadd__(self, other):
         """GlobalSimuState::operator+= (src/Simulation/MolflowSimGeom.cpp:452-458)."""
-        for name in ("global_", "facet_counts", "facet_sums", "texture", "profile", "direction", "anglemap"):
+        for name in ("global_", "facet_counts", "facet_sums", "texture", "profile", "direction", "anglemap", "histogram"):
             getattr(self, name).__iadd__(getattr(other, name))
         return self
 
@@ -229,6 +278,22 @@ class SimuState:
     def transmission(self, facet):
         """absorbed on `facet` / desorbed (the fixtures' 'A2/SUMDES' formula)."""
         return self.absorbed(facet) / max(self.n_desorbed, 1.0)
+
+    def histograms_of(self, facet=None, moment=0):
+        """(bounce, distance, time) histograms of a facet, or the global ones (facet None);
+        None for the kinds not recorded."""
+        L = self.L
+        if facet is None:
+            o, sz = 0, L["global_hist_sizes"]
+        else:
+            o, sz = L["hist_off"][facet], L["hist_sizes"][facet]
+            if o < 0:
+                return (None, None, None)
+        out = []
+        for n in sz:
+            out.append(self.histogram[moment, o:o + n] if n else None)
+            o += n
+        return tuple(out)
 
     def texture_of(self, facet, moment=0):
         L = self.L

@@ -45,25 +45,73 @@ def _i(node, attr, default=0):
 
 
 def _parse_user_moments(um_node):
-    """UserMoments entries: 'begin,spacing,end' ranges or single times (TimeMoments.cpp:58-83)."""
+    """UserMoments entries: 'begin,spacing,end' ranges or single times
+    (TimeMoments::ParseUserMoment, TimeMoments.cpp:58-83): a range needs end > begin >= 0 and
+    spacing < end - begin, is skipped when spacing < window, and is enumerated by repeated
+    addition (time += spacing while time <= end), so the rounding of the sum decides whether
+    the end point is included."""
     times, windows = [], []
     if um_node is None:
         return times, windows
     for u in um_node.findall("UserEntry"):
         content = u.get("content", "")
         win = float(u.get("window", "0"))
-        parts = [p for p in content.replace(" ", "").split(",") if p]
-        if len(parts) == 3:
-            b, s, e = map(float, parts)
-            k = 0
-            while b + k * s <= e * (1 + 1e-12) and s > 0:
-                times.append(b + k * s)
-                windows.append(win)
-                k += 1
-        elif len(parts) == 1:
-            times.append(float(parts[0]))
+        parts = []
+        for p in content.replace(" ", "").split(",")[:3]:
+            try:
+                parts.append(float(p))
+            except ValueError:
+                break
+        if len(parts) == 1 and parts[0] >= 0.0:
+            times.append(parts[0])
             windows.append(win)
+        elif len(parts) == 3:
+            b, sp, e = parts
+            if b >= 0.0 and e > b and sp < e - b and not sp < win:
+                t = b
+                while t <= e:
+                    times.append(t)
+                    windows.append(win)
+                    t += sp
     return times, windows
+
+
+def _hist_params(node):
+    """HistogramParams from a <Histograms>/<Global_histograms> settings node (LoaderXML.cpp:179-203,
+    1080-1105): dict with record bits and bin sizes / limits."""
+    h = dict(record=0, bounce_binsize=1, bounce_max=0, distance_binsize=1.0, distance_max=0.0,
+             time_binsize=1.0, time_max=0.0)
+    if node is None:
+        return h
+    b, d, t = node.find("Bounces"), node.find("Distance"), node.find("Time")
+    if b is not None:
+        h["record"] |= A.HIST_BOUNCE
+        h["bounce_binsize"] = int(float(b.get("binSize", "1")))
+        h["bounce_max"] = int(float(b.get("max", "0")))
+    if d is not None:
+        h["record"] |= A.HIST_DISTANCE
+        h["distance_binsize"] = float(d.get("binSize"))
+        h["distance_max"] = float(d.get("max"))
+    if t is not None:
+        h["record"] |= A.HIST_TIME
+        h["time_binsize"] = float(t.get("binSize"))
+        h["time_max"] = float(t.get("max"))
+    return h
+
+
+def _hist_values(node, sizes):
+    """Stored histogram bins of a results <Histograms> node, concatenated bounce/distance/time."""
+    out = []
+    for tag, n in zip(("Bounces", "Distance", "Time"), sizes):
+        if not n:
+            continue
+        vals = np.zeros(n)
+        h = node.find(tag) if node is not None else None
+        if h is not None and int(h.get("size", "0")) == n:
+            for k, b in enumerate(h.findall("Bin")[:n]):
+                vals[k] = float(b.get("count"))
+        out.append(vals)
+    return np.concatenate(out) if out else np.zeros(0)
 
 
 def load_catalog(folder):
@@ -173,6 +221,9 @@ def load(path_or_bytes, with_state=True, catalog=()):
                 m.anglemap_theta_limit[k] = _f(am, "thetaLimit", 1.570796326)
                 m.anglemap_theta_lower_res[k] = _i(am, "thetaLowerRes")
                 m.anglemap_theta_higher_res[k] = _i(am, "thetaHigherRes")
+        hp = _hist_params(f.find("Histograms"))
+        for key, val in hp.items():
+            getattr(m, "hist_" + key)[k] = val
         if tx is not None:
             m.tex_width[k] = _f(tx, "texDimX")
             m.tex_height[k] = _f(tx, "texDimY")
@@ -192,6 +243,7 @@ def load(path_or_bytes, with_state=True, catalog=()):
         lf = sims.find("LowFluxMode")
         m.low_flux_mode = _i(lf, "enabled")
         m.low_flux_cutoff = _f(lf, "cutoff", 1e-7)
+        m.global_histogram = _hist_params(sims.find("Global_histograms"))
         ts = sims.find("TimeSettings")
         m.time_window = _f(ts, "timeWindow", 1e-10)
         m.use_maxwell = _i(ts, "useMaxwellDistr", 1)
@@ -224,8 +276,16 @@ def load_state(r, m):
             st.global_[A.G_NBLEAK] = _f(gh, "totalLeak")
             st.global_[A.G_DIST_TOTAL] = _f(gh, "totalDist_total")
             st.global_[A.G_DIST_FULLHITS] = _f(gh, "totalDist_fullHitsOnly")
+        hb = L["histogram_bins"]
+        if hb:
+            gs = L["global_hist_sizes"]
+            if sum(gs):
+                st.histogram[mi, :sum(gs)] = _hist_values(mom.find("Histograms"), gs)
         for fr in mom.find("FacetResults").findall("Facet"):
             k = int(fr.get("id"))
+            if hb and L["hist_off"][k] >= 0:
+                o, sz = L["hist_off"][k], L["hist_sizes"][k]
+                st.histogram[mi, o:o + sz.sum()] = _hist_values(fr.find("Histograms"), sz)
             h = fr.find("Hits")
             st.facet_counts[mi, k, A.FC_NBMCHIT] = int(float(h.get("nbHit")))
             st.facet_counts[mi, k, A.FC_NBDESORBED] = int(float(h.get("nbDes")))
@@ -261,10 +321,14 @@ def load_state(r, m):
                     sub = np.zeros((hh, w))
                     sub[:grid.shape[0], :grid.shape[1]] = grid
                     st.texture[mi, o:o + w * hh, field] = sub.reshape(-1)
-            am = fr.find("IncidentAngleMap")
-            if am is not None and L["ang_off"][k] >= 0 and mi == 0:
-                vals = np.array(am.text.split(), dtype=np.float64) if am.text else np.zeros(0)
-                o = L["ang_off"][k]
-                n = min(vals.size, st.anglemap.size - o)
-                st.anglemap[o:o + n] = vals[:n].astype(np.uint64)
+    # recorded incident-angle maps sit in the geometry's facet nodes (LoaderXML.cpp:1043-1070)
+    for k, fnode in enumerate(r.find("Geometry").find("Facets").findall("Facet")):
+        am = fnode.find("IncidentAngleMap")
+        if am is None or am.find("map") is None or am.get("angleMapThetaLimit") is None or L["ang_off"][k] < 0:
+            continue
+        txt = am.find("map").text or ""
+        vals = np.array(txt.split(), dtype=np.float64)
+        o = L["ang_off"][k]
+        n = min(vals.size, st.anglemap.size - o)
+        st.anglemap[o:o + n] = vals[:n].astype(np.uint64)
     return st

@@ -197,6 +197,28 @@ typedef struct { double bmin[3], bmax[3]; int left, right, first, count; } onode
 typedef struct { int n; double* t; double* v; int logx, logy; } oparam;
 typedef struct { int n; double* t; double* cum; } oid;
 
+/* one histogram set (HistogramParams): bin sizes and bin counts, offset in a moment block */
+typedef struct {
+    uint32_t record;
+    uint64_t bounce_bin; double dist_bin, time_bin;
+    long nb, nd, nt;       /* bins; 0 when not recorded */
+    long off;              /* -1 when nothing is recorded */
+} ohist;
+
+static void hist_init(ohist* h, const mfg_histogram_params* p) {
+    memset(h, 0, sizeof *h);
+    h->off = -1;
+    if (!p || !p->record) return;
+    h->record = p->record;
+    h->bounce_bin = p->bounce_binsize ? p->bounce_binsize : 1;
+    h->dist_bin = p->distance_binsize;
+    h->time_bin = p->time_binsize;
+    /* bin counts restated from the sizes the reference stores with its histograms */
+    if (p->record & MFG_HIST_BOUNCE) h->nb = (long)(p->bounce_max / h->bounce_bin) + 2;
+    if (p->record & MFG_HIST_DISTANCE) h->nd = (long)(size_t)(p->distance_max / p->distance_binsize) + 1;
+    if (p->record & MFG_HIST_TIME) h->nt = (long)(size_t)(p->time_max / p->time_binsize) + 1;
+}
+
 struct orc_model {
     int nf, nstruct;
     ofacet* f;
@@ -213,6 +235,8 @@ struct orc_model {
     int nparams; oparam* params;
     int nid; oid* ids;
     double* src_prefix; int* src_facet; int nsrc; double src_total;
+    ohist ghist;           /* global histograms; offset 0 of each moment block */
+    ohist* fhist;          /* per facet, NULL when no facet records */
     mfg_state_layout L;
 };
 
@@ -576,8 +600,13 @@ int orc_model_create(const mfg_model_desc* d, orc_model** out, char* err, size_t
         F->sojourn = OPT(d->enable_sojourn, i, 0);
         F->soj_freq = OPT(d->sojourn_freq, i, 0.0);
         F->soj_e = OPT(d->sojourn_e, i, 0.0);
-        if (F->link || F->teleport || OPT(d->is_moving, i, 0) || F->desorb_type == MFG_DES_ANGLEMAP) {
-            snprintf(msg, sizeof msg, "facet %d: link/teleport/moving/angle-map desorption not traced by the oracle", i + 1);
+        if (F->link < 0 || F->link > M->nstruct) {
+            set_err(err, errlen, "structure link destination out of range");
+            orc_model_destroy(M);
+            return MFG_ERR_INVALID_MODEL;
+        }
+        if (F->teleport || OPT(d->is_moving, i, 0) || F->desorb_type == MFG_DES_ANGLEMAP) {
+            snprintf(msg, sizeof msg, "facet %d: teleport/moving/angle-map desorption not traced by the oracle", i + 1);
             set_err(err, errlen, msg); orc_model_destroy(M); return MFG_ERR_UNSUPPORTED_FEATURE;
         }
         if (F->structure < -1 || F->structure >= M->nstruct) { set_err(err, errlen, "structure index out of range"); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL; }
@@ -676,6 +705,18 @@ int orc_model_create(const mfg_model_desc* d, orc_model** out, char* err, size_t
     L->n_profile = B * L->profile_facets * MFG_PROFILE_SIZE * 3;
     L->n_direction = B * L->direction_cells * 4;
     L->n_anglemap = L->anglemap_cells;
+    hist_init(&M->ghist, &d->global_histogram);
+    long hb = 0;
+    if (M->ghist.record) { M->ghist.off = 0; hb = M->ghist.nb + M->ghist.nd + M->ghist.nt; }
+    if (d->facet_histogram) {
+        M->fhist = (ohist*)calloc(M->nf, sizeof(ohist));
+        for (int i = 0; i < M->nf; ++i) {
+            hist_init(&M->fhist[i], &d->facet_histogram[i]);
+            if (M->fhist[i].record) { M->fhist[i].off = hb; hb += M->fhist[i].nb + M->fhist[i].nd + M->fhist[i].nt; }
+        }
+    }
+    L->histogram_bins = hb;
+    L->n_histogram = B * hb;
     M->texinc = (double*)calloc(L->texture_cells + 1, sizeof(double));
     for (int i = 0; i < M->nf; ++i) {
         ofacet* F = &M->f[i];
@@ -712,6 +753,7 @@ void orc_model_destroy(orc_model* M) {
     if (M->ids) for (int k = 0; k < M->nid; ++k) { free(M->ids[k].t); free(M->ids[k].cum); }
     free(M->ids);
     free(M->src_prefix); free(M->src_facet);
+    free(M->fhist);
     free(M);
 }
 
@@ -828,6 +870,7 @@ typedef struct {
     double* prof;
     double* dir;
     uint64_t* ang;
+    double* hist;
 } otally;
 
 typedef struct {
@@ -1043,6 +1086,39 @@ static void transparent_pass(const orc_model* M, otally* T, int fi, const ohit* 
     P->u = su; P->v = sv;
 }
 
+/* RecordHistograms (Particle.cpp:926-975): bounces, flight distance and flight time of the
+ * absorbed particle, in moment 0 and the moments of the absorption time */
+static void hist_add(const ohist* h, double* block, const opart* P) {
+    if (h->off < 0) return;
+    double* b = block + h->off;
+    if (h->nb) {
+        uint64_t k = P->bounces / h->bounce_bin;
+        if (k > (uint64_t)(h->nb - 1)) k = (uint64_t)(h->nb - 1);
+        b[k] += P->ori;
+        b += h->nb;
+    }
+    if (h->nd) {
+        size_t k = (size_t)(P->dist / h->dist_bin);
+        if (k > (size_t)(h->nd - 1)) k = (size_t)(h->nd - 1);
+        b[k] += P->ori;
+        b += h->nd;
+    }
+    if (h->nt) {
+        size_t k = (size_t)((P->time - P->gen_time) / h->time_bin);
+        if (k > (size_t)(h->nt - 1)) k = (size_t)(h->nt - 1);
+        b[k] += P->ori;
+    }
+}
+static void record_histograms(const orc_model* M, otally* T, const int* ms, int nms, int fi, const opart* P) {
+    const long hb = M->L.histogram_bins;
+    if (!hb) return;
+    for (int k = -1; k < nms; ++k) {
+        double* block = T->hist + (size_t)((k < 0) ? 0 : ms[k]) * hb;
+        hist_add(&M->ghist, block, P);
+        if (M->fhist) hist_add(&M->fhist[fi], block, P);
+    }
+}
+
 /* RecordAbsorb (Particle.cpp:888-924) */
 static void record_absorb(const orc_model* M, otally* T, int fi, opart* P) {
     const ofacet* F = &M->f[fi];
@@ -1052,6 +1128,7 @@ static void record_absorb(const orc_model* M, otally* T, int fi, opart* P) {
     facet_counter(M, T, ms, nms, fi, 1, 0, 1, 2.0 / ort, (M->use_maxwell ? 1.0 : 1.1781) * ort, P);
     profile_hit(M, T, ms, nms, F, P, 1, 2.0, 1.0);
     if (F->ang_off >= 0) anglemap_hit(M, T, F, P);
+    record_histograms(M, T, ms, nms, fi, P);
     if (F->count & MFG_COUNT_ABS) texture_hit(M, T, ms, nms, F, P, 1, 2.0, 1.0);
     if ((F->count & MFG_COUNT_DIR) && F->dir_off >= 0) direction_hit(M, T, ms, nms, F, P);
 }
@@ -1071,10 +1148,23 @@ static void update_velocity(const orc_model* M, const ofacet* F, rng_t* r, opart
     }
 }
 
-/* PerformBounce (Particle.cpp:691-838), no link/moving facets */
+/* PerformBounce (Particle.cpp:691-838), no moving facets */
 static void perform_bounce(const orc_model* M, otally* T, int fi, rng_t* r, opart* P) {
     const ofacet* F = &M->f[fi];
     T->global[MFG_G_NBMCHIT] += 1; T->global[MFG_G_NBHITEQUIV] += P->ori;
+    if (F->link) {
+        /* structure link (Particle.cpp:698-724): counted like a transparent pass without
+         * velocity sums on the facet counter; the particle continues in structure link-1 with
+         * its direction, speed and last-hit facet unchanged */
+        int ms[256]; int nms = moments_of(M, P->time, ms, 256);
+        facet_counter(M, T, ms, nms, fi, 1, 0, 0, 0.0, 0.0, P);
+        profile_hit(M, T, ms, nms, F, P, 1, 2.0, 2.0);
+        if (F->ang_off >= 0) anglemap_hit(M, T, F, P);
+        if (F->count & MFG_COUNT_TRANS) texture_hit(M, T, ms, nms, F, P, 1, 2.0, 2.0);
+        if ((F->count & MFG_COUNT_DIR) && F->dir_off >= 0) direction_hit(M, T, ms, nms, F, P);
+        P->structure = F->link - 1;
+        return;
+    }
     int revert = F->two_sided ? (dot3(P->d, F->N) > 0.0) : 0;
     double ort = P->velocity * fabs(dot3(P->d, F->N));
     double vf = M->use_maxwell ? 1.0 : 1.1781;
@@ -1125,9 +1215,10 @@ static void tally_alloc(const orc_model* M, otally* T) {
     T->prof = (double*)calloc(L->n_profile + 1, sizeof(double));
     T->dir = (double*)calloc(L->n_direction + 1, sizeof(double));
     T->ang = (uint64_t*)calloc(L->n_anglemap + 1, sizeof(uint64_t));
+    T->hist = (double*)calloc(L->n_histogram + 1, sizeof(double));
 }
 static void tally_free(otally* T) {
-    free(T->global); free(T->fc); free(T->fs); free(T->tex); free(T->prof); free(T->dir); free(T->ang);
+    free(T->global); free(T->fc); free(T->fs); free(T->tex); free(T->prof); free(T->dir); free(T->ang); free(T->hist);
 }
 
 /* trace one particle to absorption/leak: the body of SimulationMCStep (Particle.cpp:221-393) */
@@ -1240,6 +1331,7 @@ int orc_run(orc_model* M, uint64_t n_des, const orc_run_opts* o, mfg_state_view*
         if (view->profile) for (int64_t k = 0; k < L->n_profile; ++k) view->profile[k] += T->prof[k];
         if (view->direction) for (int64_t k = 0; k < L->n_direction; ++k) view->direction[k] += T->dir[k];
         if (view->anglemap) for (int64_t k = 0; k < L->n_anglemap; ++k) view->anglemap[k] += T->ang[k];
+        if (view->histogram) for (int64_t k = 0; k < L->n_histogram; ++k) view->histogram[k] += T->hist[k];
         st->desorbed += th[t].st.desorbed; st->hits += th[t].st.hits; st->leaks += th[t].st.leaks;
         st->dropped += th[t].st.dropped; st->rays += th[t].st.rays;
         st->node_visits += th[t].st.node_visits; st->prim_tests += th[t].st.prim_tests;
