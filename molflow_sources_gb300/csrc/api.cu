@@ -420,7 +420,7 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     C.abort_flag = s->d_abort;
     if (sens) C.sens = s->sens;
     size_t fac_bytes = size_t(h.nf) * SF_N * 8;
-    C.smem_facets = fac_bytes <= 64 * 1024 ? 1 : 0;
+    C.smem_facets = fac_bytes <= 32 * 1024 ? 1 : 0;   // leaves room for 4 blocks per SM with their stacks
     size_t dyn = (TG_N + (C.smem_facets ? size_t(h.nf) * SF_N : 0)) * 8;
     if (o.block_size == 0 && o.blocks_per_sm == 0 && s->tuned_block[o.precision]) {
         o.block_size = s->tuned_block[o.precision];
@@ -428,6 +428,7 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     }
     int block = o.block_size > 0 ? o.block_size : 256;
     if (block % 32 || block > 256) return fail(MFG_ERR_INVALID_ARGUMENT, "block_size must be a multiple of 32, at most 256");
+    dyn += size_t(mfgk::kSmemStack) * size_t(block) * sizeof(int);   // shared-memory traversal stacks
     // kernel variant: FP64, or FP32R compiled for at least 2, 3 or 4 resident blocks per SM
     // (register budgets 128, 85, 64); blocks_per_sm selects the FP32R variant.  Models with
     // transparent or semi-transparent facets use the variants that keep a pass list (+100).

@@ -568,6 +568,8 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
     B.sfac = C.smem_facets ? smem + TG_N : nullptr;
     const int nsm = TG_N + (C.smem_facets ? M.nf * SF_N : 0);
     for (int i = threadIdx.x; i < nsm; i += blockDim.x) smem[i] = 0ull;
+    // this thread's slice of the shared-memory traversal stacks, after the tally partials
+    int* smstk = reinterpret_cast<int*>(smem + nsm) + threadIdx.x;
     for (int i = threadIdx.x; i < MFG_MAXWELL_N; i += blockDim.x) {
         s_cdf_v[i] = M.cdf_v[i];
         s_cdf_p[i] = M.cdf_p[i];
@@ -815,12 +817,12 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
         if constexpr (kFP32) {
             bool amb = false;
             HitF h = trace_f<kExt>(M, root, make_ray_f(P.ox, P.oy, P.oz, (float)dx, (float)dy, (float)dz), P.last, amb,
-                                  T.global + TG_STATUS, tlp, ocp);
+                                  T.global + TG_STATUS, tlp, ocp, smstk, blockDim.x);
             if (amb || h.f < 0) {
                 ++c_rechk;
                 if constexpr (kExt) tl.n = 0;
                 HitD hd = trace_d<R, kExt>(M, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last, T.global + TG_STATUS, tlp,
-                                          ocp);
+                                          ocp, smstk, blockDim.x);
                 hf = hd.f; ht = hd.t; hu = (R)hd.u; hv = (R)hd.v;
             } else {
                 hf = h.f;
@@ -834,7 +836,8 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                 ht = (double)h.t + (double)((float)r / (float)den);
             }
         } else {
-            HitD h = trace_d<R, kExt>(M, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last, T.global + TG_STATUS, tlp, ocp);
+            HitD h = trace_d<R, kExt>(M, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last, T.global + TG_STATUS, tlp, ocp,
+                                      smstk, blockDim.x);
             hf = h.f; ht = h.t; hu = (R)h.u; hv = (R)h.v;
         }
         if (hf < 0) {   // leak (Particle.cpp:387-392)

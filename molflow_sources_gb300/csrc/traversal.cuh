@@ -14,6 +14,26 @@
 namespace mfgk {
 
 constexpr int kStack = 64;
+constexpr int kSmemStack = 24;   // stack entries kept in shared memory by the tracer kernel
+
+// Traversal stack of one thread: the first kSmemStack entries in shared memory (entry k at
+// sm[k * stride], so a warp's accesses to one level fall in distinct banks), deeper entries and
+// every entry of callers without a shared-memory slice (sm null) in local memory.
+struct TravStack {
+    int* sm;
+    int stride;
+    int sp;
+    int loc[kStack];
+    __device__ __forceinline__ void push(int v) {
+        if (sm && sp < kSmemStack) sm[sp * stride] = v;
+        else loc[sp] = v;
+        ++sp;
+    }
+    __device__ __forceinline__ int pop() {
+        --sp;
+        return (sm && sp < kSmemStack) ? sm[sp * stride] : loc[sp];
+    }
+};
 
 // InterpolateY (no extrapolation) for time-dependent parameters
 __device__ __noinline__ double param_at(const DevModel& M, int p, double t) {
@@ -114,14 +134,17 @@ struct HitD {
 template <class LT = double, bool kTr = true>
 __device__ __noinline__ HitD trace_d(const DevModel& M, int root, double ox, double oy, double oz,
                                      double dx, double dy, double dz, int last, unsigned long long* status,
-                                     TranspList<LT>* tl = nullptr, const OpacCtx* oc = nullptr) {
+                                     TranspList<LT>* tl = nullptr, const OpacCtx* oc = nullptr,
+                                     int* smstk = nullptr, int sstride = 0) {
     HitD h;
     h.f = -1;
     h.t = 1.0e99;
     h.u = h.v = 0;
     double ix = 1.0 / dx, iy = 1.0 / dy, iz = 1.0 / dz;
-    int stack[kStack];
-    int sp = 0;
+    TravStack stk;
+    stk.sm = smstk;
+    stk.stride = sstride;
+    stk.sp = 0;
     int node = root;
     while (true) {
         const NodeD nd = M.nodes_d[node];
@@ -135,7 +158,7 @@ __device__ __noinline__ HitD trace_d(const DevModel& M, int root, double ox, dou
             int near = nd.a, far = nd.a + 1;
             double dax = nd.b == 0 ? dx : (nd.b == 1 ? dy : dz);
             if (dax < 0) { near = nd.a + 1; far = nd.a; }
-            if (sp < kStack) stack[sp++] = far;
+            if (stk.sp < kStack) stk.push(far);
             else atomicOr(status, KS_STACK);
             node = near;
             continue;
@@ -167,8 +190,8 @@ __device__ __noinline__ HitD trace_d(const DevModel& M, int root, double ox, dou
                 if (t < h.t || f < h.f) { h.f = f; h.t = t; h.u = u; h.v = v; }
             }
         }
-        if (sp == 0) break;
-        node = stack[--sp];
+        if (stk.sp == 0) break;
+        node = stk.pop();
     }
     return h;
 }
@@ -228,7 +251,7 @@ __device__ __forceinline__ RayF make_ray_f(double ox, double oy, double oz, floa
 template <bool kTr = true>
 __device__ __noinline__ HitF trace_f(const DevModel& M, int root, const RayF& ray, int last, bool& ambiguous,
                                      unsigned long long* status, TranspList<float>* tl = nullptr,
-                                     const OpacCtx* oc = nullptr) {
+                                     const OpacCtx* oc = nullptr, int* smstk = nullptr, int sstride = 0) {
     HitF h;
     h.f = -1;
     h.t = 3.0e38f;
@@ -237,8 +260,10 @@ __device__ __noinline__ HitF trace_f(const DevModel& M, int root, const RayF& ra
     const float dx = ray.dx, dy = ray.dy, dz = ray.dz;
     const float ox = ray.ohx, oy = ray.ohy, oz = ray.ohz;
     float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
-    int stack[kStack];
-    int sp = 0;
+    TravStack stk;
+    stk.sm = smstk;
+    stk.stride = sstride;
+    stk.sp = 0;
     int node = root;
     while (true) {
         const NodeF nd = M.nodes_f[node];
@@ -252,7 +277,7 @@ __device__ __noinline__ HitF trace_f(const DevModel& M, int root, const RayF& ra
             int near = nd.a, far = nd.a + 1;
             float dax = nd.b == 0 ? dx : (nd.b == 1 ? dy : dz);
             if (dax < 0) { near = nd.a + 1; far = nd.a; }
-            if (sp < kStack) stack[sp++] = far;
+            if (stk.sp < kStack) stk.push(far);
             else atomicOr(status, KS_STACK);
             node = near;
             continue;
@@ -321,8 +346,8 @@ __device__ __noinline__ HitF trace_f(const DevModel& M, int root, const RayF& ra
                 if (t < h.t) { h.f = f; h.t = t; h.u = u; h.v = v; htol = tol; }
             }
         }
-        if (sp == 0) break;
-        node = stack[--sp];
+        if (stk.sp == 0) break;
+        node = stk.pop();
     }
     return h;
 }

@@ -37,7 +37,11 @@ def test_fp64_low_flux_equals_oracle():
     np.testing.assert_allclose(g.global_[A.G_NBHITEQUIV], r.global_[A.G_NBHITEQUIV], rtol=1e-9)
     np.testing.assert_allclose(g.global_[A.G_NBABSEQUIV], r.global_[A.G_NBABSEQUIV], rtol=1e-9)
     np.testing.assert_allclose(g.facet_sums, r.facet_sums, rtol=1e-6, atol=1e-6)
-    np.testing.assert_allclose(g.texture, r.texture, rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(g.texture[..., 0], r.texture[..., 0], rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(g.texture[..., 2], r.texture[..., 2], rtol=1e-6, atol=1e-6)
+    # sum of v_ort per area: each sample is quantized to 2^-20 m/s before the 1/area increment of
+    # its cell (~4e3 /cm2 on the 64x64 wall texture), and low-flux weights make samples small
+    np.testing.assert_allclose(g.texture[..., 1], r.texture[..., 1], rtol=1e-3, atol=1e-6)
     np.testing.assert_allclose(g.profile, r.profile, rtol=1e-6, atol=1e-6)
     np.testing.assert_allclose(g.direction, r.direction, rtol=1e-6, atol=1e-6)
     # the split conserves weight: what desorbs is absorbed or dropped below the cutoff
