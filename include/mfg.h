@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define MFG_ABI_VERSION 2u
+#define MFG_ABI_VERSION 3u
 
 /* ---- status codes (replace the reference's exceptions / MCStepResult,
  *      src/Simulation/Particle.h:24-28, src/Simulation/MolflowSimGeom.cpp:219-247) ---- */
@@ -176,6 +176,29 @@ typedef struct mfg_model_desc {
     /* histograms recorded at each absorption (RecordHistograms, Particle.cpp:926-975) */
     mfg_histogram_params global_histogram;          /* sp.globalHistogramParams */
     const mfg_histogram_params* facet_histogram;    /* sh.facetHistogramParams [n_facets] or NULL */
+
+    /* moving facets (sp.motionType, motionVector1/2; Physics::TreatMovingFacet, Physics.cpp:25-39):
+     * 0 none, 1 translation with velocity motion_vector2 (m/s), 2 rotation about the axis
+     * through motion_vector1 (cm) with angular velocity vector motion_vector2 (rad/s).  The
+     * facet's velocity is added to a particle leaving a facet with is_moving set. */
+    int32_t  motion_type;
+    double   motion_vector1[3];
+    double   motion_vector2[3];
+    /* background-gas scattering (sp.scattering; PerformScatter, Particle.cpp:840-886): free
+     * paths exponential with mean scatter_mean_free_path_cm, impact parameter within
+     * scatter_rho, test/background mass ratio scatter_mass_ratio; with the cutoff on, a particle
+     * slower than scatter_cutoff_speed (m/s) after a collision ends */
+    int32_t  scatter_enabled;
+    int32_t  scatter_cutoff_enabled;
+    double   scatter_mass_ratio;
+    double   scatter_mean_free_path_cm;
+    double   scatter_rho;
+    double   scatter_cutoff_speed;
+    /* angle-map desorption (DES_ANGLEMAP; AnglemapGeneration.cpp): the recorded incident-angle
+     * counts of every facet with desorb_type MFG_DES_ANGLEMAP, in facet order, each
+     * anglemap_phi_width * (lower_res + higher_res) counts (theta-major, as recorded); NULL when
+     * no facet desorbs by angle map */
+    const uint64_t* desorb_anglemap;
 } mfg_model_desc;
 
 /*
@@ -224,7 +247,7 @@ typedef struct mfg_run_options {
     uint64_t seed;               /* Philox key; replaces MersenneTwister seeding (MolflowSimulation.cpp:44-55) */
     int32_t  block_size;         /* threads per block, 0 = autotuned default */
     int32_t  blocks_per_sm;      /* 0 = occupancy maximum */
-    int32_t  smem_bvh_nodes;     /* BVH nodes staged in shared memory, -1 = auto */
+    int32_t  reserved0;          /* set to 0 */
     double   time_limit_s;       /* kernel self-stops after this wall time (status MFG_ERR_TIMEOUT), 0 = 600 s */
     uint64_t max_steps_per_particle; /* a particle that exceeds this many bounces is dropped and counted, 0 = 2^40 */
     int32_t  use_graph;          /* 1: launch through a captured CUDA graph (captured once per launch shape) */

@@ -1,7 +1,7 @@
 """ctypes mirrors of the C structs declared in include/mfg.h (ABI version 1)."""
 import ctypes as C
 
-MFG_ABI_VERSION = 2
+MFG_ABI_VERSION = 3
 
 MFG_OK = 0
 MFG_ERR_INVALID_MODEL = 1
@@ -116,6 +116,16 @@ MODEL_DESC_FIELDS = [
     ("param_log_y", _u8),
     ("global_histogram", HistogramParams),
     ("facet_histogram", C.POINTER(HistogramParams)),
+    ("motion_type", C.c_int32),
+    ("motion_vector1", C.c_double * 3),
+    ("motion_vector2", C.c_double * 3),
+    ("scatter_enabled", C.c_int32),
+    ("scatter_cutoff_enabled", C.c_int32),
+    ("scatter_mass_ratio", C.c_double),
+    ("scatter_mean_free_path_cm", C.c_double),
+    ("scatter_rho", C.c_double),
+    ("scatter_cutoff_speed", C.c_double),
+    ("desorb_anglemap", _u64),
 ]
 
 
@@ -149,7 +159,7 @@ class RunOptions(C.Structure):
         ("seed", C.c_uint64),
         ("block_size", C.c_int32),
         ("blocks_per_sm", C.c_int32),
-        ("smem_bvh_nodes", C.c_int32),
+        ("reserved0", C.c_int32),
         ("time_limit_s", C.c_double),
         ("max_steps_per_particle", C.c_uint64),
         ("use_graph", C.c_int32),

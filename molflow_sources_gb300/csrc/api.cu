@@ -171,7 +171,9 @@ static int sim_upload(mfg_sim* s) {
     int rc;
 #define UP(vec, field) if ((rc = upload(s->owned, vec, &M.field)) != MFG_OK) return rc
     UP(h.nodes_d, nodes_d);
-    UP(h.nodes_f, nodes_f);
+    UP(h.nodes_c, nodes_c);
+    UP(h.prims_c, prims_c);
+    UP(h.roots_c, roots_c);
     UP(h.roots, roots);
     UP(h.prims, prims);
     UP(h.isect_d, isect_d);
@@ -220,6 +222,15 @@ static int sim_upload(mfg_sim* s) {
     M.low_flux = h.low_flux;
     M.pad4 = 0;
     M.low_flux_cutoff = h.low_flux_cutoff;
+    M.motion_type = h.motion_type;
+    M.scatter = h.scatter;
+    for (int k = 0; k < 3; ++k) { M.mv1[k] = h.mv1[k]; M.mv2[k] = h.mv2[k]; }
+    M.scatter_cutoff = h.scatter_cutoff;
+    M.pad5 = 0;
+    M.sc_mass_ratio = h.sc_mass_ratio;
+    M.sc_mfp = h.sc_mfp;
+    M.sc_rho = h.sc_rho;
+    M.sc_cutoff_speed = h.sc_cutoff_speed;
     M.ghist = h.ghist;
     M.hist_bins = h.layout.histogram_bins;
     {
@@ -420,7 +431,7 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     C.abort_flag = s->d_abort;
     if (sens) C.sens = s->sens;
     size_t fac_bytes = size_t(h.nf) * SF_N * 8;
-    C.smem_facets = fac_bytes <= 32 * 1024 ? 1 : 0;   // leaves room for 4 blocks per SM with their stacks
+    C.smem_facets = fac_bytes <= 32 * 1024 ? 1 : 0;   // leaves room for 4 blocks per SM
     size_t dyn = (TG_N + (C.smem_facets ? size_t(h.nf) * SF_N : 0)) * 8;
     if (o.block_size == 0 && o.blocks_per_sm == 0 && s->tuned_block[o.precision]) {
         o.block_size = s->tuned_block[o.precision];
@@ -428,7 +439,6 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     }
     int block = o.block_size > 0 ? o.block_size : 256;
     if (block % 32 || block > 256) return fail(MFG_ERR_INVALID_ARGUMENT, "block_size must be a multiple of 32, at most 256");
-    dyn += size_t(mfgk::kSmemStack) * size_t(block) * sizeof(int);   // shared-memory traversal stacks
     // kernel variant: FP64, or FP32R compiled for at least 2, 3 or 4 resident blocks per SM
     // (register budgets 128, 85, 64); blocks_per_sm selects the FP32R variant.  Models with
     // transparent or semi-transparent facets use the variants that keep a pass list (+100).
@@ -1019,7 +1029,7 @@ __global__ void noalloc_pass1(const __grid_constant__ DevModel M, int precision,
         return;
     }
     bool amb = false;
-    mfgk::HitF h = mfgk::trace_f(M, root, mfgk::make_ray_f(ox, oy, oz, (float)dx, (float)dy, (float)dz), last[i], amb,
+    mfgk::HitF h = mfgk::trace_f(M, M.roots_c[0], mfgk::make_ray_f(ox, oy, oz, (float)dx, (float)dy, (float)dz), last[i], amb,
                                  scratch + 1, nullptr, ocp);
     if (amb || h.f < 0) {   // queue the ray for the FP64 pass
         unsigned long long k = atomicAdd(scratch, 1ull);

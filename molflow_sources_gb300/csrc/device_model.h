@@ -20,11 +20,16 @@ struct __align__(16) NodeD {
     int32_t a, b;
     int32_t pad0, pad1;
 };
-// FP32 bounds rounded outward and padded by a scene-relative margin (32 B).
-struct __align__(16) NodeF {
-    float lo[3];
-    float hi[3];
-    int32_t a, b;
+// FP32 traversal node holding its two children's boxes, rounded outward and padded by a
+// scene-relative margin (64 B, four 16-byte loads), so one fetch decides which children to visit
+// and a missed child costs no fetch.  Child reference: >= 0 another NodeC, < 0 a leaf whose
+// facets are prims_c[-1 - ref ...] up to a -1 sentinel.  Every structure starts at a root NodeC
+// whose child 0 is the whole tree and child 1 an empty leaf far away.
+struct __align__(16) NodeC {
+    float lo0[3], hi0[3];
+    float lo1[3], hi1[3];
+    int32_t c0, c1;
+    int32_t pad0, pad1;
 };
 
 // Facet intersection record FP64 (128 B):
@@ -53,6 +58,7 @@ struct __align__(16) PolyF { float cu, cv, su, sv, rin2, rout2; int32_t vstart, 
 #define FF_DIFFUSE_ONLY 128u
 #define FF_FAST_REFL   256u   // diffuse, full accommodation, Maxwell speeds, no sojourn, constant temperature
 #define FF_LINK        512u   // structure link: the particle passes into structure FacetInfo2::link
+#define FF_MOVING      1024u  // moving facet: its velocity is added to particles leaving it
 
 // Per-facet physics record (FP64, 128 B).
 struct __align__(16) FacetPhysD {
@@ -148,7 +154,9 @@ struct DevModel {
     int32_t nf, nstruct;
     int32_t n_src, nm;
     const NodeD* nodes_d;
-    const NodeF* nodes_f;
+    const NodeC* nodes_c;          // FP32 two-child nodes (trace_f)
+    const int32_t* prims_c;        // leaf facet lists of nodes_c, each ended by -1
+    const int32_t* roots_c;        // root NodeC per structure
     const int32_t* roots;        // root node per structure
     const int32_t* prims;        // facet ids in leaf order
     const FacetIsectD* isect_d;
@@ -194,6 +202,12 @@ struct DevModel {
     int32_t has_ext;             // traced by the extended kernel variants (transparency, histograms, low flux)
     int32_t low_flux, pad4;      // low-flux mode (otfParams.lowFluxMode) and its cutoff weight
     double low_flux_cutoff;
+    // moving facets: motion type (1 translation, 2 rotation), axis base (cm), velocity or
+    // angular velocity vector
+    int32_t motion_type, scatter;   // scatter: background-gas collisions on
+    double mv1[3], mv2[3];
+    int32_t scatter_cutoff, pad5;
+    double sc_mass_ratio, sc_mfp, sc_rho, sc_cutoff_speed;
     // histograms recorded at absorptions: global set and per-facet sets, hist_bins per moment block
     HistDev ghist;
     const HistDev* fhist;        // [nf] or null

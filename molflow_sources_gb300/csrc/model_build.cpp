@@ -399,6 +399,19 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     m.half_life = d->half_life;
     m.low_flux = d->low_flux_mode;
     m.low_flux_cutoff = d->low_flux_cutoff;
+    m.motion_type = d->motion_type;
+    for (int k = 0; k < 3; ++k) { m.mv1[k] = d->motion_vector1[k]; m.mv2[k] = d->motion_vector2[k]; }
+    m.scatter = d->scatter_enabled;
+    m.scatter_cutoff = d->scatter_cutoff_enabled;
+    m.sc_mass_ratio = d->scatter_mass_ratio;
+    m.sc_mfp = d->scatter_mean_free_path_cm;
+    m.sc_rho = d->scatter_rho;
+    m.sc_cutoff_speed = d->scatter_cutoff_speed;
+    if (m.motion_type < 0 || m.motion_type > 2) { err = "motion type must be 0, 1 or 2"; return MFG_ERR_INVALID_MODEL; }
+    if (m.scatter && !(m.sc_mfp > 0 && m.sc_rho > 0 && m.sc_mass_ratio > 0)) {
+        err = "scattering needs a positive mean free path, collision radius and mass ratio";
+        return MFG_ERR_INVALID_MODEL;
+    }
     if (!(m.gas_mass > 0)) { err = "gas mass must be positive"; return MFG_ERR_INVALID_MODEL; }
     {
         const mfg_histogram_params& hp = d->global_histogram;
@@ -510,7 +523,6 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     for (int i = 0; i < nf; ++i) {
         std::string f = "facet " + std::to_string(i + 1) + ": ";
         if (m.teleport[i]) unsupported(f + "teleport");
-        if (m.moving[i]) unsupported(f + "moving facet");
         if (m.desorb_type[i] == MFG_DES_ANGLEMAP) unsupported(f + "angle-map desorption");
         if (m.p_temp[i] >= 0 && m.sojourn[i]) {}
     }
@@ -602,7 +614,9 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     m.roots.clear();
     m.prims.clear();
     m.nodes_d.clear();
-    m.nodes_f.clear();
+    m.nodes_c.clear();
+    m.roots_c.clear();
+    m.prims_c.clear();
     m.bvh_depth = 0;
     m.bvh_leaves = 0;
     const double pad64 = 1e-9 * m.scene_scale, pad32 = 2e-6 * m.scene_scale;
@@ -611,14 +625,22 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
         for (int i = 0; i < nf; ++i)
             if (m.structure[i] == -1 || m.structure[i] == s) ids.push_back(i);
         m.roots.push_back(int32_t(m.nodes_d.size()));
+        // root NodeC of the structure: child 0 = the whole tree (filled below), child 1 = an
+        // empty leaf whose box is a point far outside any scene
+        m.roots_c.push_back(int32_t(m.nodes_c.size()));
+        {
+            NodeC r{};
+            for (int a = 0; a < 3; ++a) { r.lo0[a] = r.hi0[a] = r.lo1[a] = r.hi1[a] = 1e30f; }
+            r.c0 = r.c1 = -1 - int32_t(m.prims_c.size());
+            m.prims_c.push_back(-1);
+            m.nodes_c.push_back(r);
+        }
         if (ids.empty()) {   // empty structure: one leaf with no facets and an empty box
             NodeD e{};
-            NodeF f{};
-            for (int a = 0; a < 3; ++a) { e.lo[a] = f.lo[a] = 1; e.hi[a] = f.hi[a] = -1; }
-            e.a = f.a = int32_t(m.prims.size());
-            e.b = f.b = -1;
+            for (int a = 0; a < 3; ++a) { e.lo[a] = 1; e.hi[a] = -1; }
+            e.a = int32_t(m.prims.size());
+            e.b = -1;
             m.nodes_d.push_back(e);
-            m.nodes_f.push_back(f);
             continue;
         }
         std::vector<BuildNode> tree;
@@ -644,12 +666,9 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
         for (size_t q = 0; q < order.size(); ++q) {
             const BuildNode& b = tree[order[q]];
             NodeD nd{};
-            NodeF nf32{};
             for (int a = 0; a < 3; ++a) {
                 nd.lo[a] = b.lo[a] - pad64;
                 nd.hi[a] = b.hi[a] + pad64;
-                nf32.lo[a] = round_down(b.lo[a] - pad32);
-                nf32.hi[a] = round_up(b.hi[a] + pad32);
             }
             if (b.left >= 0) {
                 nd.a = base + newidx[b.left];
@@ -659,12 +678,48 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
                 nd.b = -1 - b.count;
                 m.bvh_leaves++;
             }
-            nf32.a = nd.a;
-            nf32.b = nd.b;
             m.nodes_d.push_back(nd);
-            m.nodes_f.push_back(nf32);
         }
         for (int i : ids) m.prims.push_back(i);
+        // two-child FP32 layout, breadth-first over the internal nodes
+        {
+            const int croot = m.roots_c.back();
+            auto box32 = [&](const BuildNode& b, float* lo, float* hi) {
+                for (int a = 0; a < 3; ++a) { lo[a] = round_down(b.lo[a] - pad32); hi[a] = round_up(b.hi[a] + pad32); }
+            };
+            auto leaf_ref = [&](const BuildNode& b) {
+                const int32_t ref = -1 - int32_t(m.prims_c.size());
+                for (int k = 0; k < b.count; ++k) m.prims_c.push_back(ids[b.first + k]);
+                m.prims_c.push_back(-1);
+                return ref;
+            };
+            std::vector<int> inner;                 // tree indices of internal nodes, BFS order
+            std::vector<int32_t> cidx(tree.size(), -1);
+            if (tree[0].left >= 0) {
+                inner.push_back(0);
+                for (size_t q = 0; q < inner.size(); ++q) {
+                    const BuildNode& b = tree[inner[q]];
+                    for (int c : {b.left, b.right})
+                        if (tree[c].left >= 0) inner.push_back(c);
+                }
+            }
+            const int32_t cbase = int32_t(m.nodes_c.size());
+            for (size_t q = 0; q < inner.size(); ++q) cidx[inner[q]] = cbase + int32_t(q);
+            {
+                NodeC& r = m.nodes_c[croot];
+                box32(tree[0], r.lo0, r.hi0);
+                r.c0 = tree[0].left >= 0 ? cidx[0] : leaf_ref(tree[0]);
+            }
+            for (size_t q = 0; q < inner.size(); ++q) {
+                const BuildNode& b = tree[inner[q]];
+                NodeC nc{};
+                box32(tree[b.left], nc.lo0, nc.hi0);
+                box32(tree[b.right], nc.lo1, nc.hi1);
+                nc.c0 = tree[b.left].left >= 0 ? cidx[b.left] : leaf_ref(tree[b.left]);
+                nc.c1 = tree[b.right].left >= 0 ? cidx[b.right] : leaf_ref(tree[b.right]);
+                m.nodes_c.push_back(nc);
+            }
+        }
     }
 
     // device records
@@ -792,8 +847,10 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
                    (m.sojourn[i] ? FF_SOJOURN : 0) | (m.ang_off[i] >= 0 ? FF_ANGLEMAP : 0) |
                    (m.prof_idx[i] >= 0 ? FF_PROFILE : 0) | (m.diffuse[i] > 0.999999 ? FF_DIFFUSE_ONLY : 0) |
                    (m.link[i] ? FF_LINK : 0);
-        if (m.diffuse[i] > 0.999999 && m.accommodation[i] > 0.9999 && m.use_maxwell && !m.sojourn[i] && m.p_temp[i] < 0)
+        if (m.diffuse[i] > 0.999999 && m.accommodation[i] > 0.9999 && m.use_maxwell && !m.sojourn[i] && m.p_temp[i] < 0 &&
+            !m.moving[i])
             in.flags |= FF_FAST_REFL;
+        if (m.moving[i]) in.flags |= FF_MOVING;
         in.count = m.count[i];
         in.tex_off = int32_t(m.tex_off[i]);
         in.tex_w = m.tex_w[i];
@@ -826,7 +883,9 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     inst.src_total = m.src_total;
     inst.layout = m.layout;
     m.instances.assign(1, inst);
-    m.has_ext = m.has_transparent || m.layout.histogram_bins > 0 || m.low_flux;
+    bool any_moving = false;
+    for (int i = 0; i < nf; ++i) any_moving = any_moving || m.moving[i];
+    m.has_ext = m.has_transparent || m.layout.histogram_bins > 0 || m.low_flux || m.scatter || any_moving;
     return MFG_OK;
 }
 
@@ -845,6 +904,7 @@ int merge_host_models(const std::vector<const HostModel*>& parts, HostModel& out
     for (const HostModel* p : parts) {
         if (p->layout.histogram_bins > 0) { err = "histograms are not recorded in batched instances"; return MFG_ERR_UNSUPPORTED_FEATURE; }
         if (p->low_flux) { err = "low-flux mode is not traced in batched instances"; return MFG_ERR_UNSUPPORTED_FEATURE; }
+        if (p->scatter || p->motion_type) { err = "scattering and moving facets are not traced in batched instances"; return MFG_ERR_UNSUPPORTED_FEATURE; }
     }
     out = HostModel();
     out.nm = p0.nm;
@@ -878,11 +938,15 @@ int merge_host_models(const std::vector<const HostModel*>& parts, HostModel& out
             if (nd.b >= 0) nd.a += node_base; else nd.a += prim_base;
             out.nodes_d.push_back(nd);
         }
-        for (NodeF nd : p.nodes_f) {
-            if (nd.b >= 0) nd.a += node_base; else nd.a += prim_base;
-            out.nodes_f.push_back(nd);
-        }
         for (int r : p.roots) out.roots.push_back(r + node_base);
+        const int32_t cbase = int32_t(out.nodes_c.size()), pcbase = int32_t(out.prims_c.size());
+        for (NodeC nc : p.nodes_c) {
+            nc.c0 = nc.c0 >= 0 ? nc.c0 + cbase : nc.c0 - pcbase;
+            nc.c1 = nc.c1 >= 0 ? nc.c1 + cbase : nc.c1 - pcbase;
+            out.nodes_c.push_back(nc);
+        }
+        for (int r : p.roots_c) out.roots_c.push_back(r + cbase);
+        for (int f : p.prims_c) out.prims_c.push_back(f >= 0 ? f + in.facet_base : -1);
         for (int f : p.prims) out.prims.push_back(f + in.facet_base);
         out.isect_d.insert(out.isect_d.end(), p.isect_d.begin(), p.isect_d.end());
         out.isect_f.insert(out.isect_f.end(), p.isect_f.begin(), p.isect_f.end());

@@ -38,6 +38,9 @@ struct HostModel {
     std::vector<uint32_t> count;
     double gas_mass = 28, time_window = 1e-10, half_life = 1, low_flux_cutoff = 1e-7;
     int use_maxwell = 1, constant_flow = 1, enable_decay = 0, low_flux = 0;
+    int motion_type = 0, scatter = 0, scatter_cutoff = 0;
+    double mv1[3] = {0, 0, 0}, mv2[3] = {0, 0, 0};
+    double sc_mass_ratio = 1, sc_mfp = 1e30, sc_rho = 0, sc_cutoff_speed = 0;
     // derived
     double latest = 0;
     std::vector<double> mstart, mend;
@@ -59,7 +62,8 @@ struct HostModel {
     std::vector<double> tex_inc;          // 1/(cell area * sides) per texture cell
     // BVH (all structures concatenated, breadth-first per structure)
     std::vector<NodeD> nodes_d;
-    std::vector<NodeF> nodes_f;
+    std::vector<NodeC> nodes_c;           // FP32 two-child layout
+    std::vector<int32_t> roots_c, prims_c;
     std::vector<int32_t> roots, prims;
     int64_t bvh_depth = 0, bvh_leaves = 0;
     // device records

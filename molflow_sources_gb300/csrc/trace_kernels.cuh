@@ -183,6 +183,7 @@ struct ParticleState {
     double dist, gen_time;
     uint64_t refl;
     double ori;
+    double scat_at;        // flight distance (cm) of the next background-gas collision
 };
 
 // ProfileFacet (Particle.cpp:1026-1085); profiles are tallied in global memory
@@ -446,6 +447,60 @@ __device__ __noinline__ void record_histograms(const DevModel& M, const DevTally
     for_moments(M, time, add);
 }
 
+// TreatMovingFacet (Physics.cpp:25-39): the moving facet's local velocity (m/s; translation,
+// or rotation about the axis through mv1, position in cm) is added to the particle's
+template <class R>
+__device__ __noinline__ void treat_moving(const DevModel& M, double ox, double oy, double oz, R& dx, R& dy, R& dz, R& vel) {
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    if (M.motion_type == 1) {
+        ax = M.mv2[0]; ay = M.mv2[1]; az = M.mv2[2];
+    } else if (M.motion_type == 2) {
+        const double rx = 0.01 * (ox - M.mv1[0]), ry = 0.01 * (oy - M.mv1[1]), rz = 0.01 * (oz - M.mv1[2]);
+        ax = M.mv2[1] * rz - M.mv2[2] * ry;
+        ay = M.mv2[2] * rx - M.mv2[0] * rz;
+        az = M.mv2[0] * ry - M.mv2[1] * rx;
+    }
+    const double v = (double)vel;
+    const double wx = (double)dx * v + ax, wy = (double)dy * v + ay, wz = (double)dz * v + az;
+    const double n = sqrt(wx * wx + wy * wy + wz * wz);
+    dx = (R)(wx / n); dy = (R)(wy / n); dz = (R)(wz / n);
+    vel = (R)n;
+}
+
+// PerformScatter (Particle.cpp:840-886, Physics.cpp:41-63): collision with a background-gas
+// molecule at impact parameter b = rho sqrt(r); the direction turns by the scattering angle
+// about an orthonormal base built on the old direction; returns false when the particle fell
+// below the cutoff speed
+template <class Rng, class R>
+__device__ __noinline__ bool perform_scatter(const DevModel& M, Rng& rng, double dist, R& dx, R& dy, R& dz, R& vel,
+                                             double& scat_at) {
+    const double rho = M.sc_rho, mr = M.sc_mass_ratio;
+    const double b = rho * sqrt((double)rng.next());
+    const double a = sqrt(rho * rho - b * b);
+    const double ctg = 1.0 / (2.0 * a * b) * (rho * rho * mr + b * b - a * a);
+    const double theta = atan(1.0 / ctg);
+    const double phi = 2.0 * kPi * (double)rng.next();
+    const double d0 = (double)dx, d1 = (double)dy, d2 = (double)dz;
+    double r0 = 1.0, r1 = 0.0, r2 = 0.0;
+    if (d0 != 0.0) { r0 = 0.0; r2 = 1.0; }
+    else if (d1 != 0.0) { r2 = 1.0; }
+    double u0 = d1 * r2 - d2 * r1, u1 = d2 * r0 - d0 * r2, u2 = d0 * r1 - d1 * r0;
+    double l = sqrt(u0 * u0 + u1 * u1 + u2 * u2);
+    u0 /= l; u1 /= l; u2 /= l;
+    double v0 = d1 * u2 - d2 * u1, v1 = d2 * u0 - d0 * u2, v2 = d0 * u1 - d1 * u0;
+    l = sqrt(v0 * v0 + v1 * v1 + v2 * v2);
+    v0 /= l; v1 /= l; v2 /= l;
+    const double st = sin(theta), ct = cos(theta), sp = sin(phi), cp = cos(phi);
+    dx = (R)(st * cp * u0 + st * sp * v0 + ct * d0);
+    dy = (R)(st * cp * u1 + st * sp * v1 + ct * d1);
+    dz = (R)(st * cp * u2 + st * sp * v2 + ct * d2);
+    const double q = mr * rho / b * st;
+    const double v = (double)vel;
+    vel = (R)sqrt(v * v / (1.0 + q * q));
+    scat_at = dist - M.sc_mfp * log(1.0 - (double)rng.next());
+    return !(M.scatter_cutoff && (double)vel < M.sc_cutoff_speed);
+}
+
 // RegisterTransparentPass (Particle.cpp:1232-1257): crossing a transparent facet counts a hit
 // whose 1/v_ort and v_ort sums are doubled (the particle crosses, it does not turn back), on
 // the facet, its texture (countTrans), profile, direction cells and angle map, in the moment
@@ -568,8 +623,6 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
     B.sfac = C.smem_facets ? smem + TG_N : nullptr;
     const int nsm = TG_N + (C.smem_facets ? M.nf * SF_N : 0);
     for (int i = threadIdx.x; i < nsm; i += blockDim.x) smem[i] = 0ull;
-    // this thread's slice of the shared-memory traversal stacks, after the tally partials
-    int* smstk = reinterpret_cast<int*>(smem + nsm) + threadIdx.x;
     for (int i = threadIdx.x; i < MFG_MAXWELL_N; i += blockDim.x) {
         s_cdf_v[i] = M.cdf_v[i];
         s_cdf_p[i] = M.cdf_p[i];
@@ -734,6 +787,10 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
             }
             if (des) {
                 P.decay_at = M.enable_decay ? P.time - 1.44269 * M.half_life * log(1.0 - (double)rng.next()) : 1e100;
+                if constexpr (kExt) {
+                    // free path to the first background-gas collision (Particle.cpp:500-504)
+                    P.scat_at = M.scatter ? -M.sc_mfp * log(1.0 - (double)rng.next()) : 1e100;
+                }
                 // start point: rejection in the (u,v) rectangle, at most 1000 tries (Particle.cpp:513-570)
                 start_point<kFP32>(M, fo, rng, P.ox, P.oy, P.oz, pu, pv);
                 P.last = fo;
@@ -744,6 +801,9 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                 R r1 = (R)rng.next(), r2 = (R)rng.next();
                 R ct = law == 1 ? r1 : (law == 2 ? (R)pow((double)r1, 1.0 / ((double)lexp + 1.0)) : (R)sqrt(r1));
                 polar_dir<kFP32>(M, fo, ct, r2, flip, dx, dy, dz);
+            }
+            if constexpr (kExt) {
+                if (M.info[fo].flags & FF_MOVING) treat_moving(M, P.ox, P.oy, P.oz, dx, dy, dz, vel);
             }
             {
                 // outgoing tallies; a reflection's incoming half (pending) is added with them (moment 0)
@@ -816,13 +876,13 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
         }
         if constexpr (kFP32) {
             bool amb = false;
-            HitF h = trace_f<kExt>(M, root, make_ray_f(P.ox, P.oy, P.oz, (float)dx, (float)dy, (float)dz), P.last, amb,
-                                  T.global + TG_STATUS, tlp, ocp, smstk, blockDim.x);
+            HitF h = trace_f<kExt>(M, M.roots_c[P.structure], make_ray_f(P.ox, P.oy, P.oz, (float)dx, (float)dy, (float)dz), P.last, amb,
+                                  T.global + TG_STATUS, tlp, ocp);
             if (amb || h.f < 0) {
                 ++c_rechk;
                 if constexpr (kExt) tl.n = 0;
                 HitD hd = trace_d<R, kExt>(M, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last, T.global + TG_STATUS, tlp,
-                                          ocp, smstk, blockDim.x);
+                                          ocp);
                 hf = hd.f; ht = hd.t; hu = (R)hd.u; hv = (R)hd.v;
             } else {
                 hf = h.f;
@@ -836,8 +896,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                 ht = (double)h.t + (double)((float)r / (float)den);
             }
         } else {
-            HitD h = trace_d<R, kExt>(M, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last, T.global + TG_STATUS, tlp, ocp,
-                                      smstk, blockDim.x);
+            HitD h = trace_d<R, kExt>(M, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last, T.global + TG_STATUS, tlp, ocp);
             hf = h.f; ht = h.t; hu = (R)h.u; hv = (R)h.v;
         }
         if (hf < 0) {   // leak (Particle.cpp:387-392)
@@ -857,6 +916,10 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
             if (dd < travel) { travel = dd; event = 2; }
         }
         if constexpr (kExt) {
+            if (M.scatter) {   // background-gas collision (Particle.cpp:281-287)
+                const double ds = P.scat_at - P.dist;
+                if (ds < travel) { travel = ds; event = 3; }
+            }
             for (int k = 0; k < tl.n; ++k) {
                 if (!((double)tl.t[k] < travel)) continue;
                 double ort_t = transparent_pass<kFP32>(M, T, B, tl.f[k], tl.t[k], tl.u[k], tl.v[k], P.time, vel, dx, dy, dz);
@@ -873,11 +936,112 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
         else P.time += travel / 100.0 / (double)vel;
         unsigned long long qdist = kFP32 ? qf((float)travel, (float)MFG_SCALE_DIST) : qd(travel, MFG_SCALE_DIST);
         c_dist += qdist;
+        if constexpr (kExt) {
+            if (event == 3) {   // PerformScatter: counted as a hit, then a new flight from here
+                c_distf += qdist;
+                P.dist += travel;
+                ++c_hits;
+                if (M.low_flux)
+                    lf_counts(M, T, 0, P.time, 0.0, 0.0, -1, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, P.ori, 0.0);
+                ++P.refl;
+                if (!perform_scatter(M, rng, P.dist, dx, dy, dz, vel, P.scat_at)) { need_new = true; continue; }
+                P.last = -1;
+                relink = true;
+                need_new = false;
+                if (++P.bounces > max_steps) {
+                    ++c_drop;
+                    relink = false;
+                    need_new = true;
+                }
+                continue;
+            }
+        }
         if (event != 0) { need_new = true; continue; }
         c_distf += qdist;
         if constexpr (kExt) P.dist += travel;
         // ---- 4. stick or reflect at facet hf (Particle.cpp:323-357) ----
         const FacetInfo& In = M.info[hf];
+        if constexpr (!kExt) {
+            // plain variants: stick or reflect (Particle.cpp:323-357), one tally path per hit
+            bool absorb;
+            R cosn;
+            if (kFP32) {
+                const float s = (In.flags & FF_STICK_PARAM) ? (float)param_at(M, M.info2[hf].stick_param, P.time) : M.phys_f[hf].sticking;
+                absorb = (s == 1.0f) || (s > 0.0f && (float)rng.next() < s);
+                cosn = fabsf(dx * M.phys_f[hf].N[0] + dy * M.phys_f[hf].N[1] + dz * M.phys_f[hf].N[2]);
+            } else {
+                const FacetIsectD& Rh = M.isect_d[hf];
+                const double s = (In.flags & FF_STICK_PARAM) ? param_at(M, M.info2[hf].stick_param, P.time) : M.phys_d[hf].sticking;
+                absorb = (s == 1.0) || (s > 0.0 && (double)rng.next() < s);
+                cosn = (R)fabs(ddx * Rh.v[0] + ddy * Rh.v[1] + ddz * Rh.v[2]);
+            }
+            const R ort = vel * cosn;
+            const unsigned long long q1 = kFP32 ? qf(1.0f / (float)ort, (float)MFG_SCALE_INV) : qd(1.0 / (double)ort, MFG_SCALE_INV);
+            const unsigned long long q2 = kFP32 ? qf((float)ort, (float)MFG_SCALE_V) : qd((double)ort, MFG_SCALE_V);
+            const unsigned long long q3 = kFP32 ? qf(1.0f / (float)vel, (float)MFG_SCALE_INV) : qd(1.0 / (double)vel, MFG_SCALE_INV);
+            pu = hu;
+            pv = hv;
+            ++c_hits;
+            if (!absorb && (In.flags & FF_LINK)) {
+                // structure link (PerformBounce, Particle.cpp:698-724)
+                transparent_pass<kFP32>(M, T, B, hf, (R)0, hu, hv, P.time, vel, dx, dy, dz, true);
+                P.structure = M.info2[hf].link;
+                relink = true;
+                need_new = false;
+                if (++P.bounces > max_steps) {
+                    ++c_drop;
+                    relink = false;
+                    need_new = true;
+                }
+                continue;
+            }
+            const int cell = (In.tex_off >= 0 && (In.count & (absorb ? MFG_COUNT_ABS : MFG_COUNT_REFL))) ? texture_cell<kFP32>(M, hf, hu, hv) : -1;
+            if (In.flags & FF_ANGLEMAP) anglemap_add(M, T, hf, ddx, ddy, ddz);
+            if (In.count & MFG_COUNT_DIR)
+                direction_add(M, T, hf, (double)hu, (double)hv, P.time, ddx * (double)vel, ddy * (double)vel, ddz * (double)vel);
+            if (kSens) {
+                int g = C.sens.gauge_of_facet[hf];
+                if (g >= 0) sens_output(C.sens, traj, ntraj, src_idx, g, (double)ort);   // incoming half / absorption
+                int k = C.sens.param_of_facet[hf];
+                if (absorb) {
+                    if (C.sens.pump_of_facet[hf]) {
+                        sens_output(C.sens, traj, ntraj, src_idx, MFG_SENS_NOUT - 1, 1.0);
+                        if (k >= 0) atomicAdd(C.sens.B + (size_t)k * MFG_SENS_NOUT + MFG_SENS_NOUT - 1, 1.0);
+                    }
+                } else if (k >= 0) {
+                    if (ntraj < MFG_SENS_TRAJ) traj[ntraj++] = k;
+                    else if (ntraj == MFG_SENS_TRAJ) { atomicAdd(C.sens.overflow, 1ull); ++ntraj; }
+                }
+            }
+            if (absorb) {   // RecordAbsorb (Particle.cpp:888-924)
+                ++c_abs;
+                facet_add(M, T, B, hf, 0, 1, 0, 1, 2 * q1, q2, q3);
+                if (cell >= 0) cell_add(T.texture + (size_t)cell * TT_N, 1, 2 * q1, q2);
+                if (In.flags & FF_PROFILE) profile_add(M, T, hf, 0, true, 2, 1, (double)cosn, (double)vel, (double)hu, (double)hv, q1, q2);
+                if (M.nm)
+                    tally_moments(M, T, B, hf, P.time, 0, 1, 1, 2 * q1, q2, q3, cell, 1, 2 * q1, q2, true, 2, 1,
+                                  (double)cosn, (double)vel, (double)hu, (double)hv, q1, q2);
+                need_new = true;
+            } else {        // incoming half of PerformBounce (Particle.cpp:735-767)
+                if (In.flags & FF_PROFILE) profile_add(M, T, hf, 0, true, 1, 1, (double)cosn, (double)vel, (double)hu, (double)hv, q1, q2);
+                if (M.nm)
+                    tally_moments(M, T, B, hf, P.time, 0, 1, 0, q1, q2, q3, cell, 1, q1, q2, true, 1, 1,
+                                  (double)cosn, (double)vel, (double)hu, (double)hv, q1, q2);
+                P.last = hf;
+                pend = true;
+                pend_s1ov = q1;
+                pend_svort = q2;
+                pend_s1v = q3;
+                pend_cell = cell;
+                need_new = false;
+                if (++P.bounces > max_steps) {   // step cap: count the hit, drop the particle
+                    flush_pending();
+                    ++c_drop;
+                    need_new = true;
+                }
+            }
+            continue;
+        }
         // sticking; the regular mode draws stick or reflect (Particle.cpp:323-336), low-flux mode
         // splits the particle into an absorbed part wa and a reflected part wr (:338-356)
         bool do_abs, do_refl;
@@ -964,6 +1128,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
             // with its direction, speed and last-hit facet (PerformBounce, Particle.cpp:698-724)
             transparent_pass<kFP32>(M, T, B, hf, (R)0, hu, hv, P.time, vel, dx, dy, dz, true, wr);
             P.structure = M.info2[hf].link;
+            if (In.flags & FF_MOVING) treat_moving(M, P.ox, P.oy, P.oz, dx, dy, dz, vel);
             relink = true;
             need_new = false;
             if (++P.bounces > max_steps) {   // step cap
@@ -1060,7 +1225,7 @@ __global__ void replay_kernel(const __grid_constant__ DevModel M, int precision,
         hit_t[i] = h.f >= 0 ? h.t : -1.0;
     } else {
         bool amb = false;
-        HitF h = trace_f(M, root, make_ray_f(ox, oy, oz, (float)dx, (float)dy, (float)dz), last[i], amb, status,
+        HitF h = trace_f(M, M.roots_c[0], make_ray_f(ox, oy, oz, (float)dx, (float)dy, (float)dz), last[i], amb, status,
                          nullptr, ocp);
         if (amb || h.f < 0) {
             atomicAdd(rechecks, 1ull);

@@ -14,25 +14,13 @@
 namespace mfgk {
 
 constexpr int kStack = 64;
-constexpr int kSmemStack = 24;   // stack entries kept in shared memory by the tracer kernel
-
-// Traversal stack of one thread: the first kSmemStack entries in shared memory (entry k at
-// sm[k * stride], so a warp's accesses to one level fall in distinct banks), deeper entries and
-// every entry of callers without a shared-memory slice (sm null) in local memory.
+// Traversal stack of one thread (local memory; a shared-memory copy of the first levels was
+// measured 0-5 % slower, as it takes L1 capacity from the BVH nodes).
 struct TravStack {
-    int* sm;
-    int stride;
     int sp;
     int loc[kStack];
-    __device__ __forceinline__ void push(int v) {
-        if (sm && sp < kSmemStack) sm[sp * stride] = v;
-        else loc[sp] = v;
-        ++sp;
-    }
-    __device__ __forceinline__ int pop() {
-        --sp;
-        return (sm && sp < kSmemStack) ? sm[sp * stride] : loc[sp];
-    }
+    __device__ __forceinline__ void push(int v) { loc[sp++] = v; }
+    __device__ __forceinline__ int pop() { return loc[--sp]; }
 };
 
 // InterpolateY (no extrapolation) for time-dependent parameters
@@ -134,16 +122,13 @@ struct HitD {
 template <class LT = double, bool kTr = true>
 __device__ __noinline__ HitD trace_d(const DevModel& M, int root, double ox, double oy, double oz,
                                      double dx, double dy, double dz, int last, unsigned long long* status,
-                                     TranspList<LT>* tl = nullptr, const OpacCtx* oc = nullptr,
-                                     int* smstk = nullptr, int sstride = 0) {
+                                     TranspList<LT>* tl = nullptr, const OpacCtx* oc = nullptr) {
     HitD h;
     h.f = -1;
     h.t = 1.0e99;
     h.u = h.v = 0;
     double ix = 1.0 / dx, iy = 1.0 / dy, iz = 1.0 / dz;
     TravStack stk;
-    stk.sm = smstk;
-    stk.stride = sstride;
     stk.sp = 0;
     int node = root;
     while (true) {
@@ -251,7 +236,7 @@ __device__ __forceinline__ RayF make_ray_f(double ox, double oy, double oz, floa
 template <bool kTr = true>
 __device__ __noinline__ HitF trace_f(const DevModel& M, int root, const RayF& ray, int last, bool& ambiguous,
                                      unsigned long long* status, TranspList<float>* tl = nullptr,
-                                     const OpacCtx* oc = nullptr, int* smstk = nullptr, int sstride = 0) {
+                                     const OpacCtx* oc = nullptr) {
     HitF h;
     h.f = -1;
     h.t = 3.0e38f;
@@ -261,31 +246,45 @@ __device__ __noinline__ HitF trace_f(const DevModel& M, int root, const RayF& ra
     const float ox = ray.ohx, oy = ray.ohy, oz = ray.ohz;
     float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
     TravStack stk;
-    stk.sm = smstk;
-    stk.stride = sstride;
     stk.sp = 0;
-    int node = root;
+    // `root` is the structure's root NodeC; ref >= 0 a NodeC, < 0 a leaf list in prims_c
+    int ref = root;
     while (true) {
-        const NodeF nd = M.nodes_f[node];
-        float tx0 = (nd.lo[0] - ox) * ix, tx1 = (nd.hi[0] - ox) * ix;
-        float ty0 = (nd.lo[1] - oy) * iy, ty1 = (nd.hi[1] - oy) * iy;
-        float tz0 = (nd.lo[2] - oz) * iz, tz1 = (nd.hi[2] - oz) * iz;
-        float tmin = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.0f));
-        float tmax = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), h.t + 2.0f * htol));
-        bool hit = tmin <= tmax * 1.0000005f;
-        if (hit && nd.b >= 0) {
-            int near = nd.a, far = nd.a + 1;
-            float dax = nd.b == 0 ? dx : (nd.b == 1 ? dy : dz);
-            if (dax < 0) { near = nd.a + 1; far = nd.a; }
-            if (stk.sp < kStack) stk.push(far);
-            else atomicOr(status, KS_STACK);
-            node = near;
+        if (ref >= 0) {
+            // both children's boxes in one 64-byte node
+            const float4* np = reinterpret_cast<const float4*>(M.nodes_c + ref);
+            const float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
+            const float tcap = h.t + 2.0f * htol;
+            float a0 = (q0.x - ox) * ix, a1 = (q0.w - ox) * ix;
+            float b0 = (q0.y - oy) * iy, b1 = (q1.x - oy) * iy;
+            float c0 = (q0.z - oz) * iz, c1 = (q1.y - oz) * iz;
+            const float tmin0 = fmaxf(fmaxf(fminf(a0, a1), fminf(b0, b1)), fmaxf(fminf(c0, c1), 0.0f));
+            const float tmax0 = fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fminf(fmaxf(c0, c1), tcap));
+            a0 = (q1.z - ox) * ix; a1 = (q2.y - ox) * ix;
+            b0 = (q1.w - oy) * iy; b1 = (q2.z - oy) * iy;
+            c0 = (q2.x - oz) * iz; c1 = (q2.w - oz) * iz;
+            const float tmin1 = fmaxf(fmaxf(fminf(a0, a1), fminf(b0, b1)), fmaxf(fminf(c0, c1), 0.0f));
+            const float tmax1 = fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fminf(fmaxf(c0, c1), tcap));
+            const bool hit0 = tmin0 <= tmax0 * 1.0000005f, hit1 = tmin1 <= tmax1 * 1.0000005f;
+            const int r0 = __float_as_int(q3.x), r1 = __float_as_int(q3.y);
+            if (hit0 && hit1) {
+                // nearer box first
+                const bool first0 = tmin0 <= tmin1;
+                if (stk.sp < kStack) stk.push(first0 ? r1 : r0);
+                else atomicOr(status, KS_STACK);
+                ref = first0 ? r0 : r1;
+            } else if (hit0 || hit1) {
+                ref = hit0 ? r0 : r1;
+            } else {
+                if (stk.sp == 0) break;
+                ref = stk.pop();
+            }
             continue;
         }
-        if (hit) {
-            int cnt = -1 - nd.b;
-            for (int k = 0; k < cnt; ++k) {
-                int f = M.prims[nd.a + k];
+        {
+            for (int k = -1 - ref;; ++k) {
+                const int f = M.prims_c[k];
+                if (f < 0) break;
                 if (f == last) continue;
                 const FacetIsectF& R = M.isect_f[f];
                 float Nx = R.v[0], Ny = R.v[1], Nz = R.v[2];
@@ -347,7 +346,7 @@ __device__ __noinline__ HitF trace_f(const DevModel& M, int root, const RayF& ra
             }
         }
         if (stk.sp == 0) break;
-        node = stk.pop();
+        ref = stk.pop();
     }
     return h;
 }

@@ -89,6 +89,19 @@ class Model:
         self.moment_time = np.zeros(0)
         self.moment_window = np.zeros(0)
         self.params = []   # list of (t array, v array, logx, logy)
+        # sp.motionType / motionVector1 / motionVector2 (moving facets)
+        self.motion_type = 0
+        self.motion_vector1 = (0.0, 0.0, 0.0)
+        self.motion_vector2 = (0.0, 0.0, 0.0)
+        # sp.scattering (background-gas collisions)
+        self.scatter_enabled = 0
+        self.scatter_mass_ratio = 1.0
+        self.scatter_mean_free_path_cm = 1e30
+        self.scatter_rho = 1e-8
+        self.scatter_cutoff_enabled = 0
+        self.scatter_cutoff_speed = 0.0
+        # recorded angle maps of the facets that desorb by angle map: {facet: uint64 counts}
+        self.desorb_anglemaps = {}
         # sp.globalHistogramParams
         self.global_histogram = dict(record=0, bounce_binsize=1, bounce_max=0, distance_binsize=1.0,
                                      distance_max=0.0, time_binsize=1.0, time_max=0.0)
@@ -156,6 +169,25 @@ class Model:
         d.param_v = p(pv, C.c_double)
         d.param_log_x = p(np.array([x[2] for x in self.params] or [0], np.uint8), C.c_uint8)
         d.param_log_y = p(np.array([x[3] for x in self.params] or [0], np.uint8), C.c_uint8)
+        d.motion_type = int(self.motion_type)
+        d.motion_vector1 = (C.c_double * 3)(*map(float, self.motion_vector1))
+        d.motion_vector2 = (C.c_double * 3)(*map(float, self.motion_vector2))
+        d.scatter_enabled = int(self.scatter_enabled)
+        d.scatter_cutoff_enabled = int(self.scatter_cutoff_enabled)
+        d.scatter_mass_ratio = float(self.scatter_mass_ratio)
+        d.scatter_mean_free_path_cm = float(self.scatter_mean_free_path_cm)
+        d.scatter_rho = float(self.scatter_rho)
+        d.scatter_cutoff_speed = float(self.scatter_cutoff_speed)
+        am_facets = [i for i in range(self.n_facets) if self.desorb_type[i] == A.DES_ANGLEMAP]
+        if am_facets:
+            parts = []
+            for i in am_facets:
+                n = int(self.anglemap_phi_width[i]) * int(self.anglemap_theta_lower_res[i] + self.anglemap_theta_higher_res[i])
+                a = np.zeros(n, np.uint64)
+                src = np.asarray(self.desorb_anglemaps.get(i, []), np.uint64).ravel()
+                a[:min(n, src.size)] = src[:n]
+                parts.append(a)
+            d.desorb_anglemap = p(np.concatenate(parts), C.c_uint64)
         gh = A.HistogramParams()
         for k in HIST_FIELDS:
             setattr(gh, k, type(getattr(gh, k))(self.global_histogram[k]))

@@ -76,7 +76,7 @@ class SensitivityFunction:
     def forward(self, n, precision=A.PREC_FP32R, seed=0x4D6F6C66):
         out = np.zeros(N_OUT)
         st = A.RunStats()
-        o = A.RunOptions(precision=precision, seed=seed, smem_bvh_nodes=-1)
+        o = A.RunOptions(precision=precision, seed=seed)
         _check(load_library().mfg_sens_forward(self.sim.h, int(n), C.byref(o), A.ptr(out, C.c_double), C.byref(st)))
         self.last_stats = {f: getattr(st, f) for f, _ in A.RunStats._fields_}
         return out

@@ -191,7 +191,7 @@ class GpuSimulation:
         if not time_limit_s:
             time_limit_s = float(os.environ.get("MFG_TIME_LIMIT_S", "0"))
         o = A.RunOptions(precision=precision, seed=seed, block_size=block_size, blocks_per_sm=blocks_per_sm,
-                         smem_bvh_nodes=-1, time_limit_s=time_limit_s, max_steps_per_particle=max_steps)
+                         time_limit_s=time_limit_s, max_steps_per_particle=max_steps)
         st = A.RunStats()
         rc = load_library().mfg_run(self.h, int(n_desorptions), C.byref(o), C.byref(st))
         self.last_stats = {f: getattr(st, f) for f, _ in A.RunStats._fields_}
@@ -213,7 +213,7 @@ class GpuSimulation:
         return {"block_size": o.block_size, "blocks_per_sm": o.blocks_per_sm}
 
     def run_async(self, n_desorptions, precision=A.PREC_FP64, seed=0x4D6F6C66, time_limit_s=0.0):
-        o = A.RunOptions(precision=precision, seed=seed, smem_bvh_nodes=-1, time_limit_s=time_limit_s)
+        o = A.RunOptions(precision=precision, seed=seed, time_limit_s=time_limit_s)
         _check(load_library().mfg_run_async(self.h, int(n_desorptions), C.byref(o)))
 
     def poll(self):
@@ -306,7 +306,7 @@ class GpuBatch:
         if not time_limit_s:
             time_limit_s = float(os.environ.get("MFG_TIME_LIMIT_S", "0"))
         o = A.RunOptions(precision=precision, seed=seed, block_size=block_size, blocks_per_sm=blocks_per_sm,
-                         smem_bvh_nodes=-1, time_limit_s=time_limit_s, use_graph=int(bool(use_graph)))
+                         time_limit_s=time_limit_s, use_graph=int(bool(use_graph)))
         st = A.RunStats()
         rc = load_library().mfg_run_batch(self.h, A.ptr(c, C.c_uint64), C.byref(o), C.byref(st))
         self.last_stats = {f: getattr(st, f) for f, _ in A.RunStats._fields_}

@@ -221,6 +221,20 @@ def load(path_or_bytes, with_state=True, catalog=()):
                 m.anglemap_theta_limit[k] = _f(am, "thetaLimit", 1.570796326)
                 m.anglemap_theta_lower_res[k] = _i(am, "thetaLowerRes")
                 m.anglemap_theta_higher_res[k] = _i(am, "thetaHigherRes")
+        # a recorded angle map in the facet node sets the map parameters and is the source of
+        # angle-map desorption; without one, angle-map desorption falls back to none
+        # (LoaderXML.cpp:1043-1073)
+        gam = f.find("IncidentAngleMap")
+        if gam is not None and gam.find("map") is not None and gam.get("angleMapThetaLimit") is not None:
+            m.anglemap_phi_width[k] = _i(gam, "angleMapPhiWidth")
+            m.anglemap_theta_limit[k] = _f(gam, "angleMapThetaLimit")
+            m.anglemap_theta_lower_res[k] = _i(gam, "angleMapThetaLowerRes")
+            m.anglemap_theta_higher_res[k] = _i(gam, "angleMapThetaHigherRes")
+            if m.desorb_type[k] == A.DES_ANGLEMAP:
+                txt = gam.find("map").text or ""
+                m.desorb_anglemaps[k] = np.array([int(float(x)) for x in txt.split()], np.uint64)
+        elif m.desorb_type[k] == A.DES_ANGLEMAP:
+            m.desorb_type[k] = A.DES_NONE
         hp = _hist_params(f.find("Histograms"))
         for key, val in hp.items():
             getattr(m, "hist_" + key)[k] = val
@@ -238,6 +252,25 @@ def load(path_or_bytes, with_state=True, catalog=()):
     if sims is not None:
         gas = sims.find("Gas")
         m.gas_mass = _f(gas, "mass", 28.0)
+        sc = gas.find("Scattering") if gas is not None else None
+        if sc is not None:   # LoaderXML.cpp:106-116 (the collision radius is not in the file)
+            m.scatter_enabled = _i(sc, "enabled")
+            m.scatter_mass_ratio = _f(sc, "massRatio", 1.0)
+            m.scatter_mean_free_path_cm = _f(sc, "meanFreePath_cm", 1e30)
+            co = sc.find("LowSpeedCutoff")
+            if co is not None:
+                m.scatter_cutoff_enabled = _i(co, "enabled")
+                m.scatter_cutoff_speed = _f(co, "speed")
+        mo = sims.find("Motion")   # LoaderXML.cpp:144-160
+        if mo is not None:
+            m.motion_type = _i(mo, "type")
+            if m.motion_type == 1:
+                v = mo.find("VelocityVector")
+                m.motion_vector2 = (_f(v, "vx"), _f(v, "vy"), _f(v, "vz"))
+            elif m.motion_type == 2:
+                b, r = mo.find("AxisBasePoint"), mo.find("RotationVector")
+                m.motion_vector1 = (_f(b, "x"), _f(b, "y"), _f(b, "z"))
+                m.motion_vector2 = (_f(r, "x"), _f(r, "y"), _f(r, "z"))
         m.enable_decay = _i(gas, "enableDecay")
         m.half_life = _f(gas, "halfLife", 1.0)
         lf = sims.find("LowFluxMode")

@@ -180,7 +180,7 @@ typedef struct {
     double sticking, opacity, outgassing, temperature, sqrtT, accommodation;
     int desorb_type; double desorb_exp;
     double diffuse, specular, cos_exp;
-    int two_sided, structure, link, teleport;
+    int two_sided, structure, link, teleport, moving;
     double texw_p, texh_p; int texw, texh; uint32_t count;
     int profile_type; double max_speed;
     int am_record, am_phi, am_lo, am_hi; double am_limit;
@@ -190,6 +190,7 @@ typedef struct {
     long tex_off, dir_off, ang_off; int prof_idx;
     /* desorption */
     int id_idx;            /* integrated desorption table index, -1 none */
+    struct oamap* amd;     /* angle-map desorption tables, NULL unless DES_ANGLEMAP */
 } ofacet;
 
 typedef struct { double bmin[3], bmax[3]; int left, right, first, count; } onode;
@@ -219,6 +220,209 @@ static void hist_init(ohist* h, const mfg_histogram_params* p) {
     if (p->record & MFG_HIST_TIME) h->nt = (long)(size_t)(p->time_max / p->time_binsize) + 1;
 }
 
+/* ------------------------------------------------- angle-map desorption --
+ * Tables built from a recorded incident-angle map (MolflowSimFacet::InitializeAngleMap,
+ * MolflowSimFacet.cpp:90-215) and the theta / phi generation of AnglemapGeneration.cpp:14-257.
+ * The map has `lo` theta lines below thetaLimit and `hi` above, `w` phi bins per line.  CDFs are
+ * sampled at bin midpoints; between midpoints the pdf is interpolated linearly, so the CDF is
+ * inverted on a parabola. */
+typedef struct oamap {
+    int w, lo, hi; double limit;
+    double *tcdf_lo, *tcdf_hi;     /* theta CDF at each line's midpoint */
+    double *sum_lo, *sum_hi;       /* counts per theta line */
+    double *pcdf_lo, *pcdf_hi;     /* phi CDF at each bin midpoint, per line */
+    double *ppdf_lo, *ppdf_hi;     /* phi pdf per line, normalised to the line */
+    double lower_ratio, total;
+} oamap;
+
+static void oamap_free(oamap* a) {
+    if (!a) return;
+    free(a->tcdf_lo); free(a->tcdf_hi); free(a->sum_lo); free(a->sum_hi);
+    free(a->pcdf_lo); free(a->pcdf_hi); free(a->ppdf_lo); free(a->ppdf_hi);
+    free(a);
+}
+
+/* returns NULL (all-zero map) or the tables */
+static oamap* oamap_build(const uint64_t* pdf, int w, int lo, int hi, double limit) {
+    oamap* a = (oamap*)calloc(1, sizeof(oamap));
+    a->w = w; a->lo = lo; a->hi = hi; a->limit = limit;
+    a->tcdf_lo = (double*)calloc(lo + 1, sizeof(double)); a->tcdf_hi = (double*)calloc(hi + 1, sizeof(double));
+    a->sum_lo = (double*)calloc(lo + 1, sizeof(double)); a->sum_hi = (double*)calloc(hi + 1, sizeof(double));
+    a->pcdf_lo = (double*)calloc((size_t)w * lo + 1, sizeof(double)); a->pcdf_hi = (double*)calloc((size_t)w * hi + 1, sizeof(double));
+    a->ppdf_lo = (double*)calloc((size_t)w * lo + 1, sizeof(double)); a->ppdf_hi = (double*)calloc((size_t)w * hi + 1, sizeof(double));
+    double slo = 0, sall;
+    for (int t = 0; t < lo; ++t) { for (int k = 0; k < w; ++k) a->sum_lo[t] += (double)pdf[(size_t)t * w + k]; slo += a->sum_lo[t]; }
+    sall = slo;
+    for (int t = 0; t < hi; ++t) { for (int k = 0; k < w; ++k) a->sum_hi[t] += (double)pdf[(size_t)(lo + t) * w + k]; sall += a->sum_hi[t]; }
+    if (sall == 0) { oamap_free(a); return NULL; }
+    a->total = sall;
+    a->lower_ratio = slo / sall;
+    const double tn = 1.0 / sall;
+    for (int part = 0; part < 2; ++part) {
+        const int n = part ? hi : lo, base = part ? lo : 0;
+        double* tcdf = part ? a->tcdf_hi : a->tcdf_lo;
+        double* sum = part ? a->sum_hi : a->sum_lo;
+        double* pcdf = part ? a->pcdf_hi : a->pcdf_lo;
+        double* ppdf = part ? a->ppdf_hi : a->ppdf_lo;
+        for (int t = 0; t < n; ++t) {
+            if (t == 0) tcdf[0] = (part ? a->lower_ratio : 0.0) + 0.5 * sum[0] * tn;
+            else tcdf[t] = tcdf[t - 1] + (sum[t - 1] + sum[t]) * 0.5 * tn;
+            const double pn = 1.0 / sum[t];
+            const uint64_t* line = pdf + (size_t)(base + t) * w;
+            for (int k = 0; k < w; ++k) {
+                const size_t i = (size_t)t * w + k;
+                if (sum[t] == 0) {   /* empty line: uniform phi */
+                    pcdf[i] = (0.5 + k) / (double)w;
+                    ppdf[i] = 1.0 / (double)w;
+                } else {
+                    pcdf[i] = (k == 0) ? 0.5 * (double)line[0] * pn : pcdf[i - 1] + (double)(line[k - 1] + line[k]) * 0.5 * pn;
+                    ppdf[i] = (double)line[k] * pn;
+                }
+            }
+        }
+    }
+    return a;
+}
+
+static inline double am_weigh(double a, double b, double w) { return a + w * (b - a); }
+/* last index with v[i] <= key, -1 below the first */
+static int am_lower_index(double key, const double* v, int n) {
+    int lo = 0, hi = n;
+    while (lo < hi) { int mid = (lo + hi) >> 1; if (v[mid] <= key) lo = mid + 1; else hi = mid; }
+    return lo - 1;
+}
+/* the same on the line interpolated between a and b with weight w */
+static int am_weighed_lower_index(double key, double w, const double* a, const double* b, int n) {
+    int lo = 0, hi = n;
+    while (lo < hi) { int mid = (lo + hi) >> 1; if (am_weigh(a[mid], b[mid], w) <= key) lo = mid + 1; else hi = mid; }
+    return lo - 1;
+}
+static inline int am_circ(int i, int n) { return ((i % n) + n) % n; }
+static double am_theta(const oamap* a, double ti) {
+    if ((size_t)ti < (size_t)a->lo) return a->limit * ti / (double)a->lo;
+    return a->limit + (PI_D / 2.0 - a->limit) * (ti - (double)a->lo) / (double)a->hi;
+}
+static double am_phi(const oamap* a, double pi) {
+    const double w = (double)a->w;
+    const double c = (pi < w) ? pi : pi - w;
+    return -PI_D + 2.0 * PI_D * c / w;
+}
+static double am_phi_pdf(const oamap* a, double ti, int pli) {
+    const int w = a->w, lo = a->lo, hi = a->hi;
+    const int k = am_circ(pli, w);
+    if (ti < 0.5) return lo > 0 ? a->ppdf_lo[k] : a->ppdf_hi[k];
+    if (ti > (double)(lo + hi) - 0.5) return hi > 0 ? a->ppdf_hi[(size_t)w * (hi - 1) + k] : a->ppdf_lo[(size_t)w * (lo - 1) + k];
+    const size_t tl = (size_t)(ti - 0.5);
+    const double ov = ti - 0.5 - (double)tl;
+    const double v0 = tl < (size_t)lo ? a->ppdf_lo[tl * w + k] : a->ppdf_hi[(tl - lo) * w + k];
+    const size_t tn = tl + 1;
+    const double v1 = tn < (size_t)lo ? a->ppdf_lo[tn * w + k] : a->ppdf_hi[(tn - lo) * w + k];
+    return am_weigh(v0, v1, ov);
+}
+static double am_phi_cdf(const oamap* a, double ti, int pli) {
+    const int w = a->w, lo = a->lo, hi = a->hi;
+    const double* c = (ti < (double)lo) ? a->pcdf_lo : a->pcdf_hi;
+    const int base = (ti < (double)lo) ? 0 : lo, n = (ti < (double)lo) ? lo : hi;
+    size_t line0, line1;
+    double ov = 0.0;
+    if (ti < (double)base + 0.5) { line0 = line1 = 0; }
+    else if (ti > (double)(base + n) - 0.5) { line0 = line1 = (size_t)(n - 1); }
+    else {
+        const size_t tl = (size_t)(ti - 0.5);
+        ov = ti - 0.5 - (double)tl;
+        line0 = tl - base; line1 = line0 + 1;
+    }
+    const double v0 = pli < w ? c[line0 * w + pli] : 1.0 + c[line0 * w];
+    const double v1 = pli < w ? c[line1 * w + pli] : 1.0 + c[line1 * w];
+    return line0 == line1 ? v0 : am_weigh(v0, v1, ov);
+}
+/* GenerateThetaFromAngleMap (AnglemapGeneration.cpp:14-109) */
+static double am_gen_theta(const oamap* a, double r, int* out_i, double* out_ov) {
+    const int lo = a->lo, hi = a->hi;
+    int i; double ov, th;
+    const int upper = !(r < a->lower_ratio);
+    const double* tc = upper ? a->tcdf_hi : a->tcdf_lo;
+    const double* sm = upper ? a->sum_hi : a->sum_lo;
+    const int base = upper ? lo : 0, n = upper ? hi : lo;
+    i = base + am_lower_index(r, tc, n);
+    if (i == base - 1) {   /* below the first midpoint of the part */
+        if (!upper) { ov = 0.5 * r / tc[0]; th = am_theta(a, ov); }
+        else { ov = 0.5 * (r - a->lower_ratio) / (tc[0] - a->lower_ratio); th = am_theta(a, (double)lo + ov); }
+    } else if (i == base + n - 1) {   /* above the last midpoint of the part */
+        const double top = upper ? 1.0 : a->lower_ratio;
+        ov = 0.5 * (r - tc[i - base]) / (top - tc[i - base]);
+        th = am_theta(a, (double)i + 0.5 + ov);
+    } else {
+        const int j = i - base;
+        if (sm[j] == sm[j + 1]) {
+            ov = (r - tc[j]) / (tc[j + 1] - tc[j]);
+        } else {
+            const double step = am_theta(a, (double)i + 1.5) - am_theta(a, (double)i + 0.5);
+            const double c = tc[j];
+            const double b = sm[j] / a->total / step;
+            const double aa = 0.5 * (sm[j + 1] - sm[j]) / a->total / (step * step);
+            const double dy = r - c;
+            const double dx = (-b + sqrt(b * b + 4 * aa * dy)) / (2 * aa);
+            ov = dx / step;
+        }
+        th = am_theta(a, (double)i + 0.5 + ov);
+    }
+    *out_i = i; *out_ov = ov;
+    return th;
+}
+/* GeneratePhiFromAngleMap (AnglemapGeneration.cpp:120-248) */
+static double am_gen_phi(const oamap* a, int i, double tov, double r) {
+    const int w = a->w, lo = a->lo, hi = a->hi;
+    if (w == 1) return -PI_D + 2.0 * PI_D * r;
+    int pi; double weigh;
+    if (i < lo) {
+        if (i == -1) {
+            r += a->pcdf_lo[0];
+            pi = am_lower_index(r, a->pcdf_lo, w);
+            weigh = tov;
+        } else if (i == lo - 1) {
+            r += a->pcdf_lo[(size_t)i * w];
+            pi = am_lower_index(r, a->pcdf_lo + (size_t)i * w, w);
+            weigh = tov;
+        } else {
+            const double div = a->sum_lo[i] * (1.0 - tov) + a->sum_lo[i + 1] * tov;
+            weigh = div > 0.0 ? tov * a->sum_lo[i + 1] / div : tov;
+            r += am_weigh(a->pcdf_lo[(size_t)i * w], a->pcdf_lo[(size_t)(i + 1) * w], weigh);
+            pi = am_weighed_lower_index(r, weigh, a->pcdf_lo + (size_t)i * w, a->pcdf_lo + (size_t)(i + 1) * w, w);
+        }
+    } else {
+        const int j = i - lo;
+        if (i == lo + hi - 1) {
+            r += a->pcdf_hi[(size_t)j * w];
+            pi = am_lower_index(r, a->pcdf_hi + (size_t)j * w, w);
+            weigh = tov;
+        } else {
+            const double div = a->sum_hi[j] * (1.0 - tov) + a->sum_hi[j + 1] * tov;
+            weigh = div > 0.0 ? tov * a->sum_hi[j + 1] / div : tov;
+            r += am_weigh(a->pcdf_hi[(size_t)j * w], a->pcdf_hi[(size_t)(j + 1) * w], weigh);
+            pi = am_weighed_lower_index(r, weigh, a->pcdf_hi + (size_t)j * w, a->pcdf_hi + (size_t)(j + 1) * w, w);
+        }
+    }
+    const double ti = (double)i + 0.5 + weigh;
+    double pov;
+    if (pi == -1) {
+        pov = 0.5 * r / am_phi_cdf(a, ti, 0);
+        return am_phi(a, pov);
+    }
+    const double p0 = am_phi_pdf(a, ti, pi), p1 = am_phi_pdf(a, ti, pi + 1);
+    const double c0 = am_phi_cdf(a, ti, pi);
+    if (p0 == p1) {
+        pov = (r - c0) / (am_phi_cdf(a, ti, pi + 1) - c0);
+    } else {
+        const double step = 2.0 * PI_D / (double)w;
+        const double b = p0 / step, aa = 0.5 * (p1 - p0) / (step * step), dy = r - c0;
+        const double D = b * b + 4 * aa * dy;
+        if (D < 0) pov = (r - c0) / (am_phi_cdf(a, ti, am_circ(pi + 1, w)) - c0);
+        else pov = ((-b + sqrt(D)) / (2 * aa)) / step;
+    }
+    return am_phi(a, (double)pi + 0.5 + pov);
+}
+
 struct orc_model {
     int nf, nstruct;
     ofacet* f;
@@ -235,6 +439,9 @@ struct orc_model {
     int nparams; oparam* params;
     int nid; oid* ids;
     double* src_prefix; int* src_facet; int nsrc; double src_total;
+    int motion_type; double mv1[3], mv2[3];                 /* moving facets */
+    int scatter, scatter_cutoff;                            /* background-gas scattering */
+    double sc_mass_ratio, sc_mfp, sc_rho, sc_cutoff_speed;
     ohist ghist;           /* global histograms; offset 0 of each moment block */
     ohist* fhist;          /* per facet, NULL when no facet records */
     mfg_state_layout L;
@@ -553,8 +760,14 @@ int orc_model_create(const mfg_model_desc* d, orc_model** out, char* err, size_t
     M->v2 = (double*)malloc(sizeof(double) * 2 * (nvt + 1));
     M->constant_flow = d->constant_flow; M->use_maxwell = d->use_maxwell;
     M->low_flux = d->low_flux_mode; M->low_flux_cutoff = d->low_flux_cutoff;
+    M->motion_type = d->motion_type;
+    for (int k = 0; k < 3; ++k) { M->mv1[k] = d->motion_vector1[k]; M->mv2[k] = d->motion_vector2[k]; }
+    M->scatter = d->scatter_enabled; M->scatter_cutoff = d->scatter_cutoff_enabled;
+    M->sc_mass_ratio = d->scatter_mass_ratio; M->sc_mfp = d->scatter_mean_free_path_cm;
+    M->sc_rho = d->scatter_rho; M->sc_cutoff_speed = d->scatter_cutoff_speed;
     M->decay = d->enable_decay; M->half_life = d->half_life; M->gas_mass = d->gas_mass;
     char msg[256];
+    size_t am_cursor = 0;   /* position in desc->desorb_anglemap */
     for (int i = 0; i < M->nf; ++i) {
         ofacet* F = &M->f[i];
         F->vstart = d->facet_vertex_start[i];
@@ -605,8 +818,19 @@ int orc_model_create(const mfg_model_desc* d, orc_model** out, char* err, size_t
             orc_model_destroy(M);
             return MFG_ERR_INVALID_MODEL;
         }
-        if (F->teleport || OPT(d->is_moving, i, 0) || F->desorb_type == MFG_DES_ANGLEMAP) {
-            snprintf(msg, sizeof msg, "facet %d: teleport/moving/angle-map desorption not traced by the oracle", i + 1);
+        F->moving = OPT(d->is_moving, i, 0);
+        if (F->desorb_type == MFG_DES_ANGLEMAP) {
+            const int w = F->am_phi, lo = F->am_lo, hi = F->am_hi;
+            const uint64_t* map = d->desorb_anglemap ? d->desorb_anglemap + am_cursor : NULL;
+            if (w > 0 && lo >= 0 && hi >= 0 && lo + hi > 0) am_cursor += (size_t)w * (lo + hi);
+            if (map && w > 0 && lo >= 0 && hi >= 0 && lo + hi > 0) F->amd = oamap_build(map, w, lo, hi, F->am_limit);
+            if (!F->amd) {
+                snprintf(msg, sizeof msg, "facet %d desorbs by angle map but has no recorded angle map", i + 1);
+                set_err(err, errlen, msg); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL;
+            }
+        }
+        if (F->teleport) {
+            snprintf(msg, sizeof msg, "facet %d: teleport not traced by the oracle", i + 1);
             set_err(err, errlen, msg); orc_model_destroy(M); return MFG_ERR_UNSUPPORTED_FEATURE;
         }
         if (F->structure < -1 || F->structure >= M->nstruct) { set_err(err, errlen, "structure index out of range"); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL; }
@@ -744,7 +968,7 @@ int orc_model_create(const mfg_model_desc* d, orc_model** out, char* err, size_t
 
 void orc_model_destroy(orc_model* M) {
     if (!M) return;
-    free(M->f); free(M->v2); free(M->texinc);
+    free(M->v2); free(M->texinc);
     if (M->nodes) for (int s = 0; s < M->nstruct; ++s) { free(M->nodes[s]); free(M->prims[s]); }
     free(M->nodes); free(M->prims); free(M->nnodes);
     free(M->mstart); free(M->mend);
@@ -754,6 +978,8 @@ void orc_model_destroy(orc_model* M) {
     free(M->ids);
     free(M->src_prefix); free(M->src_facet);
     free(M->fhist);
+    if (M->f) for (int i = 0; i < M->nf; ++i) oamap_free(M->f[i].amd);
+    free(M->f);
     free(M);
 }
 
@@ -875,7 +1101,7 @@ typedef struct {
 
 typedef struct {
     double o[3], d[3];
-    double time, velocity, ori, dist, gen_time, decay_at;
+    double time, velocity, ori, dist, gen_time, decay_at, scatter_at;
     int last, structure;
     uint64_t bounces;
     double u, v;   /* facetHitDetails of the current facet */
@@ -1022,6 +1248,23 @@ static double temperature_at(const orc_model* M, const ofacet* F, double t) {
 }
 
 /* StartFromSource (Particle.cpp:407-685) for facets without outgassing maps. */
+/* TreatMovingFacet (Physics.cpp:25-39): the moving facet's local velocity (m/s) is added to the
+ * particle's; position in cm, rotation axis base in cm, angular velocity in rad/s */
+static void treat_moving(const orc_model* M, opart* P) {
+    double add[3] = {0, 0, 0};
+    if (M->motion_type == 1) {
+        for (int k = 0; k < 3; ++k) add[k] = M->mv2[k];
+    } else if (M->motion_type == 2) {
+        double dv[3] = {0.01 * (P->o[0] - M->mv1[0]), 0.01 * (P->o[1] - M->mv1[1]), 0.01 * (P->o[2] - M->mv1[2])};
+        cross3(M->mv2, dv, add);
+    }
+    double w[3];
+    for (int k = 0; k < 3; ++k) w[k] = P->d[k] * P->velocity + add[k];
+    double n = sqrt(dot3(w, w));
+    for (int k = 0; k < 3; ++k) P->d[k] = w[k] / n;
+    P->velocity = n;
+}
+
 static int start_from_source(const orc_model* M, otally* T, rng_t* r, opart* P) {
     double sr = rnd(r) * M->src_total;
     int lo = 0, hi = M->nsrc;   /* first k with prefix[k] > sr */
@@ -1043,6 +1286,8 @@ static int start_from_source(const orc_model* M, otally* T, rng_t* r, opart* P) 
         double tau = 1.44269 * M->half_life;
         P->decay_at = P->time - tau * log(1.0 - rnd(r));
     } else P->decay_at = 1e100;
+    /* free path to the first background-gas collision (Particle.cpp:500-504) */
+    P->scatter_at = M->scatter ? -M->sc_mfp * log(1.0 - rnd(r)) : 1e100;
     P->bounces = 0; P->dist = 0;
     int found = 0;
     for (int tries = 0; tries < 1000 && !found; ++tries) {
@@ -1057,10 +1302,20 @@ static int start_from_source(const orc_model* M, otally* T, rng_t* r, opart* P) 
     switch (F->desorb_type) {
         case MFG_DES_UNIFORM: th = acos(rnd(r)); ph = rnd(r) * 2.0 * PI_D; break;
         case MFG_DES_COSINE_N: th = acos(pow(rnd(r), 1.0 / (F->desorb_exp + 1.0))); ph = rnd(r) * 2.0 * PI_D; break;
+        case MFG_DES_ANGLEMAP: {   /* the map holds incident angles: leave at pi - theta (Particle.cpp:598-622) */
+            int ti; double tov;
+            const double r1 = rnd(r);
+            th = am_gen_theta(F->amd, r1, &ti, &tov);
+            ph = am_gen_phi(F->amd, ti, tov, rnd(r));
+            th = PI_D - th;
+            reverse = 0;
+            break;
+        }
         default: th = acos(sqrt(rnd(r))); ph = rnd(r) * 2.0 * PI_D; break;
     }
     polar_to_cart(F, th, ph, reverse, P->d);
     P->structure = F->structure;
+    if (F->moving) treat_moving(M, P);
     T->global[MFG_G_NBDESORBED] += 1.0;
     double ort = P->velocity * fabs(dot3(P->d, F->N));
     int ms[256]; int nms = moments_of(M, P->time, ms, 256);
@@ -1163,6 +1418,7 @@ static void perform_bounce(const orc_model* M, otally* T, int fi, rng_t* r, opar
         if (F->count & MFG_COUNT_TRANS) texture_hit(M, T, ms, nms, F, P, 1, 2.0, 2.0);
         if ((F->count & MFG_COUNT_DIR) && F->dir_off >= 0) direction_hit(M, T, ms, nms, F, P);
         P->structure = F->link - 1;
+        if (F->moving) treat_moving(M, P);
         return;
     }
     int revert = F->two_sided ? (dot3(P->d, F->N) > 0.0) : 0;
@@ -1197,6 +1453,7 @@ static void perform_bounce(const orc_model* M, otally* T, int fi, rng_t* r, opar
             polar_to_cart(F, th, ph, revert, P->d);
         }
     }
+    if (F->moving) treat_moving(M, P);
     ort = P->velocity * fabs(dot3(P->d, F->N));
     facet_counter(M, T, ms, nms, fi, 0, 0, 0, 1.0 / ort, vf * ort, P);
     if (F->count & MFG_COUNT_REFL) texture_hit(M, T, ms, nms, F, P, 0, 1.0, 1.0);
@@ -1222,6 +1479,37 @@ static void tally_free(otally* T) {
 }
 
 /* trace one particle to absorption/leak: the body of SimulationMCStep (Particle.cpp:221-393) */
+/* PerformScatter (Particle.cpp:840-886, Physics.cpp:41-63): collision with a background-gas
+ * molecule; returns 0 when the particle fell below the cutoff speed */
+static int perform_scatter(const orc_model* M, otally* T, rng_t* r, opart* P) {
+    T->global[MFG_G_NBMCHIT] += 1; T->global[MFG_G_NBHITEQUIV] += P->ori;
+    P->bounces++;
+    const double rho = M->sc_rho, mr = M->sc_mass_ratio;
+    const double b = rho * sqrt(rnd(r));
+    const double a = sqrt(rho * rho - b * b);
+    const double ctg = 1.0 / (2.0 * a * b) * (rho * rho * mr + b * b - a * a);
+    const double theta = atan(1.0 / ctg);
+    const double phi = 2.0 * PI_D * rnd(r);
+    double rv[3] = {1.0, 0.0, 0.0};
+    if (P->d[0] != 0.0) { rv[0] = 0.0; rv[2] = 1.0; }
+    else if (P->d[1] != 0.0) { rv[2] = 1.0; }
+    double un[3], vn[3];
+    cross3(P->d, rv, un);
+    double l = sqrt(dot3(un, un));
+    for (int k = 0; k < 3; ++k) un[k] /= l;
+    cross3(P->d, un, vn);
+    l = sqrt(dot3(vn, vn));
+    for (int k = 0; k < 3; ++k) vn[k] /= l;
+    const double st = sin(theta), ct = cos(theta), sp = sin(phi), cp = cos(phi);
+    double nd[3];
+    for (int k = 0; k < 3; ++k) nd[k] = st * cp * un[k] + st * sp * vn[k] + ct * P->d[k];
+    for (int k = 0; k < 3; ++k) P->d[k] = nd[k];
+    const double q = mr * rho / b * st;
+    P->velocity = sqrt(P->velocity * P->velocity / (1.0 + q * q));
+    P->scatter_at = P->dist - M->sc_mfp * log(1.0 - rnd(r));
+    return !(M->scatter_cutoff && P->velocity < M->sc_cutoff_speed);
+}
+
 static int trace_particle(const orc_model* M, otally* T, rng_t* r, uint64_t max_steps, orc_stats* st,
                           int64_t* nrec, int64_t maxrec, double* ro, double* rd, int32_t* rl, int32_t* rh, double* rt) {
     opart P;
@@ -1254,10 +1542,21 @@ static int trace_particle(const orc_model* M, otally* T, rng_t* r, uint64_t max_
             double dd = P.velocity * 100.0 * (P.decay_at - P.time);
             if (dd < travel) { travel = dd; event = 2; }
         }
+        if (M->scatter) {   /* background-gas collision (Particle.cpp:281-287) */
+            double ds = P.scatter_at - P.dist;
+            if (ds < travel) { travel = ds; event = 3; }
+        }
         for (int k = 0; k < H.ntr; ++k)
             if (H.tr[k].t < travel) transparent_pass(M, T, H.tr[k].facet, &H.tr[k], &P);
         for (int a = 0; a < 3; ++a) P.o[a] = P.o[a] + travel * P.d[a];
         P.time += travel / 100.0 / P.velocity;
+        if (event == 3) {
+            T->global[MFG_G_DIST_TOTAL] += travel; T->global[MFG_G_DIST_FULLHITS] += travel; P.dist += travel;
+            st->hits++;
+            if (!perform_scatter(M, T, r, &P)) return 0;
+            P.last = -1;   /* any facet may be hit after a volume collision */
+            continue;
+        }
         if (event != 0) {
             T->global[MFG_G_DIST_TOTAL] += travel;
             return 0;
