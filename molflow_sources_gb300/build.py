@@ -15,7 +15,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libmfg.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["api.cu", "model_build.cpp"]
-DEPS = SOURCES + ["trace_kernels.cuh", "traversal.cuh", "philox.cuh", "device_model.h", "model_build.h"]
+DEPS = SOURCES + ["trace_kernels.cuh", "traversal.cuh", "philox.cuh", "anglemap_gen.cuh", "device_model.h",
+                  "model_build.h"]
 
 
 def nvcc():

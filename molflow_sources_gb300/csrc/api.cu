@@ -201,6 +201,9 @@ static int sim_upload(mfg_sim* s) {
     UP(h.par_logx, par_logx);
     UP(h.par_logy, par_logy);
     UP(h.fhist, fhist);
+    UP(h.am_of_facet, am_of_facet);
+    UP(h.am_dev, am_dev);
+    UP(h.am_pool, am_pool);
 #undef UP
     M.src_total = h.src_total;
     M.latest = h.latest;

@@ -140,6 +140,16 @@ struct __align__(16) FacetInfo2 {
 #define KS_STACK 8ull
 #define KS_TRANSP 16ull   // more transparent passes on one ray than the pass list holds
 
+// Angle-map desorption tables of one source facet (built from its recorded incident-angle map,
+// MolflowSimFacet.cpp:90-215): `lo` theta lines below the limit, `hi` above, `w` phi bins; the
+// offsets index DevModel::am_pool
+struct AmDev {
+    int32_t w, lo, hi, pad;
+    double limit, lower_ratio, total;
+    int32_t tcdf_lo, tcdf_hi, sum_lo, sum_hi;      // theta CDF at line midpoints, line sums
+    int32_t pcdf_lo, pcdf_hi, ppdf_lo, ppdf_hi;    // phi CDFs at bin midpoints, phi pdfs
+};
+
 // one histogram set (RecordHistograms, Particle.cpp:926-975): bin sizes, bin counts (0 = not
 // recorded) and offset of the set in a moment block (-1 = none)
 struct HistDev {
@@ -211,6 +221,9 @@ struct DevModel {
     // histograms recorded at absorptions: global set and per-facet sets, hist_bins per moment block
     HistDev ghist;
     const HistDev* fhist;        // [nf] or null
+    const int32_t* am_of_facet;  // angle-map desorption table of each facet (-1 none), or null
+    const AmDev* am_dev;
+    const double* am_pool;
     int64_t hist_bins;
     double scene_scale;          // max |coordinate| of the scene (for FP32 tolerances)
     // instances of a batch (one for a plain model): source-table range and total weight

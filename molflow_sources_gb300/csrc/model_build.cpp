@@ -523,7 +523,6 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     for (int i = 0; i < nf; ++i) {
         std::string f = "facet " + std::to_string(i + 1) + ": ";
         if (m.teleport[i]) unsupported(f + "teleport");
-        if (m.desorb_type[i] == MFG_DES_ANGLEMAP) unsupported(f + "angle-map desorption");
         if (m.p_temp[i] >= 0 && m.sojourn[i]) {}
     }
 
@@ -558,6 +557,70 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     L.n_profile = B * L.profile_facets * MFG_PROFILE_SIZE * 3;
     L.n_direction = B * L.direction_cells * 4;
     L.n_anglemap = L.anglemap_cells;
+    // angle-map desorption: midpoint CDFs and normalised phi pdfs of each source facet's recorded
+    // map (MolflowSimFacet::InitializeAngleMap, MolflowSimFacet.cpp:90-215)
+    m.am_of_facet.clear();
+    m.am_dev.clear();
+    m.am_pool.clear();
+    {
+        size_t cursor = 0;
+        for (int i = 0; i < nf; ++i) {
+            if (m.desorb_type[i] != MFG_DES_ANGLEMAP) continue;
+            if (m.am_of_facet.empty()) m.am_of_facet.assign(nf, -1);
+            const int w = m.am_phi[i], lo = m.am_lo[i], hi = m.am_hi[i];
+            if (!(w > 0 && lo >= 0 && hi >= 0 && lo + hi > 0) || !d->desorb_anglemap) {
+                err = "facet " + std::to_string(i + 1) + " desorbs by angle map but has no recorded angle map";
+                return MFG_ERR_INVALID_MODEL;
+            }
+            const uint64_t* pdf = d->desorb_anglemap + cursor;
+            cursor += size_t(w) * (lo + hi);
+            AmDev a{};
+            a.w = w; a.lo = lo; a.hi = hi; a.limit = m.am_limit[i];
+            std::vector<double> sum_lo(lo), sum_hi(hi);
+            double slo = 0, sall = 0;
+            for (int t = 0; t < lo; ++t) { for (int k = 0; k < w; ++k) sum_lo[t] += double(pdf[size_t(t) * w + k]); slo += sum_lo[t]; }
+            sall = slo;
+            for (int t = 0; t < hi; ++t) { for (int k = 0; k < w; ++k) sum_hi[t] += double(pdf[size_t(lo + t) * w + k]); sall += sum_hi[t]; }
+            if (sall == 0) {
+                err = "facet " + std::to_string(i + 1) + " has an all-zero recorded angle map but desorbs by it";
+                return MFG_ERR_INVALID_MODEL;
+            }
+            a.total = sall;
+            a.lower_ratio = slo / sall;
+            auto put = [&](const std::vector<double>& v) { int32_t o = int32_t(m.am_pool.size()); m.am_pool.insert(m.am_pool.end(), v.begin(), v.end()); m.am_pool.push_back(0.0); return o; };
+            std::vector<double> tcdf_lo(lo), tcdf_hi(hi), pcdf_lo(size_t(w) * lo), pcdf_hi(size_t(w) * hi),
+                ppdf_lo(size_t(w) * lo), ppdf_hi(size_t(w) * hi);
+            const double tn = 1.0 / sall;
+            for (int part = 0; part < 2; ++part) {
+                const int n = part ? hi : lo, base = part ? lo : 0;
+                std::vector<double>& tcdf = part ? tcdf_hi : tcdf_lo;
+                const std::vector<double>& sum = part ? sum_hi : sum_lo;
+                std::vector<double>& pcdf = part ? pcdf_hi : pcdf_lo;
+                std::vector<double>& ppdf = part ? ppdf_hi : ppdf_lo;
+                for (int t = 0; t < n; ++t) {
+                    tcdf[t] = t == 0 ? (part ? a.lower_ratio : 0.0) + 0.5 * sum[0] * tn : tcdf[t - 1] + (sum[t - 1] + sum[t]) * 0.5 * tn;
+                    const double pn = 1.0 / sum[t];
+                    const uint64_t* line = pdf + size_t(base + t) * w;
+                    for (int k = 0; k < w; ++k) {
+                        const size_t q = size_t(t) * w + k;
+                        if (sum[t] == 0) {   // empty line: uniform phi
+                            pcdf[q] = (0.5 + k) / double(w);
+                            ppdf[q] = 1.0 / double(w);
+                        } else {
+                            pcdf[q] = k == 0 ? 0.5 * double(line[0]) * pn : pcdf[q - 1] + double(line[k - 1] + line[k]) * 0.5 * pn;
+                            ppdf[q] = double(line[k]) * pn;
+                        }
+                    }
+                }
+            }
+            a.tcdf_lo = put(tcdf_lo); a.tcdf_hi = put(tcdf_hi);
+            a.sum_lo = put(sum_lo); a.sum_hi = put(sum_hi);
+            a.pcdf_lo = put(pcdf_lo); a.pcdf_hi = put(pcdf_hi);
+            a.ppdf_lo = put(ppdf_lo); a.ppdf_hi = put(ppdf_hi);
+            m.am_of_facet[i] = int32_t(m.am_dev.size());
+            m.am_dev.push_back(a);
+        }
+    }
     // histograms: global set at offset 0, then each recording facet's (bounce, distance, time);
     // bin counts restated from the sizes the reference stores with its histograms
     auto hist_of = [](const mfg_histogram_params& p, HistDev& h) {
@@ -885,7 +948,7 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     m.instances.assign(1, inst);
     bool any_moving = false;
     for (int i = 0; i < nf; ++i) any_moving = any_moving || m.moving[i];
-    m.has_ext = m.has_transparent || m.layout.histogram_bins > 0 || m.low_flux || m.scatter || any_moving;
+    m.has_ext = m.has_transparent || m.layout.histogram_bins > 0 || m.low_flux || m.scatter || any_moving || !m.am_dev.empty();
     return MFG_OK;
 }
 
@@ -904,7 +967,10 @@ int merge_host_models(const std::vector<const HostModel*>& parts, HostModel& out
     for (const HostModel* p : parts) {
         if (p->layout.histogram_bins > 0) { err = "histograms are not recorded in batched instances"; return MFG_ERR_UNSUPPORTED_FEATURE; }
         if (p->low_flux) { err = "low-flux mode is not traced in batched instances"; return MFG_ERR_UNSUPPORTED_FEATURE; }
-        if (p->scatter || p->motion_type) { err = "scattering and moving facets are not traced in batched instances"; return MFG_ERR_UNSUPPORTED_FEATURE; }
+        if (p->scatter || p->motion_type || !p->am_dev.empty()) {
+            err = "scattering, moving facets and angle-map desorption are not traced in batched instances";
+            return MFG_ERR_UNSUPPORTED_FEATURE;
+        }
     }
     out = HostModel();
     out.nm = p0.nm;

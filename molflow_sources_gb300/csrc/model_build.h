@@ -81,6 +81,9 @@ struct HostModel {
     double scene_scale = 1;
     int has_transparent = 0;
     int has_ext = 0;                      // needs the extended kernel variants
+    std::vector<int32_t> am_of_facet;     // angle-map desorption tables (empty: none)
+    std::vector<AmDev> am_dev;
+    std::vector<double> am_pool;
     HistDev ghist{};                      // histograms (off -1: none)
     std::vector<HistDev> fhist;           // per facet, empty when no facet records
     bool gpu_supported = true;

@@ -124,6 +124,7 @@ __device__ __forceinline__ float interp_x_f(float y, const float* xs, const floa
 }  // namespace mfgk
 
 #include "traversal.cuh"
+#include "anglemap_gen.cuh"
 
 namespace mfgk {
 
@@ -311,7 +312,9 @@ __device__ __noinline__ double desorption_time(const DevModel& M, int idt, doubl
     return interp_x_d(r * M.id_cum[e - 1], M.id_t + s, M.id_cum + s, e - s);
 }
 
-// point-in-polygon in FP32 for start points (FP32R kernel)
+// point-in-polygon in FP32 for start points (FP32R kernel).  A point within rounding distance of
+// an edge is decided in FP64: a start point just outside its polygon would, on a source whose rim
+// lies on the walls (a tube's inlet disk), start the particle outside the walls.
 __device__ __forceinline__ bool in_facet_f(const DevModel& M, int f, float u, float v) {
     const PolyF P = M.poly_f[f];
     if (P.rin2 > 1e29f) return true;
@@ -319,17 +322,9 @@ __device__ __forceinline__ bool in_facet_f(const DevModel& M, int f, float u, fl
     float r2 = du * du + dv * dv;
     if (r2 < P.rin2) return true;
     if (r2 > P.rout2) return false;
-    bool in = false;
-    float2 pj = M.v2_f[P.vstart + P.nv - 1];
-    for (int i = 0; i < P.nv; ++i) {
-        float2 pi = M.v2_f[P.vstart + i];
-        if ((pi.y > v) != (pj.y > v)) {
-            float cr = (pj.x - pi.x) * (v - pi.y) - (u - pi.x) * (pj.y - pi.y);
-            if ((cr > 0) == (pj.y > pi.y)) in = !in;
-        }
-        pj = pi;
-    }
-    return in;
+    bool amb = false;
+    const bool in = edge_inside_f(M, P, u, v, 4e-7f * fmaxf(P.su, P.sv), amb);
+    return amb ? in_facet_d(M, f, (double)u, (double)v) : in;
 }
 
 // Start point of a desorption: uniform (u,v) in the bounding rectangle until inside the polygon,
@@ -726,6 +721,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
             const bool des = want;
             int fo, law;              // law: 0 cosine, 1 uniform, 2 cos^N, 3 general reflection
             bool flip = false;
+            bool amdes = false;   // extended variants: direction from the source's recorded angle map
             R lexp = 0;
             if (des) {
                 int inst = 0;
@@ -762,6 +758,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                     if (src_idx >= 0) atomicAdd(C.sens.src_count + src_idx, 1ull);
                 }
                 law = I2.desorb_type == MFG_DES_UNIFORM ? 1 : (I2.desorb_type == MFG_DES_COSINE_N ? 2 : 0);
+                if constexpr (kExt) amdes = I2.desorb_type == MFG_DES_ANGLEMAP;
                 lexp = (R)I2.desorb_exp;
                 if (!M.use_maxwell) law |= 4;   // fixed speed 145.469 sqrt(T/m) (Particle.cpp:483)
             } else {
@@ -797,6 +794,11 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
             }
             if (law == 3) {
                 reflect_general<kFP32>(M, fo, flip, rng, P.time, vel, dx, dy, dz, s_cdf_v, s_cdf_p, s_cdf_vf, s_cdf_pf);
+            } else if (amdes) {
+                const double r1 = (double)rng.next(), r2 = (double)rng.next();
+                double ax, ay, az;
+                am_direction(M, fo, r1, r2, ax, ay, az);
+                dx = (R)ax; dy = (R)ay; dz = (R)az;
             } else {
                 R r1 = (R)rng.next(), r2 = (R)rng.next();
                 R ct = law == 1 ? r1 : (law == 2 ? (R)pow((double)r1, 1.0 / ((double)lexp + 1.0)) : (R)sqrt(r1));

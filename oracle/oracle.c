@@ -1671,3 +1671,25 @@ int64_t orc_record_rays(orc_model* M, uint64_t n_des, uint64_t seed, int64_t max
     tally_free(&T);
     return nrec;
 }
+
+/* Angle-map desorption check: draw n (theta, phi) pairs from a recorded map with uniforms
+ * r[2k], r[2k+1] as the tracer would, and re-bin the incident angles into the map's bins. */
+int orc_anglemap_resample(const uint64_t* pdf, int w, int lo, int hi, double limit, int64_t n, const double* r,
+                          uint64_t* out) {
+    oamap* a = oamap_build(pdf, w, lo, hi, limit);
+    if (!a) return MFG_ERR_INVALID_MODEL;
+    for (int64_t k = 0; k < n; ++k) {
+        int ti; double tov;
+        const double th = am_gen_theta(a, r[2 * k], &ti, &tov);
+        const double ph = am_gen_phi(a, ti, tov, r[2 * k + 1]);
+        long t;
+        if (th < limit) t = (long)(th / limit * (double)lo);
+        else t = lo + (long)((th - limit) / (PI_D / 2.0 - limit) * (double)hi);
+        long p = (long)((ph + 3.1415926) / (2.0 * PI_D) * (double)w);
+        if (t >= lo + hi) t = lo + hi - 1; if (t < 0) t = 0;
+        if (p >= w) p = w - 1; if (p < 0) p = 0;
+        out[t * w + p] += 1;
+    }
+    oamap_free(a);
+    return MFG_OK;
+}

@@ -69,6 +69,10 @@ int64_t orc_record_rays(orc_model* m, uint64_t n_des, uint64_t seed, int64_t max
                         double* origin, double* dir, int32_t* last, int32_t* hit_facet, double* hit_t);
 /* Philox4x32-10 block for tests: out[4] from counter[4], key[2]. */
 void orc_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+/* Angle-map desorption check: resample n incident-angle pairs from a recorded map (uniforms
+ * r[2n]) and bin them like the map (out[(lo+hi)*w] is added to). */
+int orc_anglemap_resample(const uint64_t* pdf, int w, int lo, int hi, double limit, int64_t n, const double* r,
+                          uint64_t* out);
 /* Maxwell CDF at 1 K (100 entries of speed, cumulative probability). */
 void orc_maxwell_cdf(double gas_mass, double* speed, double* cumul);
 

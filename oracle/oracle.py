@@ -67,6 +67,8 @@ def lib():
         L.orc_record_rays.restype = C.c_int64
         L.orc_philox4x32.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         L.orc_maxwell_cdf.argtypes = [C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_anglemap_resample.argtypes = [C.POINTER(C.c_uint64), C.c_int, C.c_int, C.c_int, C.c_double, C.c_int64,
+                                            C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
         _lib = L
     return _lib
 
@@ -146,6 +148,18 @@ def philox4x32(ctr, key):
     out = (C.c_uint32 * 4)()
     lib().orc_philox4x32(c, k, out)
     return list(out)
+
+
+def anglemap_resample(pdf, w, lo, hi, limit, n, seed=1):
+    """Draw n directions from a recorded angle map with the desorption generator and re-bin them."""
+    pdf = np.ascontiguousarray(pdf, np.uint64)
+    r = np.random.default_rng(seed).random(2 * n)
+    out = np.zeros((lo + hi) * w, np.uint64)
+    rc = lib().orc_anglemap_resample(A.ptr(pdf, C.c_uint64), w, lo, hi, limit, n, A.ptr(r, C.c_double),
+                                     A.ptr(out, C.c_uint64))
+    if rc != 0:
+        raise OracleError(A.STATUS_NAMES.get(rc, rc))
+    return out
 
 
 def maxwell_cdf(gas_mass):

@@ -39,6 +39,8 @@ CASES = {
     "08-wall_sojourn_time": {"tex": [], "prof": [], "moments": True},
     "09-histograms": {"tex": [], "prof": [], "moments": True},
     "05-three_structures_nonsquare_textures": {"tex": "all", "prof": "all"},
+    "04-anglemap_desorb": {"tex": [], "prof": []},
+    "04b-anglemap_desorb-sticking source": {"tex": [], "prof": []},
 }
 
 
@@ -66,6 +68,8 @@ def save_case(src_dir, name, keep, catalog):
         out["ref_anglemap"] = st.anglemap
     if st.histogram.size:
         out["ref_histogram"] = st.histogram
+    for f, amap in m.desorb_anglemaps.items():   # recorded maps that angle-map sources desorb by
+        out["desorb_am_%d" % f] = amap
     scalars = {k: float(getattr(m, k)) for k in ("gas_mass", "use_maxwell", "constant_flow", "time_window",
                                                     "enable_decay", "half_life", "low_flux_mode",
                                                     "low_flux_cutoff", "n_structures")}

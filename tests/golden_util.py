@@ -25,6 +25,9 @@ def load(name):
         setattr(m, k, int(v) if k in ("use_maxwell", "constant_flow", "enable_decay", "low_flux_mode", "n_structures") else v)
     if "moment_time" in z.files and len(z["moment_time"]):
         m.set_moments(z["moment_time"], z["moment_window"])
+    for k in z.files:
+        if k.startswith("desorb_am_"):
+            m.desorb_anglemaps[int(k[10:])] = np.array(z[k])
     i = 0
     while "param_%d" % i in z.files:
         tv = z["param_%d" % i]

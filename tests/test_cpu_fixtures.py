@@ -1,7 +1,7 @@
 """The oracle against the reference's stored results of its own test cases (tests/TestCases):
 time-dependent sticking and outgassing parameters with moments (02, 02b), angle-map recording
 across two structures with transparent facets (03, 03b), volume decay (07), wall sojourn time
-(08), a five-moment model (09) and three structures joined by link facets (05).  Per-facet hits per desorption in every moment."""
+(08), a five-moment model (09) three structures joined by link facets (05) and angle-map desorption (04, 04b).  Per-facet hits per desorption in every moment."""
 import numpy as np
 import pytest
 
@@ -21,6 +21,8 @@ CASES = {   # test case -> desorptions per batch (the oracle finishes each case 
     "07-volume_decay": 20000,
     "08-wall_sojourn_time": 40000,
     "09-histograms": 100000,
+    "04-anglemap_desorb": 25000,
+    "04b-anglemap_desorb-sticking source": 25000,
     "05-three_structures_nonsquare_textures": 40000,
 }
 

@@ -3,7 +3,7 @@ own test cases (tests/TestCases via tests/golden): per-facet hits per desorption
 moment, and recorded angle maps.  Covers steady tubes (01, B01-B04), time-dependent sticking,
 outgassing and temperature parameters with moments (02, 02b, 02c), angle-map recording over two
 structures with transparent facets (03, 03b), volume decay (07), wall sojourn time (08) and a
-five-moment model (09) and three structures joined by link facets (05)."""
+five-moment model (09) three structures joined by link facets (05) and angle-map desorption (04, 04b)."""
 import numpy as np
 import pytest
 
@@ -30,6 +30,8 @@ CASES = {   # test case -> desorptions per batch
     "07-volume_decay": 100_000,
     "08-wall_sojourn_time": 500_000,
     "09-histograms": 1_000_000,
+    "04-anglemap_desorb": 500_000,
+    "04b-anglemap_desorb-sticking source": 500_000,
     "05-three_structures_nonsquare_textures": 1_000_000,
 }
 
