@@ -182,9 +182,7 @@ __device__ __noinline__ HitD trace_d(const DevModel& M, int root, double ox, dou
 }
 
 // --------------------------------------------------------- FP32 trace ---
-// FP32 traversal with per-candidate error bounds.  Returns the hit and sets
-// `ambiguous` when a candidate could be classified differently in exact
-// arithmetic (near an edge, near the origin, or too close to the best hit).
+// hit of the FP32 traversal
 struct HitF {
     int f;
     float t, u, v;
@@ -233,122 +231,159 @@ __device__ __forceinline__ RayF make_ray_f(double ox, double oy, double oz, floa
 }
 
 // FacetIsectF layout: [N0 N1 N2 Olo0 | Ohi0 Ohi1 Ohi2 Olo1 | Us0 Us1 Us2 Olo2 | Vs0 Vs1 Vs2 flags]
+
+// Resumable FP32 traversal of one ray: the ref to visit next (a NodeC index >= 0, a leaf list
+// -1-first < 0, or kTrDone), the stack, and the best hit so far with its error bound.  A warp
+// can step its lanes' traversals together and stop them at any step.
+constexpr int kTrDone = -0x7fffffff - 1;
+struct TravF {
+    RayF ray;
+    float ix, iy, iz;
+    int ref, last;
+    HitF h;
+    float htol;    // error bound of h.t
+    bool amb;      // a candidate could be classified differently in exact arithmetic
+    TravStack stk;
+};
+
+__device__ __forceinline__ void trav_init(TravF& s, int root, const RayF& ray, int last) {
+    s.ray = ray;
+    s.ix = 1.0f / ray.dx;
+    s.iy = 1.0f / ray.dy;
+    s.iz = 1.0f / ray.dz;
+    s.ref = root;   // the structure's root NodeC
+    s.last = last;
+    s.h.f = -1;
+    s.h.t = 3.0e38f;
+    s.h.u = s.h.v = 0;
+    s.htol = 0.0f;
+    s.amb = false;
+    s.stk.sp = 0;
+}
+
+// one step: visit the node or the leaf list `s.ref`, then set the next ref
+template <bool kTr = true>
+__device__ __forceinline__ void trav_step(const DevModel& M, TravF& s, unsigned long long* status,
+                                          TranspList<float>* tl = nullptr, const OpacCtx* oc = nullptr) {
+    const RayF& ray = s.ray;
+    const float dx = ray.dx, dy = ray.dy, dz = ray.dz;
+    const float ox = ray.ohx, oy = ray.ohy, oz = ray.ohz;
+    const float ix = s.ix, iy = s.iy, iz = s.iz;
+    const int last = s.last;
+    HitF& h = s.h;
+    float& htol = s.htol;
+    TravStack& stk = s.stk;
+    int ref = s.ref;
+    bool ambiguous = false;
+    if (ref >= 0) {
+        // both children's boxes in one 64-byte node
+        const float4* np = reinterpret_cast<const float4*>(M.nodes_c + ref);
+        const float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
+        const float tcap = h.t + 2.0f * htol;
+        float a0 = (q0.x - ox) * ix, a1 = (q0.w - ox) * ix;
+        float b0 = (q0.y - oy) * iy, b1 = (q1.x - oy) * iy;
+        float c0 = (q0.z - oz) * iz, c1 = (q1.y - oz) * iz;
+        const float tmin0 = fmaxf(fmaxf(fminf(a0, a1), fminf(b0, b1)), fmaxf(fminf(c0, c1), 0.0f));
+        const float tmax0 = fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fminf(fmaxf(c0, c1), tcap));
+        a0 = (q1.z - ox) * ix; a1 = (q2.y - ox) * ix;
+        b0 = (q1.w - oy) * iy; b1 = (q2.z - oy) * iy;
+        c0 = (q2.x - oz) * iz; c1 = (q2.w - oz) * iz;
+        const float tmin1 = fmaxf(fmaxf(fminf(a0, a1), fminf(b0, b1)), fmaxf(fminf(c0, c1), 0.0f));
+        const float tmax1 = fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fminf(fmaxf(c0, c1), tcap));
+        const bool hit0 = tmin0 <= tmax0 * 1.0000005f, hit1 = tmin1 <= tmax1 * 1.0000005f;
+        const int r0 = __float_as_int(q3.x), r1 = __float_as_int(q3.y);
+        if (hit0 && hit1) {
+            // nearer box first
+            const bool first0 = tmin0 <= tmin1;
+            if (stk.sp < kStack) stk.push(first0 ? r1 : r0);
+            else atomicOr(status, KS_STACK);
+            ref = first0 ? r0 : r1;
+        } else if (hit0 || hit1) {
+            ref = hit0 ? r0 : r1;
+        } else {
+            ref = stk.sp == 0 ? kTrDone : stk.pop();
+        }
+        s.ref = ref;
+        return;
+    }
+    for (int k = -1 - ref;; ++k) {
+        const int f = M.prims_c[k];
+        if (f < 0) break;
+        if (f == last) continue;
+        const FacetIsectF& R = M.isect_f[f];
+        float Nx = R.v[0], Ny = R.v[1], Nz = R.v[2];
+        float den = Nx * dx + Ny * dy + Nz * dz;
+        const int fl = (int)R.v[15];                     // bit 0 two-sided, bits 1-2 opacity class
+        const bool two = (fl & 1) != 0;
+        float aden = fabsf(den);
+        // back-face culling is exact when N.d is well above its rounding error
+        if (!two && den > 1e-6f) continue;
+        if (aden < 1e-30f) continue;
+        // w = O - o to ~1e-7 |w| (Sterbenz for nearby facets)
+        float wx = (R.v[4] - ray.ohx) + (R.v[3] - ray.olx);
+        float wy = (R.v[5] - ray.ohy) + (R.v[7] - ray.oly);
+        float wz = (R.v[6] - ray.ohz) + (R.v[11] - ray.olz);
+        float wabs = fabsf(wx) + fabsf(wy) + fabsf(wz);
+        float num = Nx * wx + Ny * wy + Nz * wz;
+        float t = num / den;
+        float at = fabsf(t);
+        float tol = (5e-7f * wabs + 4e-7f * at) / aden + 3e-7f * at;   // error bound of t
+        if (t + tol <= 0.0f) continue;                       // certainly behind
+        if (t - tol > h.t + htol) continue;                  // certainly beyond the best
+        float px = t * dx - wx, py = t * dy - wy, pz = t * dz - wz;   // hit point - O
+        float u = px * R.v[8] + py * R.v[9] + pz * R.v[10];
+        float v = px * R.v[12] + py * R.v[13] + pz * R.v[14];
+        const PolyF P = M.poly_f[f];
+        float em = tol + 3e-7f * (wabs + at) + 2e-7f * fmaxf(P.su, P.sv);   // position error bound, cm
+        float eu = em / P.su, ev = em / P.sv;
+        if (u < -eu || u > 1.0f + eu || v < -ev || v > 1.0f + ev) continue;   // certainly outside
+        // reason codes: 1 near the origin, 2 nearly parallel back face, 3 near a rectangle
+        // edge, 4 near a polygon edge, 5 two hits within error bounds.  A candidate that is
+        // certainly outside its polygon is dropped whatever its distance (coplanar facets
+        // of a baffle have t = 0 exactly for a ray leaving a neighbour).
+        bool inside, eamb = false;
+        if (P.rin2 > 1e29f) {
+            inside = true;                                   // rectangle: [0,1]^2 decided above
+            eamb = u < eu || u > 1.0f - eu || v < ev || v > 1.0f - ev;
+        } else {
+            float du = (u - P.cu) * P.su, dv = (v - P.cv) * P.sv;
+            float r = sqrtf(du * du + dv * dv);
+            if (r * r < P.rin2 && r + em < sqrtf(P.rin2)) inside = true;
+            else if (r - em > sqrtf(P.rout2)) continue;
+            else inside = edge_inside_f(M, P, u, v, em, eamb);
+        }
+        if (!inside && !eamb) continue;                      // certainly outside
+        int why = (t - tol <= 0.0f) ? 1 : ((!two && den >= 0.0f) ? 2 : (eamb ? (P.rin2 > 1e29f ? 3 : 4) : 0));
+        if (why) {
+            // could be a hit closer than the best one: let FP64 decide the ray
+            if (t - tol <= h.t + htol) { ambiguous = true; MFG_AMB_HOOK(why); }
+            continue;
+        }
+        if (!inside) continue;
+        if constexpr (kTr) {
+            const int cls = (fl >> 1) & 3;
+            if (cls != 0 && !is_hard(M, f, cls, oc)) { add_transp(tl, f, t, u, v, status); continue; }
+        }
+        // certain hit; ambiguous ordering when it is within error bounds of the best
+        if (h.f >= 0 && fabsf(t - h.t) <= tol + htol) { ambiguous = true; MFG_AMB_HOOK(5); }
+        if (t < h.t) { h.f = f; h.t = t; h.u = u; h.v = v; htol = tol; }
+    }
+    s.amb = s.amb || ambiguous;
+    s.ref = stk.sp == 0 ? kTrDone : stk.pop();
+}
+
+// FP32 traversal with per-candidate error bounds.  Returns the hit and sets
+// `ambiguous` when a candidate could be classified differently in exact
+// arithmetic (near an edge, near the origin, or too close to the best hit).
 template <bool kTr = true>
 __device__ __noinline__ HitF trace_f(const DevModel& M, int root, const RayF& ray, int last, bool& ambiguous,
                                      unsigned long long* status, TranspList<float>* tl = nullptr,
                                      const OpacCtx* oc = nullptr) {
-    HitF h;
-    h.f = -1;
-    h.t = 3.0e38f;
-    h.u = h.v = 0;
-    float htol = 0.0f;    // error bound of h.t
-    const float dx = ray.dx, dy = ray.dy, dz = ray.dz;
-    const float ox = ray.ohx, oy = ray.ohy, oz = ray.ohz;
-    float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
-    TravStack stk;
-    stk.sp = 0;
-    // `root` is the structure's root NodeC; ref >= 0 a NodeC, < 0 a leaf list in prims_c
-    int ref = root;
-    while (true) {
-        if (ref >= 0) {
-            // both children's boxes in one 64-byte node
-            const float4* np = reinterpret_cast<const float4*>(M.nodes_c + ref);
-            const float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
-            const float tcap = h.t + 2.0f * htol;
-            float a0 = (q0.x - ox) * ix, a1 = (q0.w - ox) * ix;
-            float b0 = (q0.y - oy) * iy, b1 = (q1.x - oy) * iy;
-            float c0 = (q0.z - oz) * iz, c1 = (q1.y - oz) * iz;
-            const float tmin0 = fmaxf(fmaxf(fminf(a0, a1), fminf(b0, b1)), fmaxf(fminf(c0, c1), 0.0f));
-            const float tmax0 = fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fminf(fmaxf(c0, c1), tcap));
-            a0 = (q1.z - ox) * ix; a1 = (q2.y - ox) * ix;
-            b0 = (q1.w - oy) * iy; b1 = (q2.z - oy) * iy;
-            c0 = (q2.x - oz) * iz; c1 = (q2.w - oz) * iz;
-            const float tmin1 = fmaxf(fmaxf(fminf(a0, a1), fminf(b0, b1)), fmaxf(fminf(c0, c1), 0.0f));
-            const float tmax1 = fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fminf(fmaxf(c0, c1), tcap));
-            const bool hit0 = tmin0 <= tmax0 * 1.0000005f, hit1 = tmin1 <= tmax1 * 1.0000005f;
-            const int r0 = __float_as_int(q3.x), r1 = __float_as_int(q3.y);
-            if (hit0 && hit1) {
-                // nearer box first
-                const bool first0 = tmin0 <= tmin1;
-                if (stk.sp < kStack) stk.push(first0 ? r1 : r0);
-                else atomicOr(status, KS_STACK);
-                ref = first0 ? r0 : r1;
-            } else if (hit0 || hit1) {
-                ref = hit0 ? r0 : r1;
-            } else {
-                if (stk.sp == 0) break;
-                ref = stk.pop();
-            }
-            continue;
-        }
-        {
-            for (int k = -1 - ref;; ++k) {
-                const int f = M.prims_c[k];
-                if (f < 0) break;
-                if (f == last) continue;
-                const FacetIsectF& R = M.isect_f[f];
-                float Nx = R.v[0], Ny = R.v[1], Nz = R.v[2];
-                float den = Nx * dx + Ny * dy + Nz * dz;
-                const int fl = (int)R.v[15];                     // bit 0 two-sided, bits 1-2 opacity class
-                const bool two = (fl & 1) != 0;
-                float aden = fabsf(den);
-                // back-face culling is exact when N.d is well above its rounding error
-                if (!two && den > 1e-6f) continue;
-                if (aden < 1e-30f) continue;
-                // w = O - o to ~1e-7 |w| (Sterbenz for nearby facets)
-                float wx = (R.v[4] - ray.ohx) + (R.v[3] - ray.olx);
-                float wy = (R.v[5] - ray.ohy) + (R.v[7] - ray.oly);
-                float wz = (R.v[6] - ray.ohz) + (R.v[11] - ray.olz);
-                float wabs = fabsf(wx) + fabsf(wy) + fabsf(wz);
-                float num = Nx * wx + Ny * wy + Nz * wz;
-                float t = num / den;
-                float at = fabsf(t);
-                float tol = (5e-7f * wabs + 4e-7f * at) / aden + 3e-7f * at;   // error bound of t
-                if (t + tol <= 0.0f) continue;                       // certainly behind
-                if (t - tol > h.t + htol) continue;                  // certainly beyond the best
-                float px = t * dx - wx, py = t * dy - wy, pz = t * dz - wz;   // hit point - O
-                float u = px * R.v[8] + py * R.v[9] + pz * R.v[10];
-                float v = px * R.v[12] + py * R.v[13] + pz * R.v[14];
-                const PolyF P = M.poly_f[f];
-                float em = tol + 3e-7f * (wabs + at) + 2e-7f * fmaxf(P.su, P.sv);   // position error bound, cm
-                float eu = em / P.su, ev = em / P.sv;
-                if (u < -eu || u > 1.0f + eu || v < -ev || v > 1.0f + ev) continue;   // certainly outside
-                // reason codes: 1 near the origin, 2 nearly parallel back face, 3 near a rectangle
-                // edge, 4 near a polygon edge, 5 two hits within error bounds.  A candidate that is
-                // certainly outside its polygon is dropped whatever its distance (coplanar facets
-                // of a baffle have t = 0 exactly for a ray leaving a neighbour).
-                bool inside, eamb = false;
-                if (P.rin2 > 1e29f) {
-                    inside = true;                                   // rectangle: [0,1]^2 decided above
-                    eamb = u < eu || u > 1.0f - eu || v < ev || v > 1.0f - ev;
-                } else {
-                    float du = (u - P.cu) * P.su, dv = (v - P.cv) * P.sv;
-                    float r = sqrtf(du * du + dv * dv);
-                    if (r * r < P.rin2 && r + em < sqrtf(P.rin2)) inside = true;
-                    else if (r - em > sqrtf(P.rout2)) continue;
-                    else inside = edge_inside_f(M, P, u, v, em, eamb);
-                }
-                if (!inside && !eamb) continue;                      // certainly outside
-                int why = (t - tol <= 0.0f) ? 1 : ((!two && den >= 0.0f) ? 2 : (eamb ? (P.rin2 > 1e29f ? 3 : 4) : 0));
-                if (why) {
-                    // could be a hit closer than the best one: let FP64 decide the ray
-                    if (t - tol <= h.t + htol) { ambiguous = true; MFG_AMB_HOOK(why); }
-                    continue;
-                }
-                if (!inside) continue;
-                if constexpr (kTr) {
-                    const int cls = (fl >> 1) & 3;
-                    if (cls != 0 && !is_hard(M, f, cls, oc)) { add_transp(tl, f, t, u, v, status); continue; }
-                }
-                // certain hit; ambiguous ordering when it is within error bounds of the best
-                if (h.f >= 0 && fabsf(t - h.t) <= tol + htol) { ambiguous = true; MFG_AMB_HOOK(5); }
-                if (t < h.t) { h.f = f; h.t = t; h.u = u; h.v = v; htol = tol; }
-            }
-        }
-        if (stk.sp == 0) break;
-        ref = stk.pop();
-    }
-    return h;
+    TravF s;
+    trav_init(s, root, ray, last);
+    while (s.ref != kTrDone) trav_step<kTr>(M, s, status, tl, oc);
+    if (s.amb) ambiguous = true;
+    return s.h;
 }
 
 
