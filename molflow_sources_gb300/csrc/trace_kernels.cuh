@@ -886,7 +886,8 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                 // Measured against one traversal loop per lane: +48 % hits/s on the 200k-facet
                 // beam chamber, +41 % on the tube.  Idle lanes take part in the votes.
                 TravF tv;
-                if (active) trav_init(tv, M.roots_c[P.structure], make_ray_f(P.ox, P.oy, P.oz, (float)dx, (float)dy, (float)dz), P.last);
+                TravStack stk;
+                if (active) trav_init(tv, stk, M.roots_c[P.structure], make_ray_f(P.ox, P.oy, P.oz, (float)dx, (float)dy, (float)dz), P.last);
                 else tv.ref = kTrDone;
                 // Node and leaf steps run in separate rounds: a lane that reaches a leaf list waits
                 // until the lanes at leaves outnumber those at nodes two to one, then the leaf lanes
@@ -898,7 +899,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                     const unsigned ml = __ballot_sync(0xffffffffu, live && !node);
                     if ((mn | ml) == 0u) break;
                     const bool leaf_round = __popc(ml) > 2 * __popc(mn);
-                    if (leaf_round ? (live && !node) : node) trav_step<kExt>(M, tv, T.global + TG_STATUS, tlp, ocp);
+                    if (leaf_round ? (live && !node) : node) trav_step<kExt>(M, tv, stk, T.global + TG_STATUS, tlp, ocp);
                 }
                 if (!active) continue;
                 h = tv.h;

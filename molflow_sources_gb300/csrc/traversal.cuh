@@ -233,8 +233,9 @@ __device__ __forceinline__ RayF make_ray_f(double ox, double oy, double oz, floa
 // FacetIsectF layout: [N0 N1 N2 Olo0 | Ohi0 Ohi1 Ohi2 Olo1 | Us0 Us1 Us2 Olo2 | Vs0 Vs1 Vs2 flags]
 
 // Resumable FP32 traversal of one ray: the ref to visit next (a NodeC index >= 0, a leaf list
-// -1-first < 0, or kTrDone), the stack, and the best hit so far with its error bound.  A warp
-// can step its lanes' traversals together and stop them at any step.
+// -1-first < 0, or kTrDone) and the best hit so far with its error bound; the stack is kept
+// apart, so that the scalar state can stay in registers.  A warp can step its lanes' traversals
+// together and stop them at any step.
 constexpr int kTrDone = -0x7fffffff - 1;
 struct TravF {
     RayF ray;
@@ -243,10 +244,9 @@ struct TravF {
     HitF h;
     float htol;    // error bound of h.t
     bool amb;      // a candidate could be classified differently in exact arithmetic
-    TravStack stk;
 };
 
-__device__ __forceinline__ void trav_init(TravF& s, int root, const RayF& ray, int last) {
+__device__ __forceinline__ void trav_init(TravF& s, TravStack& stk, int root, const RayF& ray, int last) {
     s.ray = ray;
     s.ix = 1.0f / ray.dx;
     s.iy = 1.0f / ray.dy;
@@ -258,12 +258,12 @@ __device__ __forceinline__ void trav_init(TravF& s, int root, const RayF& ray, i
     s.h.u = s.h.v = 0;
     s.htol = 0.0f;
     s.amb = false;
-    s.stk.sp = 0;
+    stk.sp = 0;
 }
 
 // one step: visit the node or the leaf list `s.ref`, then set the next ref
 template <bool kTr = true>
-__device__ __forceinline__ void trav_step(const DevModel& M, TravF& s, unsigned long long* status,
+__device__ __forceinline__ void trav_step(const DevModel& M, TravF& s, TravStack& stk, unsigned long long* status,
                                           TranspList<float>* tl = nullptr, const OpacCtx* oc = nullptr) {
     const RayF& ray = s.ray;
     const float dx = ray.dx, dy = ray.dy, dz = ray.dz;
@@ -272,7 +272,6 @@ __device__ __forceinline__ void trav_step(const DevModel& M, TravF& s, unsigned 
     const int last = s.last;
     HitF& h = s.h;
     float& htol = s.htol;
-    TravStack& stk = s.stk;
     int ref = s.ref;
     bool ambiguous = false;
     if (ref >= 0) {
@@ -380,8 +379,9 @@ __device__ __noinline__ HitF trace_f(const DevModel& M, int root, const RayF& ra
                                      unsigned long long* status, TranspList<float>* tl = nullptr,
                                      const OpacCtx* oc = nullptr) {
     TravF s;
-    trav_init(s, root, ray, last);
-    while (s.ref != kTrDone) trav_step<kTr>(M, s, status, tl, oc);
+    TravStack stk;
+    trav_init(s, stk, root, ray, last);
+    while (s.ref != kTrDone) trav_step<kTr>(M, s, stk, status, tl, oc);
     if (s.amb) ambiguous = true;
     return s.h;
 }
