@@ -340,7 +340,9 @@ def main():
         b_, k_ = (int(x) for x in args.launch.split(","))
         tuned = {"block_size": b_, "blocks_per_sm": k_}
     else:
-        tuned = sim.autotune(max(n_step // 20, 10000), precision=A.PREC_FP32R, seed=seed)   # launch shape
+        # launch shape: trial runs of a quarter step, so that each of the up to 2048 resident
+        # threads of an SM traces several particles and the tail of a launch does not decide
+        tuned = sim.autotune(max(n_step // 4, 10000), precision=A.PREC_FP32R, seed=seed)
     shape = dict(tuned) if args.launch else {}
     for _ in range(args.warmup):
         sim.SimulationMCStep(n_step, precision=A.PREC_FP32R, seed=seed, **shape)

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define MFG_ABI_VERSION 3u
+#define MFG_ABI_VERSION 4u
 
 /* ---- status codes (replace the reference's exceptions / MCStepResult,
  *      src/Simulation/Particle.h:24-28, src/Simulation/MolflowSimGeom.cpp:219-247) ---- */
@@ -199,6 +199,19 @@ typedef struct mfg_model_desc {
      * anglemap_phi_width * (lower_res + higher_res) counts (theta-major, as recorded); NULL when
      * no facet desorbs by angle map */
     const uint64_t* desorb_anglemap;
+    /* outgassing maps (useOutgassingFile; StartFromSource, Particle.cpp:425-446 and 513-535;
+     * MolflowSimFacet::InitializeOutgassingMap, MolflowSimFacet.cpp:224-239).  A facet with
+     * outgassing_map_width[i] > 0 (array NULL: none) desorbs from its map instead of
+     * `outgassing`: outgassing_map holds, for those facets in facet order, width x height cell
+     * rates (Pa m^3/s, row-major: height rows of width cells along U).  The facet's weight among
+     * the sources is the sum of its cells, a cell is chosen by its rate and the start point is
+     * uniform in the cell; the grid has ratio_u * |U| by ratio_v * |V| cells over the facet
+     * (outgassingFileRatioU/V), so its last row and column may be partial. */
+    const int32_t*  outgassing_map_width;
+    const int32_t*  outgassing_map_height;
+    const double*   outgassing_map_ratio_u;
+    const double*   outgassing_map_ratio_v;
+    const double*   outgassing_map;
 } mfg_model_desc;
 
 /*

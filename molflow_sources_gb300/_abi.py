@@ -1,7 +1,7 @@
-"""ctypes mirrors of the C structs declared in include/mfg.h (ABI version 1)."""
+"""ctypes mirrors of the C structs declared in include/mfg.h."""
 import ctypes as C
 
-MFG_ABI_VERSION = 3
+MFG_ABI_VERSION = 4
 
 MFG_OK = 0
 MFG_ERR_INVALID_MODEL = 1
@@ -126,6 +126,11 @@ MODEL_DESC_FIELDS = [
     ("scatter_rho", C.c_double),
     ("scatter_cutoff_speed", C.c_double),
     ("desorb_anglemap", _u64),
+    ("outgassing_map_width", _i32),
+    ("outgassing_map_height", _i32),
+    ("outgassing_map_ratio_u", _d),
+    ("outgassing_map_ratio_v", _d),
+    ("outgassing_map", _d),
 ]
 
 

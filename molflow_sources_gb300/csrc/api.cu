@@ -190,6 +190,8 @@ static int sim_upload(mfg_sim* s) {
     UP(h.src_cdf, src_cdf);
     UP(h.src_facet, src_facet);
     UP(h.src_id, src_id);
+    UP(h.src_cell, src_cell);
+    UP(h.og, og);
     UP(h.mstart, mstart);
     UP(h.mend, mend);
     UP(h.id_start, id_start);
@@ -384,6 +386,8 @@ static const void* kernel_of(int variant) {
         case 2: return (const void*)mfgk::trace_kernel<true, 2>;
         case 3: return (const void*)mfgk::trace_kernel<true, 3>;
         case 4: return (const void*)mfgk::trace_kernel<true, 4>;
+        case 6: return (const void*)mfgk::trace_kernel<true, 6>;
+        case 8: return (const void*)mfgk::trace_kernel<true, 8>;
         case 12: return (const void*)mfgk::trace_kernel<false, 2, true>;
         case 13: return (const void*)mfgk::trace_kernel<true, 3, true>;
         case 100: return (const void*)mfgk::trace_kernel<false, 2, false, true>;
@@ -442,16 +446,18 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     }
     int block = o.block_size > 0 ? o.block_size : 256;
     if (block % 32 || block > 256) return fail(MFG_ERR_INVALID_ARGUMENT, "block_size must be a multiple of 32, at most 256");
-    // kernel variant: FP64, or FP32R compiled for at least 2, 3 or 4 resident blocks per SM
-    // (register budgets 128, 85, 64); blocks_per_sm selects the FP32R variant.  Models with
-    // transparent or semi-transparent facets use the variants that keep a pass list (+100).
+    // kernel variant: FP64, or FP32R compiled for at least 2, 3, 4, 6 or 8 resident blocks per SM
+    // (register budgets 128, 80, 64, 40, 32); blocks_per_sm selects the FP32R variant.  Models
+    // with transparent facets, histograms, low-flux mode, scattering, moving facets or angle-map
+    // desorption use the extended variants (+100).
     int variant = 0;
     if (sens) {
         variant = o.precision == MFG_PREC_FP32R ? 13 : 12;
     } else if (o.precision == MFG_PREC_FP32R) {
-        variant = (o.blocks_per_sm == 3) ? 3 : (o.blocks_per_sm == 4 ? 4 : 2);
+        const int b = int(o.blocks_per_sm);
+        variant = (b == 3 || b == 4 || b == 6 || b == 8) ? b : (b == 5 ? 4 : (b == 7 ? 6 : (b > 8 ? 8 : 2)));
     }
-    if (h.has_ext) variant = (variant == 3 || variant == 4) ? 102 : variant + 100;
+    if (h.has_ext) variant = variant == 0 ? 100 : 102;
     const void* fn = kernel_of(variant);
     CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn)));
     int per_sm = 0;
@@ -584,14 +590,14 @@ int mfg_wait(mfg_sim* s, int64_t timeout_ms, mfg_run_stats* stats) {
 
 int mfg_autotune(mfg_sim* s, uint64_t n_trial, int32_t precision, uint64_t seed, mfg_run_options* best) {
     if (!s || (precision != MFG_PREC_FP64 && precision != MFG_PREC_FP32R)) return fail(MFG_ERR_INVALID_ARGUMENT, "bad argument");
-    const int blocks[] = {128, 256};
+    const int blocks[] = {256};   // 128-thread blocks at the same register budget hold half the threads
     const int bps64[] = {0};
-    const int bps32[] = {2, 3, 4};
+    const int bps32[] = {2, 3, 4, 6, 8};
     double best_rate = -1;
     mfg_run_options bo{};
     for (int b : blocks) {
         const int* bl = precision == MFG_PREC_FP32R ? bps32 : bps64;
-        int nb = precision == MFG_PREC_FP32R ? 3 : 1;
+        int nb = precision == MFG_PREC_FP32R ? int(sizeof(bps32) / sizeof(bps32[0])) : 1;
         for (int k = 0; k < nb; ++k) {
             mfg_run_options o{};
             o.precision = precision;

@@ -150,6 +150,14 @@ struct AmDev {
     int32_t pcdf_lo, pcdf_hi, ppdf_lo, ppdf_hi;    // phi CDFs at bin midpoints, phi pdfs
 };
 
+// Outgassing map of a source facet (MolflowSimFacet::InitializeOutgassingMap): cells along U and
+// V, and the grid's extent in cells over the facet (ratio x |U|, ratio x |V|; the last row and
+// column may be partial)
+struct OgDev {
+    int32_t w, h;
+    double wp, hp;
+};
+
 // one histogram set (RecordHistograms, Particle.cpp:926-975): bin sizes, bin counts (0 = not
 // recorded) and offset of the set in a moment block (-1 = none)
 struct HistDev {
@@ -183,6 +191,8 @@ struct DevModel {
     const double* src_cdf;       // prefix sums of source weights
     const int32_t* src_facet;
     const int32_t* src_id;       // integrated-desorption table index per source (-1 none)
+    const int32_t* src_cell;     // outgassing-map cell per source (-1 none), or null without maps
+    const OgDev* og;             // [nf] outgassing-map grids, or null without maps
     double src_total;
     double latest;               // latestMoment
     const double* mstart;        // moment window starts (sorted)

@@ -389,6 +389,10 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     cpb(m.am_record, d->anglemap_record);
     cpb(m.sojourn, d->enable_sojourn);
     cpb(m.moving, d->is_moving);
+    cpi(m.og_w, d->outgassing_map_width, 0);
+    cpi(m.og_h, d->outgassing_map_height, 0);
+    cp(m.og_ru, d->outgassing_map_ratio_u, 0.0);
+    cp(m.og_rv, d->outgassing_map_ratio_v, 0.0);
     m.count.resize(nf);
     for (int i = 0; i < nf; ++i) m.count[i] = opt<uint32_t>(d->count_flags, i, 0u);
     m.gas_mass = d->gas_mass;
@@ -499,10 +503,58 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
         }
     }
 
-    // source table (StartFromSource weights, Particle.cpp:421-464; CalcTotalOutgassing)
+    // source table (StartFromSource weights, Particle.cpp:421-464; CalcTotalOutgassing,
+    // MolflowSimGeom.cpp:297-328).  A facet with an outgassing map gets one entry per cell of
+    // non-zero rate, so that one search picks the facet and the cell (Particle.cpp:425-446:
+    // the first cell whose cumulative rate exceeds the remainder).
+    m.src_cdf.clear();
+    m.src_facet.clear();
+    m.src_id.clear();
+    m.src_cell.clear();
+    m.og.clear();
+    bool any_map = false;
+    for (int i = 0; i < nf; ++i) any_map = any_map || (m.og_w[i] > 0 && m.og_h[i] > 0);
+    if (any_map && !d->outgassing_map) { err = "outgassing_map_width is set but outgassing_map is NULL"; return MFG_ERR_INVALID_MODEL; }
+    if (any_map) {
+        m.og.assign(nf, OgDev{0, 0, 0.0, 0.0});
+        for (int i = 0; i < nf; ++i) {
+            if (!(m.og_w[i] > 0 && m.og_h[i] > 0)) continue;
+            const HostFacet& F = m.facets[i];
+            const double nu = std::sqrt(F.U[0] * F.U[0] + F.U[1] * F.U[1] + F.U[2] * F.U[2]);
+            const double nv = std::sqrt(F.V[0] * F.V[0] + F.V[1] * F.V[1] + F.V[2] * F.V[2]);
+            m.og[i] = OgDev{m.og_w[i], m.og_h[i], nu * m.og_ru[i], nv * m.og_rv[i]};
+            if (!(m.og[i].wp > m.og_w[i] - 1.0 && m.og[i].hp > m.og_h[i] - 1.0)) {
+                err = "facet " + std::to_string(i + 1) + ": the outgassing map has more cells than its ratio puts on the facet";
+                return MFG_ERR_INVALID_MODEL;
+            }
+        }
+    }
     double sum = 0;
+    size_t cursor = 0;
     for (int i = 0; i < nf; ++i) {
+        const bool map = m.og_w[i] > 0 && m.og_h[i] > 0;
+        const double* cells = map ? d->outgassing_map + cursor : nullptr;
+        const int ncell = map ? m.og_w[i] * m.og_h[i] : 0;
+        cursor += size_t(ncell);
         if (m.desorb_type[i] == MFG_DES_NONE) continue;
+        if (map) {
+            double tot = 0;
+            for (int c = 0; c < ncell; ++c) {
+                if (!(cells[c] >= 0)) { err = "facet " + std::to_string(i + 1) + ": negative outgassing-map cell"; return MFG_ERR_INVALID_MODEL; }
+                tot += cells[c];
+            }
+            if (!(tot > 0)) continue;
+            if (m.structure[i] == -1) { err = "facet " + std::to_string(i + 1) + " is in all structures, it cannot desorb"; return MFG_ERR_INVALID_MODEL; }
+            for (int c = 0; c < ncell; ++c) {
+                if (!(cells[c] > 0)) continue;
+                sum += m.latest * cells[c] / (kKb * m.temperature[i]);
+                m.src_cdf.push_back(sum);
+                m.src_facet.push_back(i);
+                m.src_id.push_back(-1);
+                m.src_cell.push_back(c);
+            }
+            continue;
+        }
         double w;
         if (m.facet_id[i] >= 0) w = m.id_cum[m.id_start[m.facet_id[i] + 1] - 1];
         else w = m.latest * m.outgassing[i];
@@ -513,6 +565,7 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
         m.src_cdf.push_back(sum);
         m.src_facet.push_back(i);
         m.src_id.push_back(m.facet_id[i]);
+        if (any_map) m.src_cell.push_back(-1);
     }
     m.src_total = sum;
 
@@ -967,8 +1020,8 @@ int merge_host_models(const std::vector<const HostModel*>& parts, HostModel& out
     for (const HostModel* p : parts) {
         if (p->layout.histogram_bins > 0) { err = "histograms are not recorded in batched instances"; return MFG_ERR_UNSUPPORTED_FEATURE; }
         if (p->low_flux) { err = "low-flux mode is not traced in batched instances"; return MFG_ERR_UNSUPPORTED_FEATURE; }
-        if (p->scatter || p->motion_type || !p->am_dev.empty()) {
-            err = "scattering, moving facets and angle-map desorption are not traced in batched instances";
+        if (p->scatter || p->motion_type || !p->am_dev.empty() || !p->og.empty()) {
+            err = "scattering, moving facets, angle-map desorption and outgassing maps are not traced in batched instances";
             return MFG_ERR_UNSUPPORTED_FEATURE;
         }
     }

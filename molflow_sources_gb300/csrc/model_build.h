@@ -54,6 +54,10 @@ struct HostModel {
     std::vector<int32_t> facet_id;        // ID table per facet (-1 none)
     std::vector<double> src_cdf;
     std::vector<int32_t> src_facet, src_id;
+    std::vector<int32_t> src_cell;        // outgassing-map cell of each source (empty: no maps)
+    std::vector<int32_t> og_w, og_h;      // outgassing-map grid per facet (0: none)
+    std::vector<double> og_ru, og_rv;
+    std::vector<OgDev> og;                // per facet (empty: no maps)
     double src_total = 0;
     // layout
     mfg_state_layout layout{};

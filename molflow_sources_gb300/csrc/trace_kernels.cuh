@@ -328,20 +328,43 @@ __device__ __forceinline__ bool in_facet_f(const DevModel& M, int f, float u, fl
 }
 
 // Start point of a desorption: uniform (u,v) in the bounding rectangle until inside the polygon,
-// at most 1000 tries, else the facet centre (Particle.cpp:513-570).  The point is formed in FP64.
+// at most 1000 tries, else the facet centre (Particle.cpp:513-570).  With an outgassing map,
+// (u,v) is uniform in the chosen cell (the last row and column of the grid may be partial) and
+// the fallback is the cell's centre.  The point is formed in FP64.
 template <bool kFP32, class Rng, class R>
-__device__ __noinline__ void start_point(const DevModel& M, int fo, Rng& rng, double& ox, double& oy, double& oz,
-                                         R& pu, R& pv) {
+__device__ __noinline__ void start_point(const DevModel& M, int fo, int cell, Rng& rng, double& ox, double& oy,
+                                         double& oz, R& pu, R& pv) {
     const FacetIsectD& Rr = M.isect_d[fo];
     const PolyD& PP = M.poly_d[fo];
     bool found = false;
     double su = 0.5, sv = 0.5;
+    int cw = 0, ch = 0;
+    double wp = 1.0, hp = 1.0, lu = 1.0, lv = 1.0;
+    if (cell >= 0) {
+        const OgDev g = M.og[fo];
+        ch = cell / g.w;
+        cw = cell - ch * g.w;
+        wp = g.wp;
+        hp = g.hp;
+        lu = cw < g.w - 1 ? 1.0 : g.wp - (g.w - 1.0);
+        lv = ch < g.h - 1 ? 1.0 : g.hp - (g.h - 1.0);
+        su = (cw + 0.5) / wp;
+        sv = (ch + 0.5) / hp;
+    }
     for (int tr = 0; tr < 1000 && !found; ++tr) {
-        R u = (R)rng.next(), v = (R)rng.next();
+        R u, v;
+        if (cell >= 0) {
+            const double ru = (double)rng.next(), rv = (double)rng.next();
+            u = (R)((cw + ru * lu) / wp);
+            v = (R)((ch + rv * lv) / hp);
+        } else {
+            u = (R)rng.next();
+            v = (R)rng.next();
+        }
         bool in = kFP32 ? in_facet_f(M, fo, (float)u, (float)v) : in_facet_d(M, fo, (double)u, (double)v);
         if (in) { su = (double)u; sv = (double)v; found = true; }
     }
-    if (found) {
+    if (found || cell >= 0) {
         double a = su * PP.su * PP.su, b = sv * PP.sv * PP.sv;   // O + u*U + v*V (record keeps U/|U|^2)
         ox = Rr.v[4] + a * Rr.v[8] + b * Rr.v[12];
         oy = Rr.v[5] + a * Rr.v[9] + b * Rr.v[13];
@@ -711,7 +734,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
             }
             if (want && P.bounces >= n_total) { active = false; want = false; }
         }
-        if (!kFP32 && !active) continue;   // FP32 variants: idle lanes still join the lockstep traversal
+        // lanes without a particle go on to the traversal too: they take part in its warp votes
 
         // ---- 1. emit: desorption (want) or reflection from P.last.  The two share the speed,
         //      direction and tally code; only short prologues differ.  Random numbers are drawn in
@@ -722,6 +745,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
             int fo, law;              // law: 0 cosine, 1 uniform, 2 cos^N, 3 general reflection
             bool flip = false;
             bool amdes = false;   // extended variants: direction from the source's recorded angle map
+            int ocell = -1;       // outgassing-map cell of the source (-1: uniform over the facet)
             R lexp = 0;
             if (des) {
                 int inst = 0;
@@ -739,6 +763,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                 if (lo >= scount) lo = scount - 1;
                 lo += sbase;
                 fo = M.src_facet[lo];
+                if (M.src_cell) ocell = M.src_cell[lo];
                 const FacetInfo2& I2 = M.info2[fo];
                 if (M.info[fo].flags & FF_TWO_SIDED) flip = (double)rng.next() > 0.5;
                 int idt = M.src_id[lo];
@@ -789,7 +814,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                     P.scat_at = M.scatter ? -M.sc_mfp * log(1.0 - (double)rng.next()) : 1e100;
                 }
                 // start point: rejection in the (u,v) rectangle, at most 1000 tries (Particle.cpp:513-570)
-                start_point<kFP32>(M, fo, rng, P.ox, P.oy, P.oz, pu, pv);
+                start_point<kFP32>(M, fo, ocell, rng, P.ox, P.oy, P.oz, pu, pv);
                 P.last = fo;
             }
             if (law == 3) {
@@ -890,15 +915,16 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                 if (active) trav_init(tv, stk, M.roots_c[P.structure], make_ray_f(P.ox, P.oy, P.oz, (float)dx, (float)dy, (float)dz), P.last);
                 else tv.ref = kTrDone;
                 // Node and leaf steps run in separate rounds: a lane that reaches a leaf list waits
-                // until the lanes at leaves outnumber those at nodes two to one, then the leaf lanes
-                // test their facets together (+26 % on C2, +15 % on C1 against mixed rounds).
+                // until the lanes at leaves outnumber those at nodes three to one, then the leaf
+                // lanes test their facets together (+26 % on C2, +15 % on C1 against mixed rounds;
+                // ratios 1, 2, 3, 4 measured, 2 to 4 within 1 %).
                 while (true) {
                     const bool live = tv.ref != kTrDone;
                     const bool node = live && tv.ref >= 0;
                     const unsigned mn = __ballot_sync(0xffffffffu, node);
                     const unsigned ml = __ballot_sync(0xffffffffu, live && !node);
                     if ((mn | ml) == 0u) break;
-                    const bool leaf_round = __popc(ml) > 2 * __popc(mn);
+                    const bool leaf_round = __popc(ml) > 3 * __popc(mn);
                     if (leaf_round ? (live && !node) : node) trav_step<kExt>(M, tv, stk, T.global + TG_STATUS, tlp, ocp);
                 }
                 if (!active) continue;
@@ -923,8 +949,15 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                 ht = (double)h.t + (double)((float)r / (float)den);
             }
         } else {
-            HitD h = trace_d<R, kExt>(M, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last, T.global + TG_STATUS, tlp, ocp);
-            hf = h.f; ht = h.t; hu = (R)h.u; hv = (R)h.v;
+            // the FP64 traversal in lockstep as well: one node per lane and step, a warp vote after each
+            TravD td;
+            TravStack stk;
+            if (active) travd_init(td, stk, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last);
+            else td.node = kTrDoneD;
+            while (__any_sync(0xffffffffu, td.node != kTrDoneD))
+                if (td.node != kTrDoneD) travd_step<R, kExt>(M, td, stk, T.global + TG_STATUS, tlp, ocp);
+            if (!active) continue;
+            hf = td.h.f; ht = td.h.t; hu = (R)td.h.u; hv = (R)td.h.v;
         }
         if (hf < 0) {   // leak (Particle.cpp:387-392)
             ++c_leak;

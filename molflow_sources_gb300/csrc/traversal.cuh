@@ -117,68 +117,93 @@ struct HitD {
     double t, u, v;
 };
 
-// closest hard hit of the ray (skipping facet `last`); BVH of structure `root`.  Transparent
+// Resumable FP64 traversal of one ray (the FP64 kernel and the FP32 path's recheck): the next
+// NodeD to visit (or kTrDoneD) and the closest hard hit so far; the stack is kept apart.
+constexpr int kTrDoneD = -1;
+struct TravD {
+    double ox, oy, oz, dx, dy, dz, ix, iy, iz;
+    int node, last;
+    HitD h;
+};
+
+__device__ __forceinline__ void travd_init(TravD& s, TravStack& stk, int root, double ox, double oy, double oz,
+                                           double dx, double dy, double dz, int last) {
+    s.ox = ox; s.oy = oy; s.oz = oz;
+    s.dx = dx; s.dy = dy; s.dz = dz;
+    s.ix = 1.0 / dx; s.iy = 1.0 / dy; s.iz = 1.0 / dz;
+    s.node = root;
+    s.last = last;
+    s.h.f = -1;
+    s.h.t = 1.0e99;
+    s.h.u = s.h.v = 0;
+    stk.sp = 0;
+}
+
+// one step: visit node `s.node` (its box; a leaf's facets), then set the next node.  Transparent
 // candidates (opacity 0, or a partial-opacity draw above the opacity) go to `tl`.
+template <class LT = double, bool kTr = true>
+__device__ __forceinline__ void travd_step(const DevModel& M, TravD& s, TravStack& stk, unsigned long long* status,
+                                           TranspList<LT>* tl = nullptr, const OpacCtx* oc = nullptr) {
+    const double ox = s.ox, oy = s.oy, oz = s.oz, dx = s.dx, dy = s.dy, dz = s.dz;
+    const double ix = s.ix, iy = s.iy, iz = s.iz;
+    const int last = s.last;
+    HitD& h = s.h;
+    const NodeD nd = M.nodes_d[s.node];
+    double tx0 = (nd.lo[0] - ox) * ix, tx1 = (nd.hi[0] - ox) * ix;
+    double ty0 = (nd.lo[1] - oy) * iy, ty1 = (nd.hi[1] - oy) * iy;
+    double tz0 = (nd.lo[2] - oz) * iz, tz1 = (nd.hi[2] - oz) * iz;
+    double tmin = fmax(fmax(fmin(tx0, tx1), fmin(ty0, ty1)), fmax(fmin(tz0, tz1), 0.0));
+    double tmax = fmin(fmin(fmax(tx0, tx1), fmax(ty0, ty1)), fmin(fmax(tz0, tz1), h.t));
+    bool hit = tmin <= tmax;
+    if (hit && nd.b >= 0) {
+        int near = nd.a, far = nd.a + 1;
+        double dax = nd.b == 0 ? dx : (nd.b == 1 ? dy : dz);
+        if (dax < 0) { near = nd.a + 1; far = nd.a; }
+        if (stk.sp < kStack) stk.push(far);
+        else atomicOr(status, KS_STACK);
+        s.node = near;
+        return;
+    }
+    if (hit) {
+        int cnt = -1 - nd.b;
+        for (int k = 0; k < cnt; ++k) {
+            int f = M.prims[nd.a + k];
+            if (f == last) continue;
+            const FacetIsectD& R = M.isect_d[f];
+            double Nx = R.v[0], Ny = R.v[1], Nz = R.v[2], D = R.v[3];
+            double den = Nx * dx + Ny * dy + Nz * dz;
+            const long long fl = __double_as_longlong(R.v[7]);   // bit 0 two-sided, bits 1-2 opacity class
+            const bool two = (fl & 1) != 0;
+            if (!two && den >= 0.0) continue;
+            if (den == 0.0) continue;
+            double t = (D - (Nx * ox + Ny * oy + Nz * oz)) / den;
+            if (!(t > 0.0) || t > h.t) continue;
+            double px = ox + t * dx - R.v[4], py = oy + t * dy - R.v[5], pz = oz + t * dz - R.v[6];
+            double u = px * R.v[8] + py * R.v[9] + pz * R.v[10];
+            if (u < 0.0 || u > 1.0) continue;
+            double v = px * R.v[12] + py * R.v[13] + pz * R.v[14];
+            if (v < 0.0 || v > 1.0) continue;
+            if (!in_facet_d(M, f, u, v)) continue;
+            if constexpr (kTr) {
+                const int cls = (int)((fl >> 1) & 3);
+                if (cls != 0 && !is_hard(M, f, cls, oc)) { add_transp(tl, f, t, u, v, status); continue; }
+            }
+            if (t < h.t || f < h.f) { h.f = f; h.t = t; h.u = u; h.v = v; }
+        }
+    }
+    s.node = stk.sp == 0 ? kTrDoneD : stk.pop();
+}
+
+// closest hard hit of the ray (skipping facet `last`); BVH of structure `root`
 template <class LT = double, bool kTr = true>
 __device__ __noinline__ HitD trace_d(const DevModel& M, int root, double ox, double oy, double oz,
                                      double dx, double dy, double dz, int last, unsigned long long* status,
                                      TranspList<LT>* tl = nullptr, const OpacCtx* oc = nullptr) {
-    HitD h;
-    h.f = -1;
-    h.t = 1.0e99;
-    h.u = h.v = 0;
-    double ix = 1.0 / dx, iy = 1.0 / dy, iz = 1.0 / dz;
+    TravD s;
     TravStack stk;
-    stk.sp = 0;
-    int node = root;
-    while (true) {
-        const NodeD nd = M.nodes_d[node];
-        double tx0 = (nd.lo[0] - ox) * ix, tx1 = (nd.hi[0] - ox) * ix;
-        double ty0 = (nd.lo[1] - oy) * iy, ty1 = (nd.hi[1] - oy) * iy;
-        double tz0 = (nd.lo[2] - oz) * iz, tz1 = (nd.hi[2] - oz) * iz;
-        double tmin = fmax(fmax(fmin(tx0, tx1), fmin(ty0, ty1)), fmax(fmin(tz0, tz1), 0.0));
-        double tmax = fmin(fmin(fmax(tx0, tx1), fmax(ty0, ty1)), fmin(fmax(tz0, tz1), h.t));
-        bool hit = tmin <= tmax;
-        if (hit && nd.b >= 0) {
-            int near = nd.a, far = nd.a + 1;
-            double dax = nd.b == 0 ? dx : (nd.b == 1 ? dy : dz);
-            if (dax < 0) { near = nd.a + 1; far = nd.a; }
-            if (stk.sp < kStack) stk.push(far);
-            else atomicOr(status, KS_STACK);
-            node = near;
-            continue;
-        }
-        if (hit) {
-            int cnt = -1 - nd.b;
-            for (int k = 0; k < cnt; ++k) {
-                int f = M.prims[nd.a + k];
-                if (f == last) continue;
-                const FacetIsectD& R = M.isect_d[f];
-                double Nx = R.v[0], Ny = R.v[1], Nz = R.v[2], D = R.v[3];
-                double den = Nx * dx + Ny * dy + Nz * dz;
-                const long long fl = __double_as_longlong(R.v[7]);   // bit 0 two-sided, bits 1-2 opacity class
-                const bool two = (fl & 1) != 0;
-                if (!two && den >= 0.0) continue;
-                if (den == 0.0) continue;
-                double t = (D - (Nx * ox + Ny * oy + Nz * oz)) / den;
-                if (!(t > 0.0) || t > h.t) continue;
-                double px = ox + t * dx - R.v[4], py = oy + t * dy - R.v[5], pz = oz + t * dz - R.v[6];
-                double u = px * R.v[8] + py * R.v[9] + pz * R.v[10];
-                if (u < 0.0 || u > 1.0) continue;
-                double v = px * R.v[12] + py * R.v[13] + pz * R.v[14];
-                if (v < 0.0 || v > 1.0) continue;
-                if (!in_facet_d(M, f, u, v)) continue;
-                if constexpr (kTr) {
-                    const int cls = (int)((fl >> 1) & 3);
-                    if (cls != 0 && !is_hard(M, f, cls, oc)) { add_transp(tl, f, t, u, v, status); continue; }
-                }
-                if (t < h.t || f < h.f) { h.f = f; h.t = t; h.u = u; h.v = v; }
-            }
-        }
-        if (stk.sp == 0) break;
-        node = stk.pop();
-    }
-    return h;
+    travd_init(s, stk, root, ox, oy, oz, dx, dy, dz, last);
+    while (s.node != kTrDoneD) travd_step<LT, kTr>(M, s, stk, status, tl, oc);
+    return s.h;
 }
 
 // --------------------------------------------------------- FP32 trace ---

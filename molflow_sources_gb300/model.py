@@ -102,6 +102,9 @@ class Model:
         self.scatter_cutoff_speed = 0.0
         # recorded angle maps of the facets that desorb by angle map: {facet: uint64 counts}
         self.desorb_anglemaps = {}
+        # outgassing maps (useOutgassingFile): {facet: dict(width, height, ratio_u, ratio_v,
+        # values = height x width rates in Pa m^3/s)}
+        self.outgassing_maps = {}
         # sp.globalHistogramParams
         self.global_histogram = dict(record=0, bounce_binsize=1, bounce_max=0, distance_binsize=1.0,
                                      distance_max=0.0, time_binsize=1.0, time_max=0.0)
@@ -188,6 +191,23 @@ class Model:
                 a[:min(n, src.size)] = src[:n]
                 parts.append(a)
             d.desorb_anglemap = p(np.concatenate(parts), C.c_uint64)
+        if self.outgassing_maps:
+            ow = np.zeros(self.n_facets, np.int32)
+            oh = np.zeros(self.n_facets, np.int32)
+            oru = np.zeros(self.n_facets, np.float64)
+            orv = np.zeros(self.n_facets, np.float64)
+            vals = []
+            for i in sorted(self.outgassing_maps):
+                g = self.outgassing_maps[i]
+                v = np.asarray(g["values"], np.float64)
+                ow[i], oh[i] = int(g["width"]), int(g["height"])
+                oru[i], orv[i] = float(g["ratio_u"]), float(g["ratio_v"])
+                vals.append(v.reshape(-1)[:ow[i] * oh[i]])
+            d.outgassing_map_width = p(ow, C.c_int32)
+            d.outgassing_map_height = p(oh, C.c_int32)
+            d.outgassing_map_ratio_u = p(oru, C.c_double)
+            d.outgassing_map_ratio_v = p(orv, C.c_double)
+            d.outgassing_map = p(np.concatenate(vals), C.c_double)
         gh = A.HistogramParams()
         for k in HIST_FIELDS:
             setattr(gh, k, type(getattr(gh, k))(self.global_histogram[k]))

@@ -235,6 +235,16 @@ def load(path_or_bytes, with_state=True, catalog=()):
                 m.desorb_anglemaps[k] = np.array([int(float(x)) for x in txt.split()], np.uint64)
         elif m.desorb_type[k] == A.DES_ANGLEMAP:
             m.desorb_type[k] = A.DES_NONE
+        # outgassing map (MolflowFacet.cpp:249-285): used only when the Outgassing node asks for it
+        # and the DynamicOutgassing node has a map; the old format has one square ratio
+        dyn = f.find("DynamicOutgassing")
+        if _i(og, "useOutgassingFile") and dyn is not None and dyn.find("map") is not None:
+            w, h = _i(dyn, "width"), _i(dyn, "height")
+            ru = _f(dyn, "ratioU", _f(dyn, "ratio"))
+            rv = _f(dyn, "ratioV", _f(dyn, "ratio"))
+            vals = np.array([float(x) for x in (dyn.find("map").text or "").split()], np.float64)
+            if w > 0 and h > 0 and vals.size >= w * h:
+                m.outgassing_maps[k] = dict(width=w, height=h, ratio_u=ru, ratio_v=rv, values=vals[:w * h].reshape(h, w))
         hp = _hist_params(f.find("Histograms"))
         for key, val in hp.items():
             getattr(m, "hist_" + key)[k] = val

@@ -191,6 +191,8 @@ typedef struct {
     /* desorption */
     int id_idx;            /* integrated desorption table index, -1 none */
     struct oamap* amd;     /* angle-map desorption tables, NULL unless DES_ANGLEMAP */
+    int og_w, og_h;        /* outgassing-map grid (0: none) and its extent in cells over U, V */
+    double og_wp, og_hp;
 } ofacet;
 
 typedef struct { double bmin[3], bmax[3]; int left, right, first, count; } onode;
@@ -438,7 +440,7 @@ struct orc_model {
     double cdf_v[MAXWELL_CDF_N], cdf_p[MAXWELL_CDF_N];
     int nparams; oparam* params;
     int nid; oid* ids;
-    double* src_prefix; int* src_facet; int nsrc; double src_total;
+    double* src_prefix; int* src_facet; int* src_cell; int nsrc; double src_total;
     int motion_type; double mv1[3], mv2[3];                 /* moving facets */
     int scatter, scatter_cutoff;                            /* background-gas scattering */
     double sc_mass_ratio, sc_mfp, sc_rho, sc_cutoff_speed;
@@ -893,20 +895,57 @@ int orc_model_create(const mfg_model_desc* d, orc_model** out, char* err, size_t
         }
     }
     free(pid2id);
-    /* source table: StartFromSource facet weights (Particle.cpp:421-464) */
-    M->src_prefix = (double*)malloc(sizeof(double) * (M->nf + 1));
-    M->src_facet = (int*)malloc(sizeof(int) * (M->nf + 1));
-    M->nsrc = 0;
-    double sum = 0;
+    /* source table: StartFromSource facet weights (Particle.cpp:421-464).  A facet with an
+     * outgassing map desorbs by its cells (Particle.cpp:425-446; MolflowSimGeom.cpp:303-310):
+     * here one entry per cell of non-zero rate, searched like the facets. */
+    size_t nmapcells = 0;
     for (int i = 0; i < M->nf; ++i) {
         ofacet* F = &M->f[i];
+        F->og_w = OPT(d->outgassing_map_width, i, 0);
+        F->og_h = OPT(d->outgassing_map_height, i, 0);
+        if (F->og_w > 0 && F->og_h > 0) {
+            if (!d->outgassing_map) { set_err(err, errlen, "outgassing map missing"); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL; }
+            F->og_wp = sqrt(dot3(F->U, F->U)) * OPT(d->outgassing_map_ratio_u, i, 0.0);
+            F->og_hp = sqrt(dot3(F->V, F->V)) * OPT(d->outgassing_map_ratio_v, i, 0.0);
+            if (!(F->og_wp > F->og_w - 1.0 && F->og_hp > F->og_h - 1.0)) {
+                set_err(err, errlen, "outgassing map has more cells than its ratio puts on the facet"); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL;
+            }
+            nmapcells += (size_t)F->og_w * F->og_h;
+        } else F->og_w = F->og_h = 0;
+    }
+    M->src_prefix = (double*)malloc(sizeof(double) * (M->nf + nmapcells + 1));
+    M->src_facet = (int*)malloc(sizeof(int) * (M->nf + nmapcells + 1));
+    M->src_cell = (int*)malloc(sizeof(int) * (M->nf + nmapcells + 1));
+    M->nsrc = 0;
+    double sum = 0;
+    size_t cursor = 0;
+    for (int i = 0; i < M->nf; ++i) {
+        ofacet* F = &M->f[i];
+        const int ncell = F->og_w * F->og_h;
+        const double* cells = ncell ? d->outgassing_map + cursor : NULL;
+        cursor += (size_t)ncell;
         if (F->desorb_type == MFG_DES_NONE) continue;
+        if (ncell) {
+            double tot = 0;
+            for (int c = 0; c < ncell; ++c) {
+                if (!(cells[c] >= 0)) { set_err(err, errlen, "negative outgassing-map cell"); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL; }
+                tot += cells[c];
+            }
+            if (!(tot > 0)) continue;
+            if (F->structure == -1) { set_err(err, errlen, "a facet in all structures cannot desorb"); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL; }
+            for (int c = 0; c < ncell; ++c) {
+                if (!(cells[c] > 0)) continue;
+                sum += M->latest * cells[c] / (KB_MOLFLOW * F->temperature);
+                M->src_prefix[M->nsrc] = sum; M->src_facet[M->nsrc] = i; M->src_cell[M->nsrc] = c; M->nsrc++;
+            }
+            continue;
+        }
         double w = (F->id_idx >= 0 ? M->ids[F->id_idx].cum[M->ids[F->id_idx].n - 1] : M->latest * F->outgassing)
                    / (KB_MOLFLOW * F->temperature);
         if (!(w > 0)) continue;
         if (F->structure == -1) { set_err(err, errlen, "a facet in all structures cannot desorb"); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL; }
         sum += w;
-        M->src_prefix[M->nsrc] = sum; M->src_facet[M->nsrc] = i; M->nsrc++;
+        M->src_prefix[M->nsrc] = sum; M->src_facet[M->nsrc] = i; M->src_cell[M->nsrc] = -1; M->nsrc++;
     }
     M->src_total = sum;
     /* layout + texture increments (Initializer.cpp:433-456) */
@@ -976,7 +1015,7 @@ void orc_model_destroy(orc_model* M) {
     free(M->params);
     if (M->ids) for (int k = 0; k < M->nid; ++k) { free(M->ids[k].t); free(M->ids[k].cum); }
     free(M->ids);
-    free(M->src_prefix); free(M->src_facet);
+    free(M->src_prefix); free(M->src_facet); free(M->src_cell);
     free(M->fhist);
     if (M->f) for (int i = 0; i < M->nf; ++i) oamap_free(M->f[i].amd);
     free(M->f);
@@ -1271,6 +1310,7 @@ static int start_from_source(const orc_model* M, otally* T, rng_t* r, opart* P) 
     while (lo < hi) { int mid = (lo + hi) >> 1; if (M->src_prefix[mid] > sr) hi = mid; else lo = mid + 1; }
     if (lo >= M->nsrc) return 0;
     int fi = M->src_facet[lo];
+    const int cell = M->src_cell[lo];
     const ofacet* F = &M->f[fi];
     int reverse = F->two_sided ? (rnd(r) > 0.5) : 0;
     P->last = fi;
@@ -1290,14 +1330,28 @@ static int start_from_source(const orc_model* M, otally* T, rng_t* r, opart* P) 
     P->scatter_at = M->scatter ? -M->sc_mfp * log(1.0 - rnd(r)) : 1e100;
     P->bounces = 0; P->dist = 0;
     int found = 0;
+    /* outgassing-map cell (Particle.cpp:513-535): u, v uniform in the cell, the last column and
+     * row of the grid only as far as the facet reaches */
+    const int cw = cell >= 0 ? cell % F->og_w : 0, ch = cell >= 0 ? cell / F->og_w : 0;
     for (int tries = 0; tries < 1000 && !found; ++tries) {
-        double u = rnd(r), v = rnd(r);
+        double u, v;
+        if (cell >= 0) {
+            u = (cw < F->og_w - 1) ? (cw + rnd(r)) / F->og_wp : (cw + rnd(r) * (F->og_wp - (F->og_w - 1.0))) / F->og_wp;
+            v = (ch < F->og_h - 1) ? (ch + rnd(r)) / F->og_hp : (ch + rnd(r) * (F->og_hp - (F->og_h - 1.0))) / F->og_hp;
+        } else {
+            u = rnd(r); v = rnd(r);
+        }
         if (in_polygon(M->v2 + 2 * F->vstart, F->nv, u, v)) {
             for (int k = 0; k < 3; ++k) P->o[k] = F->O[k] + u * F->U[k] + v * F->V[k];
             P->u = u; P->v = v; found = 1;
         }
     }
-    if (!found) { P->u = 0.5; P->v = 0.5; for (int k = 0; k < 3; ++k) P->o[k] = F->center[k]; }
+    if (!found) {
+        if (cell >= 0) {   /* the cell's centre */
+            P->u = (cw + 0.5) / F->og_wp; P->v = (ch + 0.5) / F->og_hp;
+            for (int k = 0; k < 3; ++k) P->o[k] = F->O[k] + P->u * F->U[k] + P->v * F->V[k];
+        } else { P->u = 0.5; P->v = 0.5; for (int k = 0; k < 3; ++k) P->o[k] = F->center[k]; }
+    }
     double th, ph;
     switch (F->desorb_type) {
         case MFG_DES_UNIFORM: th = acos(rnd(r)); ph = rnd(r) * 2.0 * PI_D; break;
