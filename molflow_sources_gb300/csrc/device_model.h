@@ -59,6 +59,7 @@ struct __align__(16) PolyF { float cu, cv, su, sv, rin2, rout2; int32_t vstart, 
 #define FF_FAST_REFL   256u   // diffuse, full accommodation, Maxwell speeds, no sojourn, constant temperature
 #define FF_LINK        512u   // structure link: the particle passes into structure FacetInfo2::link
 #define FF_MOVING      1024u  // moving facet: its velocity is added to particles leaving it
+#define FF_TELEPORT    2048u  // teleport source: the particle leaves FacetInfo2::teleport instead
 
 // Per-facet physics record (FP64, 128 B).
 struct __align__(16) FacetPhysD {
@@ -87,6 +88,8 @@ struct __align__(16) FacetInfo2 {
     double am_limit, max_speed, desorb_exp, temperature;
     double opacity;
     int32_t opac_param, link;   // link: destination structure of a link facet, -1 none
+    int32_t teleport;           // teleportDest: 0 none, -1 the facet last teleported to, k facet k-1
+    int32_t pad_t;
 };
 
 // Device-resident tallies.  Fixed-point scales: velocities (m/s) * 2^20,

@@ -573,10 +573,14 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     auto unsupported = [&](const std::string& why) {
         if (m.gpu_supported) { m.gpu_supported = false; m.gpu_unsupported_reason = why; }
     };
-    for (int i = 0; i < nf; ++i) {
-        std::string f = "facet " + std::to_string(i + 1) + ": ";
-        if (m.teleport[i]) unsupported(f + "teleport");
-        if (m.p_temp[i] >= 0 && m.sojourn[i]) {}
+    (void)unsupported;
+    for (int i = 0; i < nf; ++i) {   // teleport destinations (PerformTeleport, Particle.cpp:83-121)
+        const int t = m.teleport[i];
+        if (t < -1) { err = "facet " + std::to_string(i + 1) + ": teleport destination out of range"; return MFG_ERR_INVALID_MODEL; }
+        if (t > 0 && t <= nf && m.structure[t - 1] == -1) {
+            err = "facet " + std::to_string(i + 1) + ": teleport destination is in all structures";
+            return MFG_ERR_INVALID_MODEL;
+        }
     }
 
     // layout + texture increments (Initializer.cpp:433-456)
@@ -962,7 +966,7 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
                    (m.p_stick[i] >= 0 ? FF_STICK_PARAM : 0) | (m.p_temp[i] >= 0 ? FF_TEMP_PARAM : 0) |
                    (m.sojourn[i] ? FF_SOJOURN : 0) | (m.ang_off[i] >= 0 ? FF_ANGLEMAP : 0) |
                    (m.prof_idx[i] >= 0 ? FF_PROFILE : 0) | (m.diffuse[i] > 0.999999 ? FF_DIFFUSE_ONLY : 0) |
-                   (m.link[i] ? FF_LINK : 0);
+                   (m.link[i] ? FF_LINK : 0) | (m.teleport[i] ? FF_TELEPORT : 0);
         if (m.diffuse[i] > 0.999999 && m.accommodation[i] > 0.9999 && m.use_maxwell && !m.sojourn[i] && m.p_temp[i] < 0 &&
             !m.moving[i])
             in.flags |= FF_FAST_REFL;
@@ -986,6 +990,7 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
         i2.opacity = m.opacity[i];
         i2.opac_param = m.p_opac[i];
         i2.link = m.link[i] ? m.link[i] - 1 : -1;
+        i2.teleport = m.teleport[i];
         i2.am_limit = m.am_limit[i];
         i2.max_speed = m.max_speed[i];
         i2.desorb_exp = m.desorb_exp[i];
@@ -1001,7 +1006,8 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     m.instances.assign(1, inst);
     bool any_moving = false;
     for (int i = 0; i < nf; ++i) any_moving = any_moving || m.moving[i];
-    m.has_ext = m.has_transparent || m.layout.histogram_bins > 0 || m.low_flux || m.scatter || any_moving || !m.am_dev.empty();
+    m.has_ext = m.has_transparent || m.layout.histogram_bins > 0 || m.low_flux || m.scatter || any_moving || !m.am_dev.empty() ||
+                std::any_of(m.teleport.begin(), m.teleport.end(), [](int32_t t) { return t != 0; });
     return MFG_OK;
 }
 
@@ -1020,8 +1026,9 @@ int merge_host_models(const std::vector<const HostModel*>& parts, HostModel& out
     for (const HostModel* p : parts) {
         if (p->layout.histogram_bins > 0) { err = "histograms are not recorded in batched instances"; return MFG_ERR_UNSUPPORTED_FEATURE; }
         if (p->low_flux) { err = "low-flux mode is not traced in batched instances"; return MFG_ERR_UNSUPPORTED_FEATURE; }
-        if (p->scatter || p->motion_type || !p->am_dev.empty() || !p->og.empty()) {
-            err = "scattering, moving facets, angle-map desorption and outgassing maps are not traced in batched instances";
+        if (p->scatter || p->motion_type || !p->am_dev.empty() || !p->og.empty() ||
+            std::any_of(p->teleport.begin(), p->teleport.end(), [](int32_t t) { return t != 0; })) {
+            err = "scattering, moving facets, angle-map desorption, outgassing maps and teleports are not traced in batched instances";
             return MFG_ERR_UNSUPPORTED_FEATURE;
         }
     }

@@ -185,6 +185,7 @@ struct ParticleState {
     uint64_t refl;
     double ori;
     double scat_at;        // flight distance (cm) of the next background-gas collision
+    int tele_from;         // teleportedFrom: destination of the last teleport, -1 none
 };
 
 // ProfileFacet (Particle.cpp:1026-1085); profiles are tallied in global memory
@@ -563,6 +564,46 @@ __device__ __noinline__ double transparent_pass(const DevModel& M, const DevTall
     return (double)ort;
 }
 
+// PerformTeleport (Particle.cpp:76-183), after the hit on facet f was recorded as a pass: the
+// direction keeps its angles to the facet basis, now taken on the destination's basis (the polar
+// round trip written as a projection), the particle starts at the same (u,v) on the destination,
+// or, when that point is outside the destination polygon, at a uniform point of it (at most 1000
+// draws: the reference's try counter never stops the loop, Particle.cpp:152-161).  The source's
+// facet counter adds the velocity sums of the outgoing direction against its own normal.
+template <bool kFP32, class Rng, class R>
+__device__ __noinline__ void teleport_to(const DevModel& M, const DevTally& T, const BlockTally& B, int f, int dest,
+                                         Rng& rng, double time, R vel, double u, double v, double& ox, double& oy,
+                                         double& oz, R& dx, R& dy, R& dz) {
+    const FacetPhysD& Pf = M.phys_d[f];
+    const FacetPhysD& Pd = M.phys_d[dest];
+    const double* Nf = M.isect_d[f].v;
+    const double* Nd = M.isect_d[dest].v;
+    const double ddx = (double)dx, ddy = (double)dy, ddz = (double)dz;
+    const double a = ddx * Pf.nU[0] + ddy * Pf.nU[1] + ddz * Pf.nU[2];
+    const double b = ddx * Pf.nV[0] + ddy * Pf.nV[1] + ddz * Pf.nV[2];
+    const double c = ddx * Nf[0] + ddy * Nf[1] + ddz * Nf[2];
+    const double ex = a * Pd.nU[0] + b * Pd.nV[0] + c * Nd[0];
+    const double ey = a * Pd.nU[1] + b * Pd.nV[1] + c * Nd[1];
+    const double ez = a * Pd.nU[2] + b * Pd.nV[2] + c * Nd[2];
+    if (!in_facet_d(M, dest, u, v)) {
+        for (int tr = 0; tr < 1000; ++tr) {
+            const double u2 = (double)rng.next(), v2 = (double)rng.next();
+            if (in_facet_d(M, dest, u2, v2)) { u = u2; v = v2; break; }
+        }
+    }
+    const FacetIsectD& Rd = M.isect_d[dest];
+    const PolyD& PD = M.poly_d[dest];
+    const double ua = u * PD.su * PD.su, vb = v * PD.sv * PD.sv;   // O + u*U + v*V (record keeps U/|U|^2)
+    ox = Rd.v[4] + ua * Rd.v[8] + vb * Rd.v[12];
+    oy = Rd.v[5] + ua * Rd.v[9] + vb * Rd.v[13];
+    oz = Rd.v[6] + ua * Rd.v[10] + vb * Rd.v[14];
+    dx = (R)ex; dy = (R)ey; dz = (R)ez;
+    const double ort = (double)vel * fabs(ex * Nf[0] + ey * Nf[1] + ez * Nf[2]);
+    const unsigned long long q1 = qd(2.0 / ort, MFG_SCALE_INV), q2 = qd(2.0 * ort, MFG_SCALE_V);
+    facet_add(M, T, B, f, 0, 0, 0, 0, q1, q2, 0);
+    if (M.nm) for_moments(M, time, [&](int m) { facet_add(M, T, B, f, m, 0, 0, 0, q1, q2, 0); });
+}
+
 // General relaunch (any accommodation, temperature parameter, sojourn time, reflection
 // mix): UpdateVelocity, sojourn, diffuse / specular / cos^N direction, with the random
 // numbers drawn in the order of PerformBounce (Particle.cpp:769-802).
@@ -776,6 +817,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                     P.gen_time = P.time;
                     P.refl = 0;
                     P.ori = 1.0;
+                    P.tele_from = -1;
                 }
                 if (kSens) {
                     ntraj = 0;
@@ -1101,6 +1143,31 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                 }
             }
             continue;
+        }
+        if constexpr (kExt) {
+            if (In.flags & FF_TELEPORT) {   // teleport instead of stick or reflect (Particle.cpp:326-329)
+                const int tp = M.info2[hf].teleport;
+                const int dest = tp == -1 ? P.tele_from : tp - 1;
+                if (dest >= 0 && dest < M.nf) {
+                    // recorded like a transparent pass with the incoming direction, one hit and no sums
+                    transparent_pass<kFP32>(M, T, B, hf, (R)0, hu, hv, P.time, vel, dx, dy, dz, true);
+                    teleport_to<kFP32>(M, T, B, hf, dest, rng, P.time, vel, (double)hu, (double)hv, P.ox, P.oy, P.oz, dx,
+                                       dy, dz);
+                    P.structure = M.info2[dest].structure;
+                    P.tele_from = dest;
+                    P.last = dest;
+                } else {
+                    P.last = hf;    // no destination: the particle passes on through the facet
+                }
+                relink = true;
+                need_new = false;
+                if (++P.bounces > max_steps) {   // step cap
+                    ++c_drop;
+                    relink = false;
+                    need_new = true;
+                }
+                continue;
+            }
         }
         // sticking; the regular mode draws stick or reflect (Particle.cpp:323-336), low-flux mode
         // splits the particle into an absorbed part wa and a reflected part wr (:338-356)

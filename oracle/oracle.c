@@ -831,9 +831,9 @@ int orc_model_create(const mfg_model_desc* d, orc_model** out, char* err, size_t
                 set_err(err, errlen, msg); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL;
             }
         }
-        if (F->teleport) {
-            snprintf(msg, sizeof msg, "facet %d: teleport not traced by the oracle", i + 1);
-            set_err(err, errlen, msg); orc_model_destroy(M); return MFG_ERR_UNSUPPORTED_FEATURE;
+        if (F->teleport < -1) {
+            snprintf(msg, sizeof msg, "facet %d: teleport destination out of range", i + 1);
+            set_err(err, errlen, msg); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL;
         }
         if (F->structure < -1 || F->structure >= M->nstruct) { set_err(err, errlen, "structure index out of range"); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL; }
         int textured = (F->texw_p * F->texh_p) > 0;   /* isTextured (LoaderXML.cpp:1111) */
@@ -948,6 +948,12 @@ int orc_model_create(const mfg_model_desc* d, orc_model** out, char* err, size_t
         M->src_prefix[M->nsrc] = sum; M->src_facet[M->nsrc] = i; M->src_cell[M->nsrc] = -1; M->nsrc++;
     }
     M->src_total = sum;
+    for (int i = 0; i < M->nf; ++i) {   /* a teleport into a facet of all structures has no structure to go on in */
+        const int t = M->f[i].teleport;
+        if (t > 0 && t <= M->nf && M->f[t - 1].structure == -1) {
+            set_err(err, errlen, "teleport destination is in all structures"); orc_model_destroy(M); return MFG_ERR_INVALID_MODEL;
+        }
+    }
     /* layout + texture increments (Initializer.cpp:433-456) */
     mfg_state_layout* L = &M->L;
     memset(L, 0, sizeof *L);
@@ -1142,6 +1148,7 @@ typedef struct {
     double o[3], d[3];
     double time, velocity, ori, dist, gen_time, decay_at, scatter_at;
     int last, structure;
+    int tele_from;  /* teleportedFrom: destination of the last teleport, -1 none */
     uint64_t bounces;
     double u, v;   /* facetHitDetails of the current facet */
 } opart;
@@ -1328,6 +1335,7 @@ static int start_from_source(const orc_model* M, otally* T, rng_t* r, opart* P) 
     } else P->decay_at = 1e100;
     /* free path to the first background-gas collision (Particle.cpp:500-504) */
     P->scatter_at = M->scatter ? -M->sc_mfp * log(1.0 - rnd(r)) : 1e100;
+    P->tele_from = -1;
     P->bounces = 0; P->dist = 0;
     int found = 0;
     /* outgassing-map cell (Particle.cpp:513-535): u, v uniform in the cell, the last column and
@@ -1455,6 +1463,43 @@ static void update_velocity(const orc_model* M, const ofacet* F, rng_t* r, opart
         else new2 = 29369.939 * (temp / M->gas_mass);
         P->velocity = sqrt(old2 + (new2 - old2) * F->accommodation);
     }
+}
+
+/* PerformTeleport (Particle.cpp:76-183): the hit on facet fi is recorded like a transparent pass
+ * (texture, direction, profile, angle map with the incoming direction); the particle leaves the
+ * destination facet at the same (u,v) with the same angles to the destination's basis (the
+ * reference's polar round trip, written as the projection onto the destination basis), in the
+ * destination's structure.  The facet counter takes one hit and the velocity sums of the
+ * outgoing direction against the source normal; the global hit count is not increased.  A
+ * destination -1 means the facet the particle last teleported to; without one (or with an
+ * invalid one) the particle passes on through fi.  When (u,v) is outside the destination
+ * polygon, new points are drawn until one is inside: the reference draws without limit (its try
+ * counter sits outside the loop); here at most 1000 draws, then the mapped point is kept. */
+static void perform_teleport(const orc_model* M, otally* T, int fi, rng_t* r, opart* P) {
+    const ofacet* F = &M->f[fi];
+    const int dest = F->teleport == -1 ? P->tele_from : F->teleport - 1;
+    if (dest < 0 || dest >= M->nf) { P->last = fi; return; }
+    const ofacet* D = &M->f[dest];
+    P->structure = D->structure;
+    P->tele_from = dest;
+    int ms[256]; int nms = moments_of(M, P->time, ms, 256);
+    if (F->count & MFG_COUNT_TRANS) texture_hit(M, T, ms, nms, F, P, 1, 2.0, 2.0);
+    if ((F->count & MFG_COUNT_DIR) && F->dir_off >= 0) direction_hit(M, T, ms, nms, F, P);
+    profile_hit(M, T, ms, nms, F, P, 1, 2.0, 2.0);
+    if (F->ang_off >= 0) anglemap_hit(M, T, F, P);
+    const double a = dot3(P->d, F->nU), b = dot3(P->d, F->nV), c = dot3(P->d, F->N);
+    for (int k = 0; k < 3; ++k) P->d[k] = a * D->nU[k] + b * D->nV[k] + c * D->N[k];
+    double u = P->u, v = P->v;
+    if (!in_polygon(M->v2 + 2 * D->vstart, D->nv, u, v)) {
+        for (int tries = 0; tries < 1000; ++tries) {
+            const double u2 = rnd(r), v2 = rnd(r);
+            if (in_polygon(M->v2 + 2 * D->vstart, D->nv, u2, v2)) { u = u2; v = v2; break; }
+        }
+    }
+    for (int k = 0; k < 3; ++k) P->o[k] = D->O[k] + u * D->U[k] + v * D->V[k];
+    P->last = dest;
+    const double ort = P->velocity * fabs(dot3(P->d, F->N));
+    facet_counter(M, T, ms, nms, fi, 1, 0, 0, 2.0 / ort, 2.0 * (M->use_maxwell ? 1.0 : 1.1781) * ort, P);
 }
 
 /* PerformBounce (Particle.cpp:691-838), no moving facets */
@@ -1617,6 +1662,7 @@ static int trace_particle(const orc_model* M, otally* T, rng_t* r, uint64_t max_
         }
         T->global[MFG_G_DIST_TOTAL] += travel; T->global[MFG_G_DIST_FULLHITS] += travel; P.dist += travel;
         P.u = H.u; P.v = H.v;
+        if (F->teleport) { perform_teleport(M, T, fi, r, &P); continue; }   /* Particle.cpp:326-329 */
         double s = (F->p_stick >= 0) ? param_at(M, F->p_stick, P.time) : F->sticking;
         if (!M->low_flux) {
             if (s == 1.0 || (s > 0.0 && rnd(r) < s)) { record_absorb(M, T, fi, &P); st->hits++; return 0; }

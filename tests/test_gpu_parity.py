@@ -11,7 +11,7 @@ import pytest
 
 from molflow_sources_gb300 import _abi as A
 from molflow_sources_gb300.model import build_pipe, config1_tube
-from molflow_sources_gb300.simulation import GpuSimulation, MfgError
+from molflow_sources_gb300.simulation import GpuBatch, GpuSimulation, MfgError
 from oracle.oracle import Oracle
 from tests import golden_util
 from tests.stats import batch_means, binom_sigma, z_threshold, zscores
@@ -253,7 +253,7 @@ def test_autotune_and_occupancy_variants_agree(tube):
     """Every launch shape gives identical FP32R tallies for the same particles."""
     sim = GpuSimulation(tube)
     ref = None
-    for bps in (2, 3, 4):
+    for bps in (2, 3, 4, 6, 8):
         sim.ResetSimulation()
         sim.set_particle_offset(0)
         sim.SimulationMCStep(20000, precision=A.PREC_FP32R, seed=SEED, blocks_per_sm=bps)
@@ -262,14 +262,14 @@ def test_autotune_and_occupancy_variants_agree(tube):
             ref = st
         assert np.array_equal(st.facet_counts, ref.facet_counts)
     best = sim.autotune(20000)
-    assert best["block_size"] in (128, 256)
+    assert best["block_size"] == 256 and best["blocks_per_sm"] in (2, 3, 4, 6, 8)
     assert sim.fetch().n_desorbed == 0
 
 
 def test_unsupported_feature_is_reported():
+    """Teleports are traced in single models but not in batches: the merge reports it."""
     m = config1_tube()
     m.teleport_dest[5] = 3
-    sim = GpuSimulation(m)
     with pytest.raises(MfgError) as e:
-        sim.SimulationMCStep(10)
+        GpuBatch([config1_tube(), m])
     assert e.value.code == A.MFG_ERR_UNSUPPORTED_FEATURE
