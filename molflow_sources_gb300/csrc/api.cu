@@ -95,7 +95,27 @@ struct mfg_sim {
     size_t sens_bytes = 0;
     void* sens_block = nullptr;
     std::vector<double> js, jq, jy;
+    // pinned staging of the tallies for mfg_fetch (allocated at the first fetch, kept)
+    unsigned long long* h_stage = nullptr;
+    size_t stage_words = 0;
 };
+
+// Runs fn(begin, end) over [0, n) on up to 16 host threads (one when n is small): the conversion
+// of fixed-point tallies into the caller's FP64 layout, tens of MB for a 200k-facet model.
+template <class Fn>
+static void parallel_range(size_t n, Fn fn) {
+    const size_t grain = 1 << 16;
+    unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    nt = unsigned(std::min<size_t>(nt, (n + grain - 1) / grain));
+    if (nt <= 1) { fn(size_t(0), n); return; }
+    std::vector<std::thread> th;
+    const size_t chunk = (n + nt - 1) / nt;
+    for (unsigned t = 0; t < nt; ++t) {
+        const size_t b = size_t(t) * chunk, e = std::min(n, b + chunk);
+        if (b < e) th.emplace_back(fn, b, e);
+    }
+    for (auto& x : th) x.join();
+}
 
 extern "C" {
 
@@ -365,6 +385,7 @@ void mfg_sim_destroy(mfg_sim* s) {
     for (void* p : s->owned) cudaFree(p);
     if (s->h_abort) cudaFreeHost(s->h_abort);
     if (s->h_run) cudaFreeHost(s->h_run);
+    if (s->h_stage) cudaFreeHost(s->h_stage);
     if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
     if (s->sens_block) cudaFree(s->sens_block);
     if (s->ev0) cudaEventDestroy(s->ev0);
@@ -643,19 +664,34 @@ static int fetch_range(mfg_sim* s, mfg_state_view* v, int fb, int nf, int64_t tb
     const double f = h.use_maxwell ? 1.0 : 1.1781;
     const size_t B = 1 + size_t(h.nm);
     const size_t NF = size_t(h.nf), NT = size_t(h.layout.texture_cells), NP = size_t(h.layout.profile_facets) * MFG_PROFILE_SIZE;
-    std::vector<unsigned long long> g(TG_N), fa(s->n_facet), tx(s->n_texture), pr(s->n_profile), am(s->n_anglemap);
-    CK(cudaMemcpyAsync(g.data(), s->dt.global, TG_N * 8, cudaMemcpyDeviceToHost, s->stream));
-    if (s->n_facet) CK(cudaMemcpyAsync(fa.data(), s->dt.facet, s->n_facet * 8, cudaMemcpyDeviceToHost, s->stream));
-    if (s->n_texture && v->texture) CK(cudaMemcpyAsync(tx.data(), s->dt.texture, s->n_texture * 8, cudaMemcpyDeviceToHost, s->stream));
-    if (s->n_profile && v->profile) CK(cudaMemcpyAsync(pr.data(), s->dt.profile, s->n_profile * 8, cudaMemcpyDeviceToHost, s->stream));
-    if (s->n_anglemap && v->anglemap) CK(cudaMemcpyAsync(am.data(), s->dt.anglemap, s->n_anglemap * 8, cudaMemcpyDeviceToHost, s->stream));
+    const size_t words = TG_N + s->n_facet + s->n_texture + s->n_profile + s->n_anglemap;
+    if (s->stage_words < words) {
+        if (s->h_stage) cudaFreeHost(s->h_stage);
+        s->h_stage = nullptr;
+        s->stage_words = 0;
+        CK(cudaMallocHost(&s->h_stage, words * 8));
+        s->stage_words = words;
+    }
+    unsigned long long* const g = s->h_stage;
+    unsigned long long* const fa = g + TG_N;
+    unsigned long long* const tx = fa + s->n_facet;
+    unsigned long long* const pr = tx + s->n_texture;
+    unsigned long long* const am = pr + s->n_profile;
+    CK(cudaMemcpyAsync(g, s->dt.global, TG_N * 8, cudaMemcpyDeviceToHost, s->stream));
+    if (s->n_facet) CK(cudaMemcpyAsync(fa, s->dt.facet, s->n_facet * 8, cudaMemcpyDeviceToHost, s->stream));
+    if (s->n_texture && v->texture) CK(cudaMemcpyAsync(tx, s->dt.texture, s->n_texture * 8, cudaMemcpyDeviceToHost, s->stream));
+    if (s->n_profile && v->profile) CK(cudaMemcpyAsync(pr, s->dt.profile, s->n_profile * 8, cudaMemcpyDeviceToHost, s->stream));
+    if (s->n_anglemap && v->anglemap) CK(cudaMemcpyAsync(am, s->dt.anglemap, s->n_anglemap * 8, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     uint64_t sh = 0, sd = 0, sa = 0;
-    for (size_t m = 0; m < B; ++m)
-        for (int i = 0; i < nf; ++i) {
+    for (int i = 0; i < nf; ++i) {
+        const unsigned long long* t = &fa[(fb + i) * TF_N];
+        sh += t[TF_HITS]; sd += t[TF_DES]; sa += t[TF_ABS];
+    }
+    parallel_range(B * size_t(nf), [&](size_t k0, size_t k1) {
+        for (size_t k = k0; k < k1; ++k) {
+            const size_t m = k / size_t(nf), i = k % size_t(nf);
             const unsigned long long* t = &fa[(m * NF + fb + i) * TF_N];
-            size_t k = m * size_t(nf) + i;
-            if (m == 0) { sh += t[TF_HITS]; sd += t[TF_DES]; sa += t[TF_ABS]; }
             if (v->facet_counts) {
                 v->facet_counts[k * MFG_FC_N + MFG_FC_NBMCHIT] = t[TF_HITS];
                 v->facet_counts[k * MFG_FC_N + MFG_FC_NBDESORBED] = t[TF_DES];
@@ -670,6 +706,7 @@ static int fetch_range(mfg_sim* s, mfg_state_view* v, int fb, int nf, int64_t tb
                 o[MFG_FS_SUM_1_PER_VELOCITY] = u128(t + TF_S1V) / MFG_SCALE_INV;
             }
         }
+    });
     if (v->global) {
         std::fill(v->global, v->global + MFG_G_N, 0.0);
         if (whole) {
@@ -688,14 +725,16 @@ static int fetch_range(mfg_sim* s, mfg_state_view* v, int fb, int nf, int64_t tb
         }
     }
     if (v->texture)
-        for (size_t m = 0; m < B; ++m)
-            for (int64_t c = 0; c < nt; ++c) {
+        parallel_range(B * size_t(nt), [&](size_t k0, size_t k1) {
+            for (size_t k = k0; k < k1; ++k) {
+                const size_t m = k / size_t(nt), c = k % size_t(nt);
                 const unsigned long long* t = &tx[(m * NT + tb + c) * TT_N];
-                double* o = v->texture + (m * size_t(nt) + c) * 3;
+                double* o = v->texture + k * 3;
                 o[0] = double(t[TT_COUNT]);
                 o[1] = u128(t + TT_SVORT) / MFG_SCALE_V * f * h.tex_inc[tb + c];
                 o[2] = u128(t + TT_S1OV) / MFG_SCALE_INV / f;
             }
+        });
     if (v->profile)
         for (size_t m = 0; m < B; ++m)
             for (int64_t c = 0; c < np * MFG_PROFILE_SIZE; ++c) {

@@ -165,6 +165,7 @@ class GpuSimulation:
         self.close()
         self.model = model
         self.gmodel = GpuModel(model)
+        self._scratch = None   # host state reused by UpdateHitsAndLog
         h = C.c_void_p()
         _check(load_library().mfg_sim_create(self.gmodel.h, self.device, C.byref(h)))
         self.h = h
@@ -237,7 +238,9 @@ class GpuSimulation:
 
     def UpdateHitsAndLog(self, global_state: SimuState, lock: threading.Lock = None, timeout_ms=10000):
         """Add this simulation's tallies into global_state and clear them (Particle.cpp:21-73,1294-1312)."""
-        local = self.fetch()
+        if self._scratch is None:
+            self._scratch = SimuState(self.model)
+        local = self.fetch(self._scratch)   # every field is rewritten by the fetch
         if lock is not None:
             if not lock.acquire(timeout=timeout_ms / 1000.0):
                 return False
