@@ -4,8 +4,10 @@
 
 A step traces one batch of desorptions to absorption on the workload's geometry.
 `value` = hits (Sum nbMCHit, src/MolflowCLI.cpp:61-68) per second of device time
-over K timed steps, max over ranks; `e2e` = the same through the public API with
-the tallies read back to host memory every step.  One JSON line on rank 0.
+over K timed steps, max over ranks; `e2e` = the same through the public API
+(SimulationMCStep + UpdateHitsAndLog) over K steps, with the tallies read back to host memory
+and added into a host GlobalSimuState every step, after one untimed step that allocates the
+host buffers.  One JSON line on rank 0.
 Under torchrun each rank traces its own particle range (no data-path collective).
 """
 import argparse
@@ -372,10 +374,13 @@ def main():
     # end to end: public API call + tallies copied to host memory every step
     from molflow_sources_gb300.model import SimuState
     gstate = SimuState(model)
+    # one untimed end-to-end step: host buffers are allocated and first touched here, once
+    sim.SimulationMCStep(n_step, precision=A.PREC_FP32R, seed=seed, **shape)
+    sim.UpdateHitsAndLog(gstate)
     e2e_hits = 0
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    for k in range(max(1, args.steps // 2)):
+    for k in range(max(1, args.steps)):
         sim.SimulationMCStep(n_step, precision=A.PREC_FP32R, seed=seed, **shape)
         e2e_hits += sim.last_stats["hits"]
         sim.UpdateHitsAndLog(gstate)
