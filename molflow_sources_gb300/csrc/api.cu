@@ -200,6 +200,7 @@ static int sim_upload(mfg_sim* s) {
     UP(h.isect_f, isect_f);
     UP(h.poly_d, poly_d);
     UP(h.poly_f, poly_f);
+    UP(h.tri_f, tri_f);
     UP(h.v2_d, v2_d);
     UP(h.v2_f, v2_f);
     UP(h.phys_d, phys_d);

@@ -46,6 +46,10 @@ struct __align__(16) FacetIsectF { float v[16]; };
 //  of a disk certainly inside / a disk containing the polygon; vstart, nv.
 struct __align__(16) PolyD { double cu, cv, su, sv, rin2, rout2; int32_t vstart, nv; };
 struct __align__(16) PolyF { float cu, cv, su, sv, rin2, rout2; int32_t vstart, nv; };
+// Triangle edges for the FP32 test: edge i as a function of (u,v) giving the signed distance (cm)
+// of the point from the edge line, positive inside: e_i = a u + b v + c in e[i] = (a, b, c, 0).
+// All zero for a degenerate triangle (every point then goes to the FP64 test).
+struct __align__(16) TriF { float e[3][4]; };
 
 // Facet flags
 #define FF_TWO_SIDED   1u
@@ -184,6 +188,7 @@ struct DevModel {
     const FacetIsectF* isect_f;
     const PolyD* poly_d;
     const PolyF* poly_f;
+    const TriF* tri_f;             // [nf] edges of triangular facets (unused for other polygons)
     const double2* v2_d;
     const float2* v2_f;
     const FacetPhysD* phys_d;

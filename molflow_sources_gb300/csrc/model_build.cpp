@@ -847,6 +847,7 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     m.isect_f.resize(nf);
     m.poly_d.resize(nf);
     m.poly_f.resize(nf);
+    m.tri_f.assign(nf, TriF{});
     m.phys_d.resize(nf);
     m.phys_f.resize(nf);
     m.info.resize(nf);
@@ -938,6 +939,22 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
         Q.rout2 = float(P.rout2 * (1 + 1e-5));
         Q.vstart = F.vstart;
         Q.nv = F.nv;
+        if (F.nv == 3) {   // edge lines in cm, oriented so that the inside is positive
+            double px[3], py[3];
+            for (int k = 0; k < 3; ++k) { px[k] = pv[2 * k] * su; py[k] = pv[2 * k + 1] * sv; }
+            const double area2 = (px[1] - px[0]) * (py[2] - py[0]) - (px[2] - px[0]) * (py[1] - py[0]);
+            if (area2 != 0) {
+                const double sg = area2 > 0 ? 1.0 : -1.0;
+                for (int k = 0; k < 3; ++k) {
+                    const int j = (k + 1) % 3;
+                    const double ex = px[j] - px[k], ey = py[j] - py[k], len = std::hypot(ex, ey);
+                    // distance of (x, y) = (u su, v sv): sg (ex (y - py_k) - (x - px_k) ey) / len
+                    const double a = -sg * ey * su / len, b = sg * ex * sv / len, c = sg * (px[k] * ey - py[k] * ex) / len;
+                    float* e = m.tri_f[i].e[k];
+                    e[0] = float(a); e[1] = float(b); e[2] = float(c); e[3] = 0.0f;
+                }
+            }
+        }
         FacetPhysD& ph = m.phys_d[i];
         for (int a = 0; a < 3; ++a) { ph.nU[a] = F.nU[a]; ph.nV[a] = F.nV[a]; }
         ph.sticking = m.sticking[i];
@@ -1078,6 +1095,7 @@ int merge_host_models(const std::vector<const HostModel*>& parts, HostModel& out
         out.isect_f.insert(out.isect_f.end(), p.isect_f.begin(), p.isect_f.end());
         for (PolyD q : p.poly_d) { q.vstart += v2_base; out.poly_d.push_back(q); }
         for (PolyF q : p.poly_f) { q.vstart += v2_base; out.poly_f.push_back(q); }
+        out.tri_f.insert(out.tri_f.end(), p.tri_f.begin(), p.tri_f.end());
         out.v2_d.insert(out.v2_d.end(), p.v2_d.begin(), p.v2_d.end());
         out.v2_f.insert(out.v2_f.end(), p.v2_f.begin(), p.v2_f.end());
         out.phys_d.insert(out.phys_d.end(), p.phys_d.begin(), p.phys_d.end());

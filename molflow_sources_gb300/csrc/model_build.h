@@ -75,6 +75,7 @@ struct HostModel {
     std::vector<FacetIsectF> isect_f;
     std::vector<PolyD> poly_d;
     std::vector<PolyF> poly_f;
+    std::vector<TriF> tri_f;
     std::vector<double2> v2_d;
     std::vector<float2> v2_f;
     std::vector<FacetPhysD> phys_d;

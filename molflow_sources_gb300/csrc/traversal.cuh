@@ -369,6 +369,23 @@ __device__ __forceinline__ void trav_step(const DevModel& M, TravF& s, TravStack
         if (P.rin2 > 1e29f) {
             inside = true;                                   // rectangle: [0,1]^2 decided above
             eamb = u < eu || u > 1.0f - eu || v < ev || v > 1.0f - ev;
+        } else if (P.nv == 3) {
+            // triangle: signed distances to the three edge lines; a point within the position
+            // error (plus the rounding of the edge function) of a line is ambiguous
+            const float4* te = reinterpret_cast<const float4*>(M.tri_f + f);
+            bool out = false;
+            inside = true;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float4 e = __ldg(te + k);
+                const float au = e.x * u, bv = e.y * v;
+                const float dist = au + bv + e.z;
+                const float tl = em + 4e-7f * (fabsf(au) + fabsf(bv) + fabsf(e.z));
+                if (dist < -tl) out = true;
+                else if (dist <= tl) eamb = true;
+                inside = inside && dist > tl;
+            }
+            if (out) continue;                               // certainly outside
         } else {
             float du = (u - P.cu) * P.su, dv = (v - P.cv) * P.sv;
             float r = sqrtf(du * du + dv * dv);

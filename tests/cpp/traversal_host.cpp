@@ -43,6 +43,7 @@ extern "C" int trav_run(const mfg_model_desc* d, int64_t n, const double* o, con
     M.isect_f = h.isect_f.data();
     M.poly_d = h.poly_d.data();
     M.poly_f = h.poly_f.data();
+    M.tri_f = h.tri_f.data();
     M.v2_d = h.v2_d.data();
     M.v2_f = h.v2_f.data();
     M.info = h.info.data();
