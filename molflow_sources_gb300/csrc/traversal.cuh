@@ -15,7 +15,8 @@ namespace mfgk {
 
 constexpr int kStack = 64;
 // Traversal stack of one thread (local memory; a shared-memory copy of the first levels was
-// measured 0-5 % slower, as it takes L1 capacity from the BVH nodes).
+// measured slower, 26-36 % under the lockstep traversal, as it takes L1 capacity from the BVH
+// nodes and facet records).
 struct TravStack {
     int sp;
     int loc[kStack];
