@@ -212,6 +212,13 @@ typedef struct mfg_model_desc {
     const double*   outgassing_map_ratio_u;
     const double*   outgassing_map_ratio_v;
     const double*   outgassing_map;
+    /* force measurement (sp.enableForceMeasurement, sp.torqueRefPoint; IncreaseFacetCounter,
+     * Particle.cpp:1194-1230): per facet and moment, the sums of the momentum v*d carried onto the
+     * facet (a leaving particle counts -v*d), of its componentwise squares, and of the torque
+     * (o - ref) x v*d about torque_ref_point (cm x m/s), for desorptions, hits and absorptions;
+     * passes carry none */
+    int32_t  enable_force_measurement;
+    double   torque_ref_point[3];
 } mfg_model_desc;
 
 /*
@@ -238,6 +245,8 @@ typedef struct mfg_state_layout {
     int64_t histogram_bins;        /* bins of one moment block: the global histograms (bounce,
                                       distance, time, those recorded), then each facet's in id order */
     int64_t n_histogram;           /* (1+M)*histogram_bins */
+    int64_t n_force;               /* (1+M)*F*9 with force measurement (impulse, impulse_square,
+                                      impulse_momentum, x y z each), else 0 */
 } mfg_state_layout;
 
 typedef struct mfg_state_view {
@@ -249,6 +258,7 @@ typedef struct mfg_state_view {
     double*   direction;     /* [n_direction] */
     uint64_t* anglemap;      /* [n_anglemap] */
     double*   histogram;     /* [n_histogram] */
+    double*   force;         /* [n_force] */
 } mfg_state_view;
 
 /* Run options (precision, RNG, launch shape). */

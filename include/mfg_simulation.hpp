@@ -45,6 +45,7 @@ struct HostState {
     std::vector<double> facet_sums, texture, profile, direction;
     std::vector<uint64_t> anglemap;
     std::vector<double> histogram;
+    std::vector<double> force;   // impulse, impulse_square, impulse_momentum per facet and moment
     std::timed_mutex mutex;   // simuStateMutex
 
     void resize(const mfg_state_layout& L) {
@@ -57,10 +58,12 @@ struct HostState {
         direction.assign(size_t(L.n_direction), 0.0);
         anglemap.assign(size_t(L.n_anglemap), 0);
         histogram.assign(size_t(L.n_histogram), 0.0);
+        force.assign(size_t(L.n_force), 0.0);
     }
     mfg_state_view view() {
         return mfg_state_view{global.data(), facet_counts.data(), facet_sums.data(), texture.data(),
-                              profile.data(), direction.data(), anglemap.data(), histogram.data()};
+                              profile.data(), direction.data(), anglemap.data(), histogram.data(),
+                              force.empty() ? nullptr : force.data()};
     }
     // GlobalSimuState::operator+= (src/Simulation/MolflowSimGeom.cpp:452-458)
     HostState& operator+=(const HostState& o) {
@@ -72,6 +75,7 @@ struct HostState {
         for (size_t i = 0; i < direction.size(); ++i) direction[i] += o.direction[i];
         for (size_t i = 0; i < anglemap.size(); ++i) anglemap[i] += o.anglemap[i];
         for (size_t i = 0; i < histogram.size(); ++i) histogram[i] += o.histogram[i];
+        for (size_t i = 0; i < force.size(); ++i) force[i] += o.force[i];
         return *this;
     }
 };

@@ -131,6 +131,8 @@ MODEL_DESC_FIELDS = [
     ("outgassing_map_ratio_u", _d),
     ("outgassing_map_ratio_v", _d),
     ("outgassing_map", _d),
+    ("enable_force_measurement", C.c_int32),
+    ("torque_ref_point", C.c_double * 3),
 ]
 
 
@@ -142,7 +144,7 @@ class StateLayout(C.Structure):
     _fields_ = [(n, C.c_int64) for n in (
         "n_facets", "n_moments", "texture_cells", "profile_facets", "direction_cells", "anglemap_cells",
         "n_global", "n_facet_counts", "n_facet_sums", "n_texture", "n_profile", "n_direction", "n_anglemap",
-        "histogram_bins", "n_histogram")]
+        "histogram_bins", "n_histogram", "n_force")]
 
 
 class StateView(C.Structure):
@@ -155,6 +157,7 @@ class StateView(C.Structure):
         ("direction", _d),
         ("anglemap", _u64),
         ("histogram", _d),
+        ("force", _d),
     ]
 
 

@@ -73,6 +73,7 @@ struct mfg_sim {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     size_t n_global = TG_N, n_facet = 0, n_texture = 0, n_profile = 0, n_anglemap = 0, n_dir = 0, n_hist = 0;
     size_t n_lf = 0;   // low-flux equivalent counts: 2 global + facet pairs + texture cells + profile bins
+    size_t n_force = 0;   // force measurement sums
     std::vector<uint64_t> particles_started;   // per instance
     unsigned char* h_run = nullptr;            // pinned RunDesc + prefix + first (staging)
     unsigned char* d_run = nullptr;
@@ -251,6 +252,8 @@ static int sim_upload(mfg_sim* s) {
     M.motion_type = h.motion_type;
     M.scatter = h.scatter;
     for (int k = 0; k < 3; ++k) { M.mv1[k] = h.mv1[k]; M.mv2[k] = h.mv2[k]; }
+    M.force = h.force;
+    for (int k = 0; k < 3; ++k) M.torque_ref[k] = h.torque_ref[k];
     M.scatter_cutoff = h.scatter_cutoff;
     M.pad5 = 0;
     M.sc_mass_ratio = h.sc_mass_ratio;
@@ -300,6 +303,8 @@ static int sim_upload(mfg_sim* s) {
     if ((rc = alloc(&s->dt.dir_count, s->n_dir))) return rc;
     if ((rc = alloc(reinterpret_cast<unsigned long long**>(&s->dt.direction), 3 * s->n_dir))) return rc;
     if ((rc = alloc(reinterpret_cast<unsigned long long**>(&s->dt.histogram), s->n_hist))) return rc;
+    s->n_force = size_t(h.layout.n_force);
+    if ((rc = alloc(reinterpret_cast<unsigned long long**>(&s->dt.force), s->n_force))) return rc;
     if (h.low_flux) {
         const size_t nfc = B * size_t(h.nf) * 2, ntx = B * size_t(h.layout.texture_cells),
                      npr = B * size_t(h.layout.profile_facets) * MFG_PROFILE_SIZE;
@@ -330,6 +335,7 @@ int mfg_reset(mfg_sim* s) {
         CK(cudaMemsetAsync(s->dt.direction, 0, s->n_dir * 24, s->stream));
     }
     if (s->n_hist) CK(cudaMemsetAsync(s->dt.histogram, 0, s->n_hist * 8, s->stream));
+    if (s->n_force) CK(cudaMemsetAsync(s->dt.force, 0, s->n_force * 8, s->stream));
     if (s->n_lf) CK(cudaMemsetAsync(s->dt.lf_glob, 0, s->n_lf * 8, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return MFG_OK;
@@ -749,6 +755,12 @@ static int fetch_range(mfg_sim* s, mfg_state_view* v, int fb, int nf, int64_t tb
         for (int64_t c = 0; c < na; ++c) v->anglemap[c] = am[ab + c];
     if (v->histogram && s->n_hist && whole)
         CK(cudaMemcpy(v->histogram, s->dt.histogram, s->n_hist * 8, cudaMemcpyDeviceToHost));
+    if (v->force && s->n_force) {   // facets [fb, fb+nf) of every moment block
+        std::vector<double> fr(s->n_force);
+        CK(cudaMemcpy(fr.data(), s->dt.force, s->n_force * 8, cudaMemcpyDeviceToHost));
+        for (size_t m = 0; m < B; ++m)
+            std::memcpy(v->force + (m * size_t(nf)) * 9, fr.data() + (m * NF + fb) * 9, size_t(nf) * 9 * 8);
+    }
     if (s->n_lf && whole) {
         // low-flux mode: equivalent (weighted) hits, absorptions and texture / profile counts
         std::vector<double> lf(s->n_lf);

@@ -394,6 +394,25 @@ __device__ __forceinline__ int texture_cell(const DevModel& M, int f, R u, R v) 
 
 // RecordDirectionVector (Particle.cpp:1006-1023): Sum of v*direction and a count per cell,
 // constant flow and every moment window holding t
+// Force measurement (IncreaseFacetCounter, Particle.cpp:1208-1212): the momentum sgn*v*d of the
+// particle onto facet f (sgn = -1 for a particle leaving it), its componentwise squares and its
+// torque about the reference point, weighted by w (oriRatio), in moment 0 and every moment
+// window holding `time`; FP64 atomics
+__device__ __noinline__ void force_add(const DevModel& M, const DevTally& T, int f, double time, double w, double sgn,
+                                       double vel, double dx, double dy, double dz, double ox, double oy, double oz) {
+    const double px = sgn * vel * dx, py = sgn * vel * dy, pz = sgn * vel * dz;
+    const double rx = ox - M.torque_ref[0], ry = oy - M.torque_ref[1], rz = oz - M.torque_ref[2];
+    const double q[9] = {w * px, w * py, w * pz, w * px * px, w * py * py, w * pz * pz,
+                         w * (ry * pz - rz * py), w * (rz * px - rx * pz), w * (rx * py - ry * px)};
+    auto add = [&](int m) {
+        double* b = T.force + ((size_t)m * M.nf + f) * 9;
+#pragma unroll
+        for (int j = 0; j < 9; ++j) atomicAdd(b + j, q[j]);
+    };
+    add(0);
+    if (M.nm) for_moments(M, time, add);
+}
+
 __device__ __noinline__ void direction_add(const DevModel& M, const DevTally& T, int f, double u, double v, double time,
                                            double vx, double vy, double vz) {
     const FacetInfo& In = M.info[f];
@@ -873,6 +892,9 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
             }
             if constexpr (kExt) {
                 if (M.info[fo].flags & FF_MOVING) treat_moving(M, P.ox, P.oy, P.oz, dx, dy, dz, vel);
+                if (M.force)   // desorbed particle onto its source, or reflected particle leaving the facet
+                    force_add(M, T, fo, P.time, P.ori, des ? 1.0 : -1.0, (double)vel, (double)dx, (double)dy, (double)dz,
+                              P.ox, P.oy, P.oz);
             }
             {
                 // outgoing tallies; a reflection's incoming half (pending) is added with them (moment 0)
@@ -1221,6 +1243,9 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
         if (do_abs) {   // RecordAbsorb (Particle.cpp:888-924)
             unsigned long long q1, q2, q3;
             quant(wa, q1, q2, q3);
+            if constexpr (kExt) {
+                if (M.force) force_add(M, T, hf, P.time, wa, 1.0, (double)vel, ddx, ddy, ddz, P.ox, P.oy, P.oz);
+            }
             ++c_abs;
             const int cell = (In.tex_off >= 0 && (In.count & MFG_COUNT_ABS)) ? texture_cell<kFP32>(M, hf, hu, hv) : -1;
             if (In.flags & FF_ANGLEMAP) anglemap_add(M, T, hf, ddx, ddy, ddz);
@@ -1268,6 +1293,9 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
         {   // incoming half of PerformBounce (Particle.cpp:735-767)
             unsigned long long q1, q2, q3;
             quant(wr, q1, q2, q3);
+            if constexpr (kExt) {
+                if (M.force) force_add(M, T, hf, P.time, wr, 1.0, (double)vel, ddx, ddy, ddz, P.ox, P.oy, P.oz);
+            }
             const int cell = (In.tex_off >= 0 && (In.count & MFG_COUNT_REFL)) ? texture_cell<kFP32>(M, hf, hu, hv) : -1;
             if (In.flags & FF_ANGLEMAP) anglemap_add(M, T, hf, ddx, ddy, ddz);
             if (In.count & MFG_COUNT_DIR)

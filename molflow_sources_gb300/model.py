@@ -105,6 +105,9 @@ class Model:
         # outgassing maps (useOutgassingFile): {facet: dict(width, height, ratio_u, ratio_v,
         # values = height x width rates in Pa m^3/s)}
         self.outgassing_maps = {}
+        # sp.enableForceMeasurement, sp.torqueRefPoint (cm)
+        self.enable_force_measurement = 0
+        self.torque_ref_point = (0.0, 0.0, 0.0)
         # sp.globalHistogramParams
         self.global_histogram = dict(record=0, bounce_binsize=1, bounce_max=0, distance_binsize=1.0,
                                      distance_max=0.0, time_binsize=1.0, time_max=0.0)
@@ -191,6 +194,8 @@ class Model:
                 a[:min(n, src.size)] = src[:n]
                 parts.append(a)
             d.desorb_anglemap = p(np.concatenate(parts), C.c_uint64)
+        d.enable_force_measurement = int(self.enable_force_measurement)
+        d.torque_ref_point = (C.c_double * 3)(*map(float, self.torque_ref_point))
         if self.outgassing_maps:
             ow = np.zeros(self.n_facets, np.int32)
             oh = np.zeros(self.n_facets, np.int32)
@@ -278,7 +283,8 @@ class Model:
         return dict(n_facets=self.n_facets, n_moments=nm, blocks=B, texture_cells=int(tc), direction_cells=int(dc),
                     anglemap_cells=int(ac), profile_facets=int(pc), tex_off=tex_off, dir_off=dir_off,
                     ang_off=ang_off, prof_idx=prof_idx, tex_w=w, tex_h=h, histogram_bins=int(hb),
-                    global_hist_sizes=gsz, hist_off=hist_off, hist_sizes=hist_sz)
+                    global_hist_sizes=gsz, hist_off=hist_off, hist_sizes=hist_sz,
+                    force=bool(self.enable_force_measurement))
 
 
 class SimuState:
@@ -296,6 +302,8 @@ class SimuState:
         self.direction = np.zeros((B, L["direction_cells"], 4), np.float64)
         self.anglemap = np.zeros(max(L["anglemap_cells"], 0), np.uint64)
         self.histogram = np.zeros((B, L.get("histogram_bins", 0)), np.float64)
+        # impulse, impulse_square, impulse_momentum (x, y, z each) per facet and moment
+        self.force = np.zeros((B, F, 9) if L.get("force", False) or L.get("n_force", 0) else (B, 0, 9), np.float64)
 
     def view(self):
         v = A.StateView()
@@ -307,11 +315,13 @@ class SimuState:
         v.direction = A.ptr(self.direction, C.c_double)
         v.anglemap = A.ptr(self.anglemap, C.c_uint64)
         v.histogram = A.ptr(self.histogram, C.c_double)
+        v.force = A.ptr(self.force, C.c_double) if self.force.size else None
         return v
 
     def __iadd__(self, other):
         """GlobalSimuState::operator+= (src/Simulation/MolflowSimGeom.cpp:452-458)."""
-        for name in ("global_", "facet_counts", "facet_sums", "texture", "profile", "direction", "anglemap", "histogram"):
+        for name in ("global_", "facet_counts", "facet_sums", "texture", "profile", "direction", "anglemap", "histogram",
+                     "force"):
             getattr(self, name).__iadd__(getattr(other, name))
         return self
 

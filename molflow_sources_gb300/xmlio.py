@@ -283,6 +283,13 @@ def load(path_or_bytes, with_state=True, catalog=()):
                 m.motion_vector2 = (_f(r, "x"), _f(r, "y"), _f(r, "z"))
         m.enable_decay = _i(gas, "enableDecay")
         m.half_life = _f(gas, "halfLife", 1.0)
+        fm = sims.find("MeasureForces")   # LoaderXML.cpp:163-177
+        if fm is not None:
+            m.enable_force_measurement = _i(fm, "enabled")
+            tq = fm.find("Torque")
+            rp = tq.find("refPoint") if tq is not None else None
+            if rp is not None:
+                m.torque_ref_point = (_f(rp, "x"), _f(rp, "y"), _f(rp, "z"))
         lf = sims.find("LowFluxMode")
         m.low_flux_mode = _i(lf, "enabled")
         m.low_flux_cutoff = _f(lf, "cutoff", 1e-7)

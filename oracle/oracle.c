@@ -443,6 +443,7 @@ struct orc_model {
     double* src_prefix; int* src_facet; int* src_cell; int nsrc; double src_total;
     int motion_type; double mv1[3], mv2[3];                 /* moving facets */
     int scatter, scatter_cutoff;                            /* background-gas scattering */
+    int force; double torque_ref[3];                        /* force measurement */
     double sc_mass_ratio, sc_mfp, sc_rho, sc_cutoff_speed;
     ohist ghist;           /* global histograms; offset 0 of each moment block */
     ohist* fhist;          /* per facet, NULL when no facet records */
@@ -765,6 +766,8 @@ int orc_model_create(const mfg_model_desc* d, orc_model** out, char* err, size_t
     M->motion_type = d->motion_type;
     for (int k = 0; k < 3; ++k) { M->mv1[k] = d->motion_vector1[k]; M->mv2[k] = d->motion_vector2[k]; }
     M->scatter = d->scatter_enabled; M->scatter_cutoff = d->scatter_cutoff_enabled;
+    M->force = d->enable_force_measurement != 0;
+    for (int k = 0; k < 3; ++k) M->torque_ref[k] = d->torque_ref_point[k];
     M->sc_mass_ratio = d->scatter_mass_ratio; M->sc_mfp = d->scatter_mean_free_path_cm;
     M->sc_rho = d->scatter_rho; M->sc_cutoff_speed = d->scatter_cutoff_speed;
     M->decay = d->enable_decay; M->half_life = d->half_life; M->gas_mass = d->gas_mass;
@@ -986,6 +989,7 @@ int orc_model_create(const mfg_model_desc* d, orc_model** out, char* err, size_t
     }
     L->histogram_bins = hb;
     L->n_histogram = B * hb;
+    L->n_force = M->force ? B * (int64_t)M->nf * 9 : 0;
     M->texinc = (double*)calloc(L->texture_cells + 1, sizeof(double));
     for (int i = 0; i < M->nf; ++i) {
         ofacet* F = &M->f[i];
@@ -1142,6 +1146,7 @@ typedef struct {
     double* dir;
     uint64_t* ang;
     double* hist;
+    double* force;   /* [(1+M) * nf * 9] with force measurement */
 } otally;
 
 typedef struct {
@@ -1198,6 +1203,21 @@ static void facet_counter(const orc_model* M, otally* T, const int* ms, int nms,
                           double absn, double s1v, double svort, const opart* P) {
     add_moment_block(M, T, 0, fi, hit, des, absn, s1v, svort, P);
     for (int k = 0; k < nms; ++k) add_moment_block(M, T, ms[k], fi, hit, des, absn, s1v, svort, P);
+}
+/* force measurement (IncreaseFacetCounter, Particle.cpp:1208-1212): momentum s*v*d of the particle
+ * onto facet fi (s = -1 for a particle leaving it), its squares and its torque about the
+ * reference point, weighted by oriRatio, in moment 0 and the moments of the event */
+static void force_add(const orc_model* M, otally* T, const int* ms, int nms, int fi, const opart* P, double s) {
+    if (!M->force) return;
+    const double w = P->ori;
+    double p[3], r[3];
+    for (int a = 0; a < 3; ++a) { p[a] = s * P->velocity * P->d[a]; r[a] = P->o[a] - M->torque_ref[a]; }
+    const double q[9] = {w * p[0], w * p[1], w * p[2], w * p[0] * p[0], w * p[1] * p[1], w * p[2] * p[2],
+                         w * (r[1] * p[2] - r[2] * p[1]), w * (r[2] * p[0] - r[0] * p[2]), w * (r[0] * p[1] - r[1] * p[0])};
+    for (int k = -1; k < nms; ++k) {
+        double* b = T->force + ((size_t)((k < 0) ? 0 : ms[k]) * M->nf + fi) * 9;
+        for (int j = 0; j < 9; ++j) b[j] += q[j];
+    }
 }
 /* RecordHitOnTexture (Particle.cpp:978-1004) */
 static void texture_hit(const orc_model* M, otally* T, const int* ms, int nms, const ofacet* F, const opart* P,
@@ -1382,6 +1402,7 @@ static int start_from_source(const orc_model* M, otally* T, rng_t* r, opart* P) 
     double ort = P->velocity * fabs(dot3(P->d, F->N));
     int ms[256]; int nms = moments_of(M, P->time, ms, 256);
     facet_counter(M, T, ms, nms, fi, 0, 1, 0, 2.0 / ort, (M->use_maxwell ? 1.0 : 1.1781) * ort, P);
+    force_add(M, T, ms, nms, fi, P, 1.0);
     profile_hit(M, T, ms, nms, F, P, 0, 2.0, 1.0);
     if (F->count & MFG_COUNT_DES) texture_hit(M, T, ms, nms, F, P, 1, 2.0, 1.0);
     return 1;
@@ -1443,6 +1464,7 @@ static void record_absorb(const orc_model* M, otally* T, int fi, opart* P) {
     int ms[256]; int nms = moments_of(M, P->time, ms, 256);
     double ort = P->velocity * fabs(dot3(P->d, F->N));
     facet_counter(M, T, ms, nms, fi, 1, 0, 1, 2.0 / ort, (M->use_maxwell ? 1.0 : 1.1781) * ort, P);
+    force_add(M, T, ms, nms, fi, P, 1.0);
     profile_hit(M, T, ms, nms, F, P, 1, 2.0, 1.0);
     if (F->ang_off >= 0) anglemap_hit(M, T, F, P);
     record_histograms(M, T, ms, nms, fi, P);
@@ -1525,6 +1547,7 @@ static void perform_bounce(const orc_model* M, otally* T, int fi, rng_t* r, opar
     double vf = M->use_maxwell ? 1.0 : 1.1781;
     int ms[256]; int nms = moments_of(M, P->time, ms, 256);
     facet_counter(M, T, ms, nms, fi, 1, 0, 0, 1.0 / ort, vf * ort, P);
+    force_add(M, T, ms, nms, fi, P, 1.0);
     P->bounces++;
     if (F->count & MFG_COUNT_REFL) texture_hit(M, T, ms, nms, F, P, 1, 1.0, 1.0);
     if ((F->count & MFG_COUNT_DIR) && F->dir_off >= 0) direction_hit(M, T, ms, nms, F, P);
@@ -1555,6 +1578,7 @@ static void perform_bounce(const orc_model* M, otally* T, int fi, rng_t* r, opar
     if (F->moving) treat_moving(M, P);
     ort = P->velocity * fabs(dot3(P->d, F->N));
     facet_counter(M, T, ms, nms, fi, 0, 0, 0, 1.0 / ort, vf * ort, P);
+    force_add(M, T, ms, nms, fi, P, -1.0);
     if (F->count & MFG_COUNT_REFL) texture_hit(M, T, ms, nms, F, P, 0, 1.0, 1.0);
     profile_hit(M, T, ms, nms, F, P, 0, 1.0, 1.0);
     P->last = fi;
@@ -1572,9 +1596,11 @@ static void tally_alloc(const orc_model* M, otally* T) {
     T->dir = (double*)calloc(L->n_direction + 1, sizeof(double));
     T->ang = (uint64_t*)calloc(L->n_anglemap + 1, sizeof(uint64_t));
     T->hist = (double*)calloc(L->n_histogram + 1, sizeof(double));
+    T->force = (double*)calloc(L->n_force + 1, sizeof(double));
 }
 static void tally_free(otally* T) {
     free(T->global); free(T->fc); free(T->fs); free(T->tex); free(T->prof); free(T->dir); free(T->ang); free(T->hist);
+    free(T->force);
 }
 
 /* trace one particle to absorption/leak: the body of SimulationMCStep (Particle.cpp:221-393) */
@@ -1731,6 +1757,7 @@ int orc_run(orc_model* M, uint64_t n_des, const orc_run_opts* o, mfg_state_view*
         if (view->direction) for (int64_t k = 0; k < L->n_direction; ++k) view->direction[k] += T->dir[k];
         if (view->anglemap) for (int64_t k = 0; k < L->n_anglemap; ++k) view->anglemap[k] += T->ang[k];
         if (view->histogram) for (int64_t k = 0; k < L->n_histogram; ++k) view->histogram[k] += T->hist[k];
+        if (view->force) for (int64_t k = 0; k < L->n_force; ++k) view->force[k] += T->force[k];
         st->desorbed += th[t].st.desorbed; st->hits += th[t].st.hits; st->leaks += th[t].st.leaks;
         st->dropped += th[t].st.dropped; st->rays += th[t].st.rays;
         st->node_visits += th[t].st.node_visits; st->prim_tests += th[t].st.prim_tests;
