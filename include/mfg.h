@@ -219,6 +219,10 @@ typedef struct mfg_model_desc {
      * passes carry none */
     int32_t  enable_force_measurement;
     double   torque_ref_point[3];
+    /* BVH split weights, one per facet (RebuildAccelStructure with SplitMethod::ProbSplit,
+     * MolflowSimGeom.cpp:155-169: the share of nbHitEquiv each facet took in a prior run); NULL
+     * builds by the surface-area heuristic alone.  Only the tree changes, never the results. */
+    const double* bvh_facet_weight;
 } mfg_model_desc;
 
 /*

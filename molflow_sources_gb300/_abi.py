@@ -133,6 +133,7 @@ MODEL_DESC_FIELDS = [
     ("outgassing_map", _d),
     ("enable_force_measurement", C.c_int32),
     ("torque_ref_point", C.c_double * 3),
+    ("bvh_facet_weight", _d),
 ]
 
 

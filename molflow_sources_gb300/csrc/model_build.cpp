@@ -225,8 +225,13 @@ struct BuildNode {
     int left = -1, right = -1, first = 0, count = 0, axis = 0;
 };
 
+// Binned SAH build.  With per-facet weights W (the share of the hits a prior run recorded on each
+// facet, RebuildAccelStructure with ProbSplit, MolflowSimGeom.cpp:155-169) the chance that a ray
+// enters a child is taken as the mean of its surface-area fraction and its share of the node's
+// weight, so often-hit facets end up in shallow, tight subtrees.
 int build_rec(std::vector<BuildNode>& out, std::vector<int>& ids, int begin, int end,
-              const std::vector<HostFacet>& F, int leaf_max, int depth, int64_t& max_depth) {
+              const std::vector<HostFacet>& F, int leaf_max, int depth, int64_t& max_depth,
+              const double* W = nullptr) {
     BuildNode nd;
     for (int a = 0; a < 3; ++a) { nd.lo[a] = DBL_MAX; nd.hi[a] = -DBL_MAX; }
     double cmin[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, cmax[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
@@ -249,6 +254,15 @@ int build_rec(std::vector<BuildNode>& out, std::vector<int>& ids, int begin, int
         return me;
     }
     constexpr int NB = 32;
+    auto area = [](const double* lo, const double* hi) {
+        double dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+        return dx * dy + dy * dz + dz * dx;
+    };
+    const double parea = area(nd.lo, nd.hi);
+    double wtot = 0;
+    if (W)
+        for (int k = begin; k < end; ++k) wtot += W[ids[k]];
+    const bool weighted = W && wtot > 0 && parea > 0;
     double best = DBL_MAX;
     int bax = -1;
     double bsplit = 0;
@@ -256,6 +270,7 @@ int build_rec(std::vector<BuildNode>& out, std::vector<int>& ids, int begin, int
         double ext = cmax[ax] - cmin[ax];
         if (!(ext > 0)) continue;
         int cnt[NB] = {0};
+        double bw[NB] = {0};
         double bl[NB][3], bh[NB][3];
         for (int b = 0; b < NB; ++b)
             for (int a = 0; a < 3; ++a) { bl[b][a] = DBL_MAX; bh[b][a] = -DBL_MAX; }
@@ -263,11 +278,13 @@ int build_rec(std::vector<BuildNode>& out, std::vector<int>& ids, int begin, int
             const HostFacet& f = F[ids[k]];
             int b = std::min(NB - 1, std::max(0, int((f.center[ax] - cmin[ax]) / ext * NB)));
             cnt[b]++;
+            if (weighted) bw[b] += W[ids[k]];
             for (int a = 0; a < 3; ++a) { bl[b][a] = std::min(bl[b][a], f.bbmin[a]); bh[b][a] = std::max(bh[b][a], f.bbmax[a]); }
         }
-        double rl[NB][3], rh[NB][3];
+        double rl[NB][3], rh[NB][3], rw[NB];
         int rc[NB];
         for (int b = NB - 1; b >= 0; --b) {
+            rw[b] = bw[b] + (b == NB - 1 ? 0.0 : rw[b + 1]);
             for (int a = 0; a < 3; ++a) {
                 rl[b][a] = (b == NB - 1) ? bl[b][a] : std::min(bl[b][a], rl[b + 1][a]);
                 rh[b][a] = (b == NB - 1) ? bh[b][a] : std::max(bh[b][a], rh[b + 1][a]);
@@ -276,15 +293,17 @@ int build_rec(std::vector<BuildNode>& out, std::vector<int>& ids, int begin, int
         }
         double ll[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, lh[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
         int lc = 0;
+        double lw = 0;
         for (int s = 1; s < NB; ++s) {
             lc += cnt[s - 1];
+            lw += bw[s - 1];
             for (int a = 0; a < 3; ++a) { ll[a] = std::min(ll[a], bl[s - 1][a]); lh[a] = std::max(lh[a], bh[s - 1][a]); }
             if (!lc || !rc[s]) continue;
-            auto area = [](const double* lo, const double* hi) {
-                double dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
-                return dx * dy + dy * dz + dz * dx;
-            };
-            double c = area(ll, lh) * lc + area(rl[s], rh[s]) * rc[s];
+            double c;
+            if (weighted)
+                c = (0.5 * area(ll, lh) / parea + 0.5 * lw / wtot) * lc + (0.5 * area(rl[s], rh[s]) / parea + 0.5 * rw[s] / wtot) * rc[s];
+            else
+                c = area(ll, lh) * lc + area(rl[s], rh[s]) * rc[s];
             if (c < best) { best = c; bax = ax; bsplit = cmin[ax] + ext * double(s) / NB; }
         }
     }
@@ -298,8 +317,8 @@ int build_rec(std::vector<BuildNode>& out, std::vector<int>& ids, int begin, int
         if (mid == begin || mid == end) mid = begin + n / 2;
     }
     out[me].axis = std::max(bax, 0);
-    int l = build_rec(out, ids, begin, mid, F, leaf_max, depth + 1, max_depth);
-    int r = build_rec(out, ids, mid, end, F, leaf_max, depth + 1, max_depth);
+    int l = build_rec(out, ids, begin, mid, F, leaf_max, depth + 1, max_depth, W);
+    int r = build_rec(out, ids, mid, end, F, leaf_max, depth + 1, max_depth, W);
     out[me].left = l;
     out[me].right = r;
     return me;
@@ -768,7 +787,7 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
         }
         std::vector<BuildNode> tree;
         int64_t depth = 0;
-        build_rec(tree, ids, 0, int(ids.size()), m.facets, std::max(1, leaf_max), 0, depth);
+        build_rec(tree, ids, 0, int(ids.size()), m.facets, std::max(1, leaf_max), 0, depth, d->bvh_facet_weight);
         m.bvh_depth = std::max(m.bvh_depth, depth);
         // breadth-first relabel
         std::vector<int> order;

@@ -171,6 +171,19 @@ class GpuSimulation:
         self.h = h
         return 0
 
+    def RebuildAccelStructure(self, global_state: SimuState = None):
+        """Rebuild the BVHs (MolflowSimulationModel::BuildAccelStructure, MolflowSimGeom.cpp:124-184).
+        With a state that holds hits, the splits weigh each facet by its share of the hits
+        (SplitMethod::ProbSplit); without one, by surface area.  Tallies start from zero."""
+        w = None
+        if global_state is not None:
+            h = np.asarray(global_state.facet_sums[0, :, A.FS_NBHITEQUIV], np.float64)
+            if h.sum() > 0:
+                w = h / h.sum()
+        self.model.bvh_facet_weight = w
+        self.LoadSimulation(self.model)
+        return 0
+
     def ResetSimulation(self):
         _check(load_library().mfg_reset(self.h))
 

@@ -49,3 +49,15 @@ def test_fp32_traversal_with_recheck_is_exact(trav, which):
     assert np.array_equal(h64, hf)
     assert np.array_equal(h32, h64)
     assert amb < 1e-3, (amb, rs.tolist())
+
+
+def test_hit_weighted_bvh_gives_the_same_hits(trav):
+    """ProbSplit-style BVH (facets weighted by a prior run's hits) changes the tree, not the hits."""
+    m = workloads.config2_beam_chamber(n_rings=400, length=100.0, n_baffles=6, n_textures=5)
+    r, _ = Oracle(m).run(5000, seed=3)
+    w = r.facet_sums[0, :, A.FS_NBHITEQUIV]
+    m.bvh_facet_weight = w / w.sum()
+    hf, h32, h64, amb, rs = _run(trav, m, 20000, 200000)
+    assert np.array_equal(h64, hf)
+    assert np.array_equal(h32, h64)
+    assert amb < 1e-3
