@@ -223,6 +223,11 @@ typedef struct mfg_model_desc {
      * MolflowSimGeom.cpp:155-169: the share of nbHitEquiv each facet took in a prior run); NULL
      * builds by the surface-area heuristic alone.  Only the tree changes, never the results. */
     const double* bvh_facet_weight;
+    /* particle logger (otfParams.enableLogging, logFacetId, logLimit; LogHit, Particle.cpp:1088-1102):
+     * each desorption from, hit on, absorption on, link pass through and teleport from facet
+     * log_facet (0-based; -1 none) is recorded, up to log_limit records until mfg_reset (mfg_fetch_log) */
+    int32_t  log_facet;
+    int64_t  log_limit;
 } mfg_model_desc;
 
 /*
@@ -345,6 +350,13 @@ int mfg_abort(mfg_sim* sim);                     /* sets the host-mapped abort w
 /* Copy accumulated tallies into the caller's view (overwrites). Replaces
  * UpdateMCHits / GlobalSimuState::operator+= (Particle.cpp:21-73, MolflowSimGeom.cpp:452-458). */
 int mfg_fetch(mfg_sim* sim, mfg_state_view* view);
+
+/* Particle log of the runs since the last mfg_reset (ParticleLog, MolflowSimGeom.h:242-270; merged
+ * by UpdateHitsAndLog, Particle.cpp:1294-1312): up to `capacity` records of MFG_LOG_N doubles
+ * (u, v, theta, phi to the facet basis, oriRatio, expected decay moment, time, speed), in no
+ * particular order; *n_records receives the number copied. */
+#define MFG_LOG_N 8
+int mfg_fetch_log(mfg_sim* sim, double* records, int64_t capacity, int64_t* n_records);
 
 /* Autotuner: times short trial runs (n_trial desorptions each) over block sizes and register
  * budgets for the given precision, keeps the fastest launch shape as this handle's default

@@ -107,16 +107,27 @@ public:
         return MCStepResult::Success;
     }
 
-    // UpdateHitsAndLog: add the tallies into the global state under its timed lock, then clear them.
-    bool UpdateHitsAndLog(HostState& global, size_t timeout_ms) {
+    // UpdateHitsAndLog: add the tallies into the global state under its timed lock, append the
+    // particle log records (MFG_LOG_N doubles each) to `log` up to `log_limit` records, then clear.
+    bool UpdateHitsAndLog(HostState& global, size_t timeout_ms, std::vector<double>* log = nullptr,
+                          size_t log_limit = 0) {
         HostState local;
         local.resize(layout_);
         mfg_state_view v = local.view();
         check(mfg_fetch(sim_, &v));
+        std::vector<double> recs;
+        if (log && log_limit * MFG_LOG_N > log->size()) {
+            const int64_t room = int64_t(log_limit - log->size() / MFG_LOG_N);
+            recs.resize(size_t(room) * MFG_LOG_N);
+            int64_t n = 0;
+            check(mfg_fetch_log(sim_, recs.data(), room, &n));
+            recs.resize(size_t(n) * MFG_LOG_N);
+        }
         std::unique_lock<std::timed_mutex> lk(global.mutex, std::defer_lock);
         if (!lk.try_lock_for(std::chrono::milliseconds(timeout_ms))) return false;   // GetHitLock timeout
         if (global.global.empty()) global.resize(layout_);
         global += local;
+        if (log) log->insert(log->end(), recs.begin(), recs.end());
         lk.unlock();
         check(mfg_reset(sim_));
         return true;

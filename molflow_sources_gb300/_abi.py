@@ -2,6 +2,7 @@
 import ctypes as C
 
 MFG_ABI_VERSION = 4
+LOG_N = 8   # particle log record: u, v, theta, phi, oriRatio, decay moment, time, speed
 
 MFG_OK = 0
 MFG_ERR_INVALID_MODEL = 1
@@ -134,6 +135,8 @@ MODEL_DESC_FIELDS = [
     ("enable_force_measurement", C.c_int32),
     ("torque_ref_point", C.c_double * 3),
     ("bvh_facet_weight", _d),
+    ("log_facet", C.c_int32),
+    ("log_limit", C.c_int64),
 ]
 
 

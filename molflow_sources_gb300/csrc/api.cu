@@ -253,6 +253,8 @@ static int sim_upload(mfg_sim* s) {
     M.scatter = h.scatter;
     for (int k = 0; k < 3; ++k) { M.mv1[k] = h.mv1[k]; M.mv2[k] = h.mv2[k]; }
     M.force = h.force;
+    M.log_facet = h.log_facet;
+    M.log_cap = (unsigned long long)h.log_cap;
     for (int k = 0; k < 3; ++k) M.torque_ref[k] = h.torque_ref[k];
     M.scatter_cutoff = h.scatter_cutoff;
     M.pad5 = 0;
@@ -305,6 +307,10 @@ static int sim_upload(mfg_sim* s) {
     if ((rc = alloc(reinterpret_cast<unsigned long long**>(&s->dt.histogram), s->n_hist))) return rc;
     s->n_force = size_t(h.layout.n_force);
     if ((rc = alloc(reinterpret_cast<unsigned long long**>(&s->dt.force), s->n_force))) return rc;
+    if (h.log_cap > 0) {
+        if ((rc = alloc(reinterpret_cast<unsigned long long**>(&s->dt.plog), size_t(h.log_cap) * MFG_LOG_N))) return rc;
+        if ((rc = alloc(&s->dt.plog_n, 1))) return rc;
+    }
     if (h.low_flux) {
         const size_t nfc = B * size_t(h.nf) * 2, ntx = B * size_t(h.layout.texture_cells),
                      npr = B * size_t(h.layout.profile_facets) * MFG_PROFILE_SIZE;
@@ -336,6 +342,7 @@ int mfg_reset(mfg_sim* s) {
     }
     if (s->n_hist) CK(cudaMemsetAsync(s->dt.histogram, 0, s->n_hist * 8, s->stream));
     if (s->n_force) CK(cudaMemsetAsync(s->dt.force, 0, s->n_force * 8, s->stream));
+    if (s->dt.plog_n) CK(cudaMemsetAsync(s->dt.plog_n, 0, 8, s->stream));
     if (s->n_lf) CK(cudaMemsetAsync(s->dt.lf_glob, 0, s->n_lf * 8, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return MFG_OK;
@@ -819,6 +826,21 @@ int mfg_fetch(mfg_sim* s, mfg_state_view* v) {
     if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
     const mfg::HostModel& h = s->model->h;
     return fetch_range(s, v, 0, h.nf, 0, h.layout.texture_cells, 0, h.layout.profile_facets, 0, h.layout.anglemap_cells, true);
+}
+
+int mfg_fetch_log(mfg_sim* s, double* records, int64_t capacity, int64_t* n_records) {
+    if (!s || capacity < 0 || (capacity > 0 && !records)) return fail(MFG_ERR_INVALID_ARGUMENT, "bad argument");
+    if (n_records) *n_records = 0;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
+    if (!s->dt.plog_n) return MFG_OK;
+    CK(cudaSetDevice(s->device));
+    unsigned long long claimed = 0;
+    CK(cudaMemcpy(&claimed, s->dt.plog_n, 8, cudaMemcpyDeviceToHost));
+    const int64_t n = std::min<int64_t>({int64_t(claimed), int64_t(s->model->h.log_cap), capacity});
+    if (n > 0) CK(cudaMemcpy(records, s->dt.plog, size_t(n) * MFG_LOG_N * 8, cudaMemcpyDeviceToHost));
+    if (n_records) *n_records = n;
+    return MFG_OK;
 }
 
 int mfg_fetch_instance(mfg_sim* s, int32_t i, mfg_state_view* v) {

@@ -234,7 +234,8 @@ struct DevModel {
     // angular velocity vector
     int32_t motion_type, scatter;   // scatter: background-gas collisions on
     double mv1[3], mv2[3];
-    int32_t force, pad_force;       // force measurement on (sp.enableForceMeasurement)
+    int32_t force, log_facet;       // force measurement on; particle logger facet (-1 none)
+    unsigned long long log_cap;     // particle logger capacity (records)
     double torque_ref[3];           // sp.torqueRefPoint (cm)
     int32_t scatter_cutoff, pad5;
     double sc_mass_ratio, sc_mfp, sc_rho, sc_cutoff_speed;
@@ -256,6 +257,8 @@ struct DevModel {
 struct DevTally {
     double* histogram;               // (1+M) * hist_bins (FP64 atomics)
     double* force;                   // (1+M) * nf * 9: impulse, its squares, torque (FP64 atomics), or null
+    double* plog;                    // particle log: log_cap records of 8 doubles, or null
+    unsigned long long* plog_n;      // records claimed (may exceed log_cap; only log_cap are written)
     // low-flux mode: weighted ("equivalent") counts, FP64 atomics; null otherwise
     double* lf_glob;                 // [2] nbHitEquiv, nbAbsEquiv
     double* lf_facet;                // (1+M) * nf * 2 (nbHitEquiv, nbAbsEquiv)

@@ -430,6 +430,8 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     m.sc_mfp = d->scatter_mean_free_path_cm;
     m.sc_rho = d->scatter_rho;
     m.sc_cutoff_speed = d->scatter_cutoff_speed;
+    m.log_facet = (d->log_facet >= 0 && d->log_facet < nf && d->log_limit > 0) ? d->log_facet : -1;
+    m.log_cap = m.log_facet >= 0 ? d->log_limit : 0;
     m.force = d->enable_force_measurement != 0;
     for (int k = 0; k < 3; ++k) m.torque_ref[k] = d->torque_ref_point[k];
     if (m.motion_type < 0 || m.motion_type > 2) { err = "motion type must be 0, 1 or 2"; return MFG_ERR_INVALID_MODEL; }
@@ -1045,7 +1047,7 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     m.instances.assign(1, inst);
     bool any_moving = false;
     for (int i = 0; i < nf; ++i) any_moving = any_moving || m.moving[i];
-    m.has_ext = m.has_transparent || m.layout.histogram_bins > 0 || m.low_flux || m.scatter || any_moving || !m.am_dev.empty() || m.force ||
+    m.has_ext = m.has_transparent || m.layout.histogram_bins > 0 || m.low_flux || m.scatter || any_moving || !m.am_dev.empty() || m.force || m.log_facet >= 0 ||
                 std::any_of(m.teleport.begin(), m.teleport.end(), [](int32_t t) { return t != 0; });
     return MFG_OK;
 }
@@ -1065,9 +1067,9 @@ int merge_host_models(const std::vector<const HostModel*>& parts, HostModel& out
     for (const HostModel* p : parts) {
         if (p->layout.histogram_bins > 0) { err = "histograms are not recorded in batched instances"; return MFG_ERR_UNSUPPORTED_FEATURE; }
         if (p->low_flux) { err = "low-flux mode is not traced in batched instances"; return MFG_ERR_UNSUPPORTED_FEATURE; }
-        if (p->scatter || p->motion_type || !p->am_dev.empty() || !p->og.empty() || p->force ||
+        if (p->scatter || p->motion_type || !p->am_dev.empty() || !p->og.empty() || p->force || p->log_facet >= 0 ||
             std::any_of(p->teleport.begin(), p->teleport.end(), [](int32_t t) { return t != 0; })) {
-            err = "scattering, moving facets, angle-map desorption, outgassing maps, teleports and force measurement are not traced in batched instances";
+            err = "scattering, moving facets, angle-map desorption, outgassing maps, teleports, force measurement and the particle logger are not traced in batched instances";
             return MFG_ERR_UNSUPPORTED_FEATURE;
         }
     }

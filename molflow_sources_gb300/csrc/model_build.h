@@ -41,6 +41,8 @@ struct HostModel {
     int motion_type = 0, scatter = 0, scatter_cutoff = 0;
     double mv1[3] = {0, 0, 0}, mv2[3] = {0, 0, 0};
     double sc_mass_ratio = 1, sc_mfp = 1e30, sc_rho = 0, sc_cutoff_speed = 0;
+    int log_facet = -1;                   // particle logger facet (-1 none) and capacity
+    int64_t log_cap = 0;
     int force = 0;                        // force measurement
     double torque_ref[3] = {0, 0, 0};
     // derived

@@ -394,6 +394,24 @@ __device__ __forceinline__ int texture_cell(const DevModel& M, int f, R u, R v) 
 
 // RecordDirectionVector (Particle.cpp:1006-1023): Sum of v*direction and a count per cell,
 // constant flow and every moment window holding t
+// Particle logger (LogHit, Particle.cpp:1088-1102): an event on the logged facet takes the next
+// record (u, v, theta and phi of the direction to the facet basis, oriRatio, expected decay
+// moment, time, speed) while records are left
+__device__ __noinline__ void log_hit(const DevModel& M, const DevTally& T, int f, double u, double v, double dx,
+                                     double dy, double dz, double w, double decay_at, double time, double vel) {
+    if (f != M.log_facet) return;
+    const unsigned long long k = atomicAdd(T.plog_n, 1ull);
+    if (k >= M.log_cap) return;
+    const FacetPhysD& Ph = M.phys_d[f];
+    const double* N = M.isect_d[f].v;
+    const double cu = dx * Ph.nU[0] + dy * Ph.nU[1] + dz * Ph.nU[2];
+    const double cv = dx * Ph.nV[0] + dy * Ph.nV[1] + dz * Ph.nV[2];
+    const double cn = fmin(1.0, fmax(-1.0, dx * N[0] + dy * N[1] + dz * N[2]));
+    double* r = T.plog + k * MFG_LOG_N;
+    r[0] = u; r[1] = v; r[2] = acos(cn); r[3] = atan2(cv, cu);
+    r[4] = w; r[5] = decay_at; r[6] = time; r[7] = vel;
+}
+
 // Force measurement (IncreaseFacetCounter, Particle.cpp:1208-1212): the momentum sgn*v*d of the
 // particle onto facet f (sgn = -1 for a particle leaving it), its componentwise squares and its
 // torque about the reference point, weighted by w (oriRatio), in moment 0 and every moment
@@ -895,6 +913,9 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                 if (M.force)   // desorbed particle onto its source, or reflected particle leaving the facet
                     force_add(M, T, fo, P.time, P.ori, des ? 1.0 : -1.0, (double)vel, (double)dx, (double)dy, (double)dz,
                               P.ox, P.oy, P.oz);
+                if (des && M.log_facet >= 0)
+                    log_hit(M, T, fo, (double)pu, (double)pv, (double)dx, (double)dy, (double)dz, P.ori, P.decay_at, P.time,
+                            (double)vel);
             }
             {
                 // outgoing tallies; a reflection's incoming half (pending) is added with them (moment 0)
@@ -1173,6 +1194,8 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                 if (dest >= 0 && dest < M.nf) {
                     // recorded like a transparent pass with the incoming direction, one hit and no sums
                     transparent_pass<kFP32>(M, T, B, hf, (R)0, hu, hv, P.time, vel, dx, dy, dz, true);
+                    if (M.log_facet >= 0)
+                        log_hit(M, T, hf, (double)hu, (double)hv, ddx, ddy, ddz, P.ori, P.decay_at, P.time, (double)vel);
                     teleport_to<kFP32>(M, T, B, hf, dest, rng, P.time, vel, (double)hu, (double)hv, P.ox, P.oy, P.oz, dx,
                                        dy, dz);
                     P.structure = M.info2[dest].structure;
@@ -1245,6 +1268,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
             quant(wa, q1, q2, q3);
             if constexpr (kExt) {
                 if (M.force) force_add(M, T, hf, P.time, wa, 1.0, (double)vel, ddx, ddy, ddz, P.ox, P.oy, P.oz);
+                if (M.log_facet >= 0) log_hit(M, T, hf, (double)hu, (double)hv, ddx, ddy, ddz, wa, P.decay_at, P.time, (double)vel);
             }
             ++c_abs;
             const int cell = (In.tex_off >= 0 && (In.count & MFG_COUNT_ABS)) ? texture_cell<kFP32>(M, hf, hu, hv) : -1;
@@ -1281,6 +1305,11 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
             transparent_pass<kFP32>(M, T, B, hf, (R)0, hu, hv, P.time, vel, dx, dy, dz, true, wr);
             P.structure = M.info2[hf].link;
             if (In.flags & FF_MOVING) treat_moving(M, P.ox, P.oy, P.oz, dx, dy, dz, vel);
+            if constexpr (kExt) {
+                if (M.log_facet >= 0)
+                    log_hit(M, T, hf, (double)hu, (double)hv, (double)dx, (double)dy, (double)dz, wr, P.decay_at, P.time,
+                            (double)vel);
+            }
             relink = true;
             need_new = false;
             if (++P.bounces > max_steps) {   // step cap
@@ -1295,6 +1324,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
             quant(wr, q1, q2, q3);
             if constexpr (kExt) {
                 if (M.force) force_add(M, T, hf, P.time, wr, 1.0, (double)vel, ddx, ddy, ddz, P.ox, P.oy, P.oz);
+                if (M.log_facet >= 0) log_hit(M, T, hf, (double)hu, (double)hv, ddx, ddy, ddz, wr, P.decay_at, P.time, (double)vel);
             }
             const int cell = (In.tex_off >= 0 && (In.count & MFG_COUNT_REFL)) ? texture_cell<kFP32>(M, hf, hu, hv) : -1;
             if (In.flags & FF_ANGLEMAP) anglemap_add(M, T, hf, ddx, ddy, ddz);

@@ -110,6 +110,9 @@ class Model:
         self.torque_ref_point = (0.0, 0.0, 0.0)
         # BVH split weights per facet (ProbSplit), None: surface-area heuristic
         self.bvh_facet_weight = None
+        # particle logger: facet (-1 none) and record limit (otfParams.logFacetId, logLimit)
+        self.log_facet = -1
+        self.log_limit = 0
         # sp.globalHistogramParams
         self.global_histogram = dict(record=0, bounce_binsize=1, bounce_max=0, distance_binsize=1.0,
                                      distance_max=0.0, time_binsize=1.0, time_max=0.0)
@@ -198,6 +201,8 @@ class Model:
             d.desorb_anglemap = p(np.concatenate(parts), C.c_uint64)
         if self.bvh_facet_weight is not None:
             d.bvh_facet_weight = p(np.asarray(self.bvh_facet_weight, np.float64).reshape(self.n_facets), C.c_double)
+        d.log_facet = int(self.log_facet)
+        d.log_limit = int(self.log_limit)
         d.enable_force_measurement = int(self.enable_force_measurement)
         d.torque_ref_point = (C.c_double * 3)(*map(float, self.torque_ref_point))
         if self.outgassing_maps:

@@ -75,6 +75,7 @@ def load_library(build_if_missing=True):
         L.mfg_wait.argtypes = [vp, C.c_int64, C.POINTER(A.RunStats)]
         L.mfg_abort.argtypes = [vp]
         L.mfg_fetch.argtypes = [vp, C.POINTER(A.StateView)]
+        L.mfg_fetch_log.argtypes = [vp, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_int64)]
         L.mfg_model_merge.argtypes = [C.POINTER(vp), C.c_int32, C.POINTER(vp)]
         L.mfg_model_instances.argtypes = [vp]
         L.mfg_model_instances.restype = C.c_int32
@@ -248,6 +249,15 @@ class GpuSimulation:
         v = st.view()
         _check(load_library().mfg_fetch(self.h, C.byref(v)))
         return st
+
+    def fetch_log(self, capacity=None):
+        """Particle log since the last reset as an (n, 8) array (u, v, theta, phi, oriRatio, decay
+        moment, time, speed), in no particular order."""
+        cap = int(capacity if capacity is not None else max(int(self.model.log_limit), 0))
+        out = np.zeros((max(cap, 1), A.LOG_N))
+        n = C.c_int64()
+        _check(load_library().mfg_fetch_log(self.h, A.ptr(out, C.c_double), cap, C.byref(n)))
+        return out[:n.value]
 
     def UpdateHitsAndLog(self, global_state: SimuState, lock: threading.Lock = None, timeout_ms=10000):
         """Add this simulation's tallies into global_state and clear them (Particle.cpp:21-73,1294-1312)."""

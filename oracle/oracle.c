@@ -444,6 +444,7 @@ struct orc_model {
     int motion_type; double mv1[3], mv2[3];                 /* moving facets */
     int scatter, scatter_cutoff;                            /* background-gas scattering */
     int force; double torque_ref[3];                        /* force measurement */
+    int log_facet; int64_t log_cap;                         /* particle logger */
     double sc_mass_ratio, sc_mfp, sc_rho, sc_cutoff_speed;
     ohist ghist;           /* global histograms; offset 0 of each moment block */
     ohist* fhist;          /* per facet, NULL when no facet records */
@@ -767,6 +768,8 @@ int orc_model_create(const mfg_model_desc* d, orc_model** out, char* err, size_t
     for (int k = 0; k < 3; ++k) { M->mv1[k] = d->motion_vector1[k]; M->mv2[k] = d->motion_vector2[k]; }
     M->scatter = d->scatter_enabled; M->scatter_cutoff = d->scatter_cutoff_enabled;
     M->force = d->enable_force_measurement != 0;
+    M->log_facet = (d->log_facet >= 0 && d->log_facet < d->n_facets && d->log_limit > 0) ? d->log_facet : -1;
+    M->log_cap = M->log_facet >= 0 ? d->log_limit : 0;
     for (int k = 0; k < 3; ++k) M->torque_ref[k] = d->torque_ref_point[k];
     M->sc_mass_ratio = d->scatter_mass_ratio; M->sc_mfp = d->scatter_mean_free_path_cm;
     M->sc_rho = d->scatter_rho; M->sc_cutoff_speed = d->scatter_cutoff_speed;
@@ -1147,6 +1150,8 @@ typedef struct {
     uint64_t* ang;
     double* hist;
     double* force;   /* [(1+M) * nf * 9] with force measurement */
+    double* plog;    /* particle log records (MFG_LOG_N doubles each) */
+    int64_t plog_n;
 } otally;
 
 typedef struct {
@@ -1203,6 +1208,19 @@ static void facet_counter(const orc_model* M, otally* T, const int* ms, int nms,
                           double absn, double s1v, double svort, const opart* P) {
     add_moment_block(M, T, 0, fi, hit, des, absn, s1v, svort, P);
     for (int k = 0; k < nms; ++k) add_moment_block(M, T, ms[k], fi, hit, des, absn, s1v, svort, P);
+}
+/* LogHit (Particle.cpp:1088-1102): an event on the logged facet adds a record (u, v, theta and phi
+ * of the direction to the facet basis, oriRatio, expected decay moment, time, speed) while the
+ * thread's log has room */
+static void log_hit(const orc_model* M, otally* T, int fi, const opart* P) {
+    if (fi != M->log_facet || T->plog_n >= M->log_cap) return;
+    const ofacet* F = &M->f[fi];
+    double th, ph;
+    cart_to_polar(F, P->d, &th, &ph);
+    double* r = T->plog + (size_t)T->plog_n * MFG_LOG_N;
+    r[0] = P->u; r[1] = P->v; r[2] = th; r[3] = ph;
+    r[4] = P->ori; r[5] = P->decay_at; r[6] = P->time; r[7] = P->velocity;
+    T->plog_n++;
 }
 /* force measurement (IncreaseFacetCounter, Particle.cpp:1208-1212): momentum s*v*d of the particle
  * onto facet fi (s = -1 for a particle leaving it), its squares and its torque about the
@@ -1403,6 +1421,7 @@ static int start_from_source(const orc_model* M, otally* T, rng_t* r, opart* P) 
     int ms[256]; int nms = moments_of(M, P->time, ms, 256);
     facet_counter(M, T, ms, nms, fi, 0, 1, 0, 2.0 / ort, (M->use_maxwell ? 1.0 : 1.1781) * ort, P);
     force_add(M, T, ms, nms, fi, P, 1.0);
+    log_hit(M, T, fi, P);
     profile_hit(M, T, ms, nms, F, P, 0, 2.0, 1.0);
     if (F->count & MFG_COUNT_DES) texture_hit(M, T, ms, nms, F, P, 1, 2.0, 1.0);
     return 1;
@@ -1465,6 +1484,7 @@ static void record_absorb(const orc_model* M, otally* T, int fi, opart* P) {
     double ort = P->velocity * fabs(dot3(P->d, F->N));
     facet_counter(M, T, ms, nms, fi, 1, 0, 1, 2.0 / ort, (M->use_maxwell ? 1.0 : 1.1781) * ort, P);
     force_add(M, T, ms, nms, fi, P, 1.0);
+    log_hit(M, T, fi, P);
     profile_hit(M, T, ms, nms, F, P, 1, 2.0, 1.0);
     if (F->ang_off >= 0) anglemap_hit(M, T, F, P);
     record_histograms(M, T, ms, nms, fi, P);
@@ -1509,6 +1529,7 @@ static void perform_teleport(const orc_model* M, otally* T, int fi, rng_t* r, op
     if ((F->count & MFG_COUNT_DIR) && F->dir_off >= 0) direction_hit(M, T, ms, nms, F, P);
     profile_hit(M, T, ms, nms, F, P, 1, 2.0, 2.0);
     if (F->ang_off >= 0) anglemap_hit(M, T, F, P);
+    log_hit(M, T, fi, P);
     const double a = dot3(P->d, F->nU), b = dot3(P->d, F->nV), c = dot3(P->d, F->N);
     for (int k = 0; k < 3; ++k) P->d[k] = a * D->nU[k] + b * D->nV[k] + c * D->N[k];
     double u = P->u, v = P->v;
@@ -1540,6 +1561,7 @@ static void perform_bounce(const orc_model* M, otally* T, int fi, rng_t* r, opar
         if ((F->count & MFG_COUNT_DIR) && F->dir_off >= 0) direction_hit(M, T, ms, nms, F, P);
         P->structure = F->link - 1;
         if (F->moving) treat_moving(M, P);
+        log_hit(M, T, fi, P);
         return;
     }
     int revert = F->two_sided ? (dot3(P->d, F->N) > 0.0) : 0;
@@ -1548,6 +1570,7 @@ static void perform_bounce(const orc_model* M, otally* T, int fi, rng_t* r, opar
     int ms[256]; int nms = moments_of(M, P->time, ms, 256);
     facet_counter(M, T, ms, nms, fi, 1, 0, 0, 1.0 / ort, vf * ort, P);
     force_add(M, T, ms, nms, fi, P, 1.0);
+    log_hit(M, T, fi, P);
     P->bounces++;
     if (F->count & MFG_COUNT_REFL) texture_hit(M, T, ms, nms, F, P, 1, 1.0, 1.0);
     if ((F->count & MFG_COUNT_DIR) && F->dir_off >= 0) direction_hit(M, T, ms, nms, F, P);
@@ -1597,10 +1620,12 @@ static void tally_alloc(const orc_model* M, otally* T) {
     T->ang = (uint64_t*)calloc(L->n_anglemap + 1, sizeof(uint64_t));
     T->hist = (double*)calloc(L->n_histogram + 1, sizeof(double));
     T->force = (double*)calloc(L->n_force + 1, sizeof(double));
+    T->plog = (double*)calloc((size_t)M->log_cap * MFG_LOG_N + 1, sizeof(double));
+    T->plog_n = 0;
 }
 static void tally_free(otally* T) {
     free(T->global); free(T->fc); free(T->fs); free(T->tex); free(T->prof); free(T->dir); free(T->ang); free(T->hist);
-    free(T->force);
+    free(T->force); free(T->plog);
 }
 
 /* trace one particle to absorption/leak: the body of SimulationMCStep (Particle.cpp:221-393) */
@@ -1713,6 +1738,12 @@ static double now_s(void) {
 }
 
 int orc_run(orc_model* M, uint64_t n_des, const orc_run_opts* o, mfg_state_view* view, orc_stats* st) {
+    return orc_run_logged(M, n_des, o, view, st, NULL, 0, NULL);
+}
+
+int orc_run_logged(orc_model* M, uint64_t n_des, const orc_run_opts* o, mfg_state_view* view, orc_stats* st,
+                   double* log, int64_t log_capacity, int64_t* log_n) {
+    if (log_n) *log_n = 0;
     if (M->nsrc == 0) return MFG_ERR_NO_SOURCE;
     int nt = o->n_threads;
 #ifdef _OPENMP
@@ -1758,6 +1789,12 @@ int orc_run(orc_model* M, uint64_t n_des, const orc_run_opts* o, mfg_state_view*
         if (view->anglemap) for (int64_t k = 0; k < L->n_anglemap; ++k) view->anglemap[k] += T->ang[k];
         if (view->histogram) for (int64_t k = 0; k < L->n_histogram; ++k) view->histogram[k] += T->hist[k];
         if (view->force) for (int64_t k = 0; k < L->n_force; ++k) view->force[k] += T->force[k];
+        if (log && log_n) {   /* the threads' logs one after the other, up to the capacity */
+            int64_t take = T->plog_n;
+            if (take > log_capacity - *log_n) take = log_capacity - *log_n;
+            if (take > 0) memcpy(log + (size_t)(*log_n) * MFG_LOG_N, T->plog, (size_t)take * MFG_LOG_N * sizeof(double));
+            if (take > 0) *log_n += take;
+        }
         st->desorbed += th[t].st.desorbed; st->hits += th[t].st.hits; st->leaks += th[t].st.leaks;
         st->dropped += th[t].st.dropped; st->rays += th[t].st.rays;
         st->node_visits += th[t].st.node_visits; st->prim_tests += th[t].st.prim_tests;

@@ -61,6 +61,10 @@ int  orc_layout(const orc_model* m, mfg_state_layout* out);
 int  orc_facet_geometry(const orc_model* m, double* out18, double* area);
 /* Simulate n_des particles and ADD the tallies into view (like UpdateMCHits). */
 int  orc_run(orc_model* m, uint64_t n_des, const orc_run_opts* o, mfg_state_view* view, orc_stats* st);
+/* orc_run that also returns the particle log (LogHit records, MFG_LOG_N doubles each) of all
+ * threads, up to log_capacity records; *log_n receives the number returned. */
+int  orc_run_logged(orc_model* m, uint64_t n_des, const orc_run_opts* o, mfg_state_view* view, orc_stats* st,
+                    double* log, int64_t log_capacity, int64_t* log_n);
 /* Intersect given rays (replay mode). */
 int  orc_replay(orc_model* m, int64_t n, const double* origin, const double* dir, const int32_t* last,
                 int32_t* hit_facet, double* hit_t, orc_stats* st);

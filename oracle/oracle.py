@@ -59,6 +59,8 @@ def lib():
         L.orc_layout.argtypes = [C.c_void_p, C.POINTER(A.StateLayout)]
         L.orc_facet_geometry.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.orc_run.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(OrcRunOpts), C.POINTER(A.StateView), C.POINTER(OrcStats)]
+        L.orc_run_logged.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(OrcRunOpts), C.POINTER(A.StateView),
+                                     C.POINTER(OrcStats), C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_int64)]
         L.orc_replay.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                  C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(OrcStats)]
         L.orc_record_rays.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int64, C.POINTER(C.c_double),
@@ -118,6 +120,20 @@ class Oracle:
         if rc != 0:
             raise OracleError(A.STATUS_NAMES.get(rc, rc))
         return st, {f: getattr(s, f) for f, _ in OrcStats._fields_}
+
+    def run_logged(self, n_des, seed=0x4D6F6C66, first_particle=0, threads=0, capacity=1_000_000):
+        """run() that also returns the particle log as an (n, 8) array."""
+        st = SimuState(self.model)
+        o = OrcRunOpts(seed=seed, first_particle=first_particle, n_threads=threads, rng_mode=ORC_RNG_PHILOX)
+        s = OrcStats()
+        v = st.view()
+        log = np.zeros((capacity, A.LOG_N))
+        n = C.c_int64()
+        rc = lib().orc_run_logged(self.h, n_des, C.byref(o), C.byref(v), C.byref(s), A.ptr(log, C.c_double),
+                                  capacity, C.byref(n))
+        if rc != 0:
+            raise OracleError(A.STATUS_NAMES.get(rc, rc))
+        return st, log[:n.value]
 
     def replay(self, origin, direction, last):
         n = len(last)
