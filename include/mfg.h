@@ -36,7 +36,7 @@ extern "C" {
 #define MFG_ERR_TIMEOUT              3  /* wait or kernel time limit reached (GetHitLock timeout, MolflowSimGeom.cpp:1239-1248) */
 #define MFG_ERR_ABORTED              4  /* mfg_abort() was called while running */
 #define MFG_ERR_CUDA                 5  /* CUDA runtime error; text in mfg_last_error */
-#define MFG_ERR_UNSUPPORTED_FEATURE  6  /* model uses a feature this build does not trace */
+#define MFG_ERR_UNSUPPORTED_FEATURE  6  /* model uses a feature the library does not trace */
 #define MFG_ERR_INVALID_ARGUMENT     7
 #define MFG_ERR_BUSY                 8  /* a run is still in flight on this handle */
 #define MFG_ERR_NO_DEVICE            9
