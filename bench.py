@@ -25,12 +25,20 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
-    "c1": dict(name="config1_tube_L10cm_R1cm_64gon_tex64x64_maxwell_N2_293K", step=100_000_000, fp64_step=5_000_000),
-    "c2": dict(name="config2_beam_chamber_200k_triangles", step=10_000_000, fp64_step=500_000),
-    "c3": dict(name="config3_tube_1ms_pulse_100_logspaced_moments", step=20_000_000, fp64_step=2_000_000),
-    "c4": dict(name="config4_batch_256_instances_1k-50k_facets", step=1_000_000, fp64_step=0),
-    "c5": dict(name="config5_neg_tube_1000_sticking_parameters_8_gauges", step=20_000_000, fp64_step=0),
+    "c1": dict(name="config1_tube_L10cm_R1cm_64gon_tex64x64_maxwell_N2_293K", step=100_000_000),
+    "c2": dict(name="config2_beam_chamber_200k_triangles", step=10_000_000),
+    "c3": dict(name="config3_tube_1ms_pulse_100_logspaced_moments", step=20_000_000),
+    "c4": dict(name="config4_batch_256_instances_1k-50k_facets", step=1_000_000),
+    "c5": dict(name="config5_neg_tube_1000_sticking_parameters_8_gauges", step=20_000_000),
 }
+
+
+# The metric each workload reports; the CPU reference arm prints the same string for the same
+# workload, so that the two lines divide.
+HEADLINE = "hits/s per GB300: FP32+FP64-recheck vs plain FP64 kernel at same 3\u03c3 transmission"
+METRIC = {"c1": HEADLINE, "c2": HEADLINE, "c3": HEADLINE,
+          "c4": "hits/s per GB300, 256-instance batch in one persistent launch",
+          "c5": "hits/s per GB300 with sticking and outgassing gradients (score function)"}
 
 
 def make_model(workload):
@@ -39,7 +47,30 @@ def make_model(workload):
         return workloads.config1_tube()
     if workload == "c3":
         return workloads.config3_transient()
+    if workload == "c5":
+        from molflow_sources_gb300.sensitivity import config5_neg_tube
+        return config5_neg_tube()
     return workloads.config2_beam_chamber()
+
+
+def pumped_fraction(model, st):
+    """(absorbed on the sinks) / desorbed, the transmission of the workload: the outlet of the
+    tubes (facet 1), the four ports of the beam chamber."""
+    ports = np.where(np.asarray(getattr(model, "kind", [])) >= 3)[0] if hasattr(model, "kind") else np.array([1])
+    from molflow_sources_gb300 import _abi as A
+    return float(st.facet_counts[0, ports, A.FC_NBABSORBED].sum()) / max(st.n_desorbed, 1.0)
+
+
+def transmission_gate(model, st32, st64):
+    """FP32R against FP64 kernel: difference of the transmissions in units of the combined
+    binomial standard error (independent particles: the two runs use disjoint particle ids)."""
+    p32, n32 = pumped_fraction(model, st32), st32.n_desorbed
+    p64, n64 = pumped_fraction(model, st64), st64.n_desorbed
+    sig = ((p32 * (1 - p32) / n32) + (p64 * (1 - p64) / n64)) ** 0.5
+    z = (p32 - p64) / sig if sig > 0 else 0.0
+    return {"quantity": "absorbed on the sinks / desorbed", "fp32r": p32, "fp32r_desorbed": int(n32),
+            "fp64": p64, "fp64_desorbed": int(n64), "difference": p32 - p64, "sigma": sig, "z": z,
+            "pass": bool(abs(z) < 3.0)}
 
 
 class ClockSampler:
@@ -142,24 +173,33 @@ def cpu_baseline(model, target_s=12.0):
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
-    model = make_model(args.workload)
     t0 = time.time()
     steps = []
     hits_total = 0
     secs_total = 0.0
     from oracle.oracle import Oracle
-    orc = Oracle(model)
+    if args.workload == "c4":
+        # one oracle per instance; a step traces n particles in each, one instance after another
+        from molflow_sources_gb300 import batch_workloads as BW
+        orcs = [Oracle(m) for m in BW.config4_batch()]
+    else:
+        orcs = [Oracle(make_model(args.workload))]
     for _ in range(args.warmup):
-        orc.run(500, seed=3)
-    rate_des = calibrate(orc, 4)
-    n = int(max(500, min(rate_des * args.ref_step_s, 5e8)))
+        for orc in orcs:
+            orc.run(50, seed=3)
+    rate_des = calibrate(orcs[0], 4) if len(orcs) == 1 else 50.0 * len(orcs) / max(
+        sum(o.run(50, seed=4)[1]["seconds"] for o in orcs), 1e-6)
+    n = int(max(20, min(rate_des * args.ref_step_s / len(orcs), 5e8)))
+    s = {"threads": 0}
     for k in range(args.steps):
-        st, s = orc.run(n, seed=5, first_particle=k * n)
-        steps.append(s["seconds"])
-        hits_total += s["hits"]
-        secs_total += s["seconds"]
+        for i, orc in enumerate(orcs):
+            st, s = orc.run(n, seed=5, first_particle=k * n, instance=i if len(orcs) > 1 else 0)
+            steps.append(s["seconds"])
+            hits_total += s["hits"]
+            secs_total += s["seconds"]
+    n = n * len(orcs)
     v = hits_total / secs_total
-    line = {"metric": "hits/s per GB300 host (CPU reference arm)", "value": v, "unit": "hits/s", "n_gpus": world,
+    line = {"metric": METRIC[args.workload], "value": v, "unit": "hits/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs_total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
@@ -167,8 +207,9 @@ def run_reference(args, rank, world):
             "cpu_baseline": {"value": v, "unit": "hits/s", "cores": s["threads"], "kind": "port",
                              "sample": "%d desorptions per step x %d steps" % (n, args.steps)},
             "e2e": {"value": v, "unit": "hits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "the reference tracer cannot be built (src_shared submodule absent); the arm runs the FP64 CPU "
-                    "restatement of ParticleTracer in oracle/ on all host cores",
+            "note": "CPU reference arm: the reference tracer cannot be built (src_shared submodule absent), so the "
+                    "arm runs the FP64 CPU restatement of ParticleTracer in oracle/ on all host cores, on the same "
+                    "workload; each step is a bounded sample of desorptions (hits/s is a rate)",
             "wall_s": time.time() - t0}
     print(json.dumps(line), flush=True)
     return 0
@@ -185,40 +226,46 @@ def run_batch(args, torch, dist, rank, world, local, W, n_step):
     batch.set_particle_offset(rank * (1 << 48))
     load_s = time.time() - t0
     seed = 0x4D6F6C66
+    tuned = batch.autotune(max(n_step // 20, 1000), precision=A.PREC_FP32R, seed=seed)
     for _ in range(args.warmup):
-        batch.run(n_step // 10, precision=A.PREC_FP32R, seed=seed, use_graph=True)
+        batch.run(n_step // 10, precision=A.PREC_FP32R, seed=seed, use_graph=True, **tuned)
     batch.reset()
     sampler = ClockSampler(local)
     sampler.start()
     torch.cuda.synchronize()
     ms, hits, des, launches = 0.0, 0, 0, 0
     for k in range(args.steps):
-        st = batch.run(n_step, precision=A.PREC_FP32R, seed=seed, use_graph=True)
+        st = batch.run(n_step, precision=A.PREC_FP32R, seed=seed, use_graph=True, **tuned)
         ms += st["kernel_ms"]
         hits += st["hits"]
         des += st["desorbed"]
         launches += st["kernel_launches"]
     clocks = sampler.stop()
-    # separate launches: one simulation per instance, each stepped on its own
+    # separate launches: one simulation per instance, each stepped on its own with the same
+    # desorptions per instance as the batch step, through a captured graph as well (the first
+    # step of each captures it), at the launch shape the batch uses
     sims = [GpuSimulation(m, device=local) for m in models]
     sep_ms, sep_hits = 0.0, 0
     for s_ in sims:
-        s_.SimulationMCStep(max(n_step // 100, 1000), precision=A.PREC_FP32R, seed=seed)
+        s_.set_particle_offset(rank * (1 << 48))
+        s_.SimulationMCStep(max(n_step // 100, 1000), precision=A.PREC_FP32R, seed=seed, use_graph=True, **tuned)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     for s_ in sims:
-        s_.SimulationMCStep(n_step // 10, precision=A.PREC_FP32R, seed=seed)
+        s_.SimulationMCStep(n_step, precision=A.PREC_FP32R, seed=seed, use_graph=True, **tuned)
         sep_hits += s_.last_stats["hits"]
         sep_ms += s_.last_stats["kernel_ms"]
     sep_wall = time.perf_counter() - t1
     rate = hits / (ms / 1e3)
-    line = {"metric": "hits/s per GB300, 256-instance batch in one persistent launch", "value": rate, "unit": "hits/s",
+    line = {"metric": METRIC["c4"], "value": rate, "unit": "hits/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": W["name"], "instances": len(models), "facets_total": int(sum(m.n_facets for m in models)),
-                       "desorptions_per_instance_per_step": n_step, "launch": "CUDA graph, one persistent kernel"},
+                       "desorptions_per_instance_per_step": n_step, "launch": "CUDA graph, one persistent kernel",
+                       "launch_shape": tuned},
             "separate_launches": {"hits_per_s_device": sep_hits / (sep_ms / 1e3), "hits_per_s_wall": sep_hits / sep_wall,
-                                  "desorptions_per_instance": n_step // 10, "launches": len(models)},
+                                  "desorptions_per_instance": n_step, "launches": len(models),
+                                  "launch": "CUDA graph per instance"},
             "gpu_launches": launches, "model_load_s": load_s, "clocks": clocks,
             "e2e": {"value": rate, "unit": "hits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "cpu_baseline": None}
@@ -261,7 +308,7 @@ def run_sensitivity(args, torch, dist, rank, world, local, W, n_step):
     js, jq, src = sf.jacobian()
     e2e_s = time.perf_counter() - t1
     rate = s_hits / (s_ms / 1e3)
-    line = {"metric": "hits/s per GB300 with sticking and outgassing gradients (score function)", "value": rate,
+    line = {"metric": METRIC["c5"], "value": rate,
             "unit": "hits/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": s_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32+f64", "data": "synthetic",
@@ -285,7 +332,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=os.environ.get("MFG_BENCH_WORKLOAD", "c2"), choices=list(WORKLOADS))
     ap.add_argument("--step-desorptions", type=int, default=0)
-    ap.add_argument("--fp64-step", type=int, default=0)
+    ap.add_argument("--fp64-step", type=int, default=0, help="desorptions per FP64 step (default: the FP32R step)")
+    ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--ref-step-s", type=float, default=6.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--launch", default="",
@@ -327,16 +375,21 @@ def main():
         if dist is not None:
             dist.barrier()
 
-    # plain FP64 kernel on the same workload (smaller batch; hits/s is a rate)
-    fp64_step = args.fp64_step or W["fp64_step"]
-    sim.SimulationMCStep(max(1, fp64_step // 10), precision=A.PREC_FP64, seed=seed)
+    # plain FP64 kernel on the same workload and step size, at the launch shape its own autotuner
+    # picks (register budgets of 2, 3 and 4 resident blocks); its tallies are the FP64 side of the
+    # transmission gate
+    fp64_step = args.fp64_step or n_step
+    sim.SimulationMCStep(max(1, fp64_step // 20), precision=A.PREC_FP64, seed=seed)
+    tuned64 = sim.autotune(max(fp64_step // 10, 10000), precision=A.PREC_FP64, seed=seed)
     f64_ms = 0.0
     f64_hits = 0
-    for _ in range(2):
+    for _ in range(args.fp64_steps):
         sim.SimulationMCStep(fp64_step, precision=A.PREC_FP64, seed=seed)
         f64_ms += sim.last_stats["kernel_ms"]
         f64_hits += sim.last_stats["hits"]
     fp64_rate = f64_hits / (f64_ms / 1e3)
+    st64 = sim.fetch()
+    sim.ResetSimulation()
 
     if args.launch:
         b_, k_ = (int(x) for x in args.launch.split(","))
@@ -371,6 +424,7 @@ def main():
     if args.profile_steps:
         torch.cuda.profiler.stop()
     barrier()
+    gate = transmission_gate(model, sim.fetch(), st64)
     # end to end: public API call + tallies copied to host memory every step
     from molflow_sources_gb300.model import SimuState
     gstate = SimuState(model)
@@ -419,7 +473,7 @@ def main():
     d2h = 8 * (A.G_N + L["blocks"] * model.n_facets * (A.FC_N + A.FS_N) + L["blocks"] * L["texture_cells"] * 3 +
                L["blocks"] * L["profile_facets"] * 300 + L["anglemap_cells"])
     line = {
-        "metric": "hits/s per GB300: FP32+FP64-recheck vs plain FP64 kernel at same 3sigma transmission",
+        "metric": METRIC[args.workload],
         "value": rate, "unit": "hits/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64", "data": "synthetic",
@@ -427,6 +481,8 @@ def main():
                    "precision": "FP32 traversal + FP64 recheck", "l2": "256 MiB write between timed steps",
                    "parallelism": "particle ranges per rank" if world > 1 else "single GPU"},
         "fp64_kernel_hits_per_s": fp64_rate, "fp32r_over_fp64": rate / fp64_rate,
+        "fp64_launch_shape": tuned64, "fp64_desorptions_per_step": fp64_step,
+        "transmission_gate": gate,
         "desorptions_per_s": des / dev_s * (world if dist is None else 1),
         "recheck_fraction": rechecks / max(hits + des, 1),
         "e2e": {"value": e2e_rate, "unit": "hits/s", "h2d_bytes_per_step": int(A.RunOptions.__basicsize__ if hasattr(A.RunOptions, "__basicsize__") else 48),

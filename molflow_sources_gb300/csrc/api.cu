@@ -429,6 +429,8 @@ static const void* kernel_of(int variant) {
         case 102: return (const void*)mfgk::trace_kernel<true, 2, false, true>;
         case 112: return (const void*)mfgk::trace_kernel<false, 2, true, true>;
         case 113: return (const void*)mfgk::trace_kernel<true, 3, true, true>;
+        case 203: return (const void*)mfgk::trace_kernel<false, 3>;
+        case 204: return (const void*)mfgk::trace_kernel<false, 4>;
         default: return (const void*)mfgk::trace_kernel<false, 2>;
     }
 }
@@ -481,18 +483,22 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     }
     int block = o.block_size > 0 ? o.block_size : 256;
     if (block % 32 || block > 256) return fail(MFG_ERR_INVALID_ARGUMENT, "block_size must be a multiple of 32, at most 256");
-    // kernel variant: FP64, or FP32R compiled for at least 2, 3, 4, 6 or 8 resident blocks per SM
-    // (register budgets 128, 80, 64, 40, 32); blocks_per_sm selects the FP32R variant.  Models
-    // with transparent facets, histograms, low-flux mode, scattering, moving facets or angle-map
-    // desorption use the extended variants (+100).
+    // kernel variant: FP64 compiled for at least 2, 3 or 4 resident blocks per SM (register budgets
+    // 128, 80, 64), FP32R for 2, 3, 4, 6 or 8 (128, 80, 64, 40, 32); blocks_per_sm selects the
+    // variant.  Models with transparent facets, histograms, low-flux mode, scattering, moving
+    // facets, angle-map desorption, teleports, forces or the particle logger use the extended
+    // variants.
     int variant = 0;
+    const int b = int(o.blocks_per_sm);
     if (sens) {
         variant = o.precision == MFG_PREC_FP32R ? 13 : 12;
     } else if (o.precision == MFG_PREC_FP32R) {
-        const int b = int(o.blocks_per_sm);
         variant = (b == 3 || b == 4 || b == 6 || b == 8) ? b : (b == 5 ? 4 : (b == 7 ? 6 : (b > 8 ? 8 : 2)));
+    } else {
+        variant = b == 3 ? 203 : (b >= 4 ? 204 : 0);
     }
-    if (h.has_ext) variant = variant == 0 ? 100 : 102;
+    // extended variants: FP64 100, FP32R 102; with sensitivities FP64 112, FP32R 113
+    if (h.has_ext) variant = sens ? variant + 100 : (o.precision == MFG_PREC_FP64 ? 100 : 102);
     const void* fn = kernel_of(variant);
     CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn)));
     int per_sm = 0;
@@ -626,13 +632,13 @@ int mfg_wait(mfg_sim* s, int64_t timeout_ms, mfg_run_stats* stats) {
 int mfg_autotune(mfg_sim* s, uint64_t n_trial, int32_t precision, uint64_t seed, mfg_run_options* best) {
     if (!s || (precision != MFG_PREC_FP64 && precision != MFG_PREC_FP32R)) return fail(MFG_ERR_INVALID_ARGUMENT, "bad argument");
     const int blocks[] = {256};   // 128-thread blocks at the same register budget hold half the threads
-    const int bps64[] = {0};
+    const int bps64[] = {2, 3, 4};
     const int bps32[] = {2, 3, 4, 6, 8};
     double best_rate = -1;
     mfg_run_options bo{};
     for (int b : blocks) {
         const int* bl = precision == MFG_PREC_FP32R ? bps32 : bps64;
-        int nb = precision == MFG_PREC_FP32R ? int(sizeof(bps32) / sizeof(bps32[0])) : 1;
+        int nb = precision == MFG_PREC_FP32R ? int(sizeof(bps32) / sizeof(bps32[0])) : int(sizeof(bps64) / sizeof(bps64[0]));
         for (int k = 0; k < nb; ++k) {
             mfg_run_options o{};
             o.precision = precision;
@@ -907,12 +913,19 @@ int mfg_sens_setup(mfg_sim* s, int32_t n_params, const int32_t* param_facets, in
     if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
     const mfg::HostModel& h = s->model->h;
     if (h.instances.size() != 1) return fail(MFG_ERR_INVALID_ARGUMENT, "sensitivities are for single models");
+    // the score function needs a stick-or-reflect draw at every hit on a parameter facet: low-flux
+    // mode splits particles by weight instead of drawing
+    if (h.low_flux) return fail(MFG_ERR_UNSUPPORTED_FEATURE, "sensitivities need stick/reflect draws; low-flux mode has none");
     std::vector<int32_t> pof(h.nf, -1), gof(h.nf, -1), sof(h.nf, -1);
     std::vector<uint8_t> pump(h.nf, 0);
     for (int i = 0; i < n_params; ++i) {
         int f = param_facets[i];
         if (f < 0 || f >= h.nf || pof[f] >= 0) return fail(MFG_ERR_INVALID_ARGUMENT, "bad or repeated parameter facet");
         if (!(s->sticking[f] > 0.0 && s->sticking[f] < 1.0)) return fail(MFG_ERR_INVALID_ARGUMENT, "parameter sticking must be in (0,1)");
+        if (h.info[f].flags & FF_STICK_PARAM)
+            return fail(MFG_ERR_INVALID_ARGUMENT, "parameter facet has a time-dependent sticking");
+        if (h.info[f].flags & (FF_LINK | FF_TELEPORT))
+            return fail(MFG_ERR_INVALID_ARGUMENT, "parameter facet is a link or teleport (no stick/reflect draw)");
         pof[f] = i;
     }
     for (int i = 0; i < n_gauges; ++i) {

@@ -3,8 +3,10 @@
 The GB300 equivalent of the reference's MPI layer (input broadcast, per-rank run,
 state gather and sum to rank 0; src/MolflowCLI.cpp:76-101,165-196): every rank traces
 the particle ids [rank * stride, ...) with the same seed, and the GlobalSimuState-shaped
-tallies are added across ranks.  Counts are integers and the velocity sums are
-fixed-point derived, so the sum does not depend on the order of ranks.
+tallies are added across ranks.  The integer fields (hit, desorption and absorption counts,
+angle-map cells) are summed as 64-bit integers, so their sum does not depend on the order of
+the ranks.  The float64 fields (velocity sums, texture and profile sums, direction vectors) are
+summed as doubles: their sum can differ in the last bits with the reduction order.
 """
 import numpy as np
 

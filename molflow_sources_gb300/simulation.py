@@ -201,12 +201,12 @@ class GpuSimulation:
 
     # --- ParticleTracer surface (Particle.h:45,86) ---
     def SimulationMCStep(self, n_desorptions, precision=A.PREC_FP64, seed=0x4D6F6C66, block_size=0,
-                         blocks_per_sm=0, time_limit_s=0.0, max_steps=0):
+                         blocks_per_sm=0, time_limit_s=0.0, max_steps=0, use_graph=False):
         """Desorb and trace n_desorptions particles on the GPU (blocking)."""
         if not time_limit_s:
             time_limit_s = float(os.environ.get("MFG_TIME_LIMIT_S", "0"))
         o = A.RunOptions(precision=precision, seed=seed, block_size=block_size, blocks_per_sm=blocks_per_sm,
-                         time_limit_s=time_limit_s, max_steps_per_particle=max_steps)
+                         time_limit_s=time_limit_s, max_steps_per_particle=max_steps, use_graph=int(use_graph))
         st = A.RunStats()
         rc = load_library().mfg_run(self.h, int(n_desorptions), C.byref(o), C.byref(st))
         self.last_stats = {f: getattr(st, f) for f, _ in A.RunStats._fields_}
@@ -338,6 +338,12 @@ class GpuBatch:
         self.last_stats = {f: getattr(st, f) for f, _ in A.RunStats._fields_}
         _check(rc)
         return self.last_stats
+
+    def autotune(self, n_trial, precision=A.PREC_FP32R, seed=0x4D6F6C66):
+        """Fastest launch shape for the batch (n_trial particles per instance per trial); clears tallies."""
+        o = A.RunOptions()
+        _check(load_library().mfg_autotune(self.h, int(n_trial), precision, seed, C.byref(o)))
+        return {"block_size": o.block_size, "blocks_per_sm": o.blocks_per_sm}
 
     def fetch_instance(self, i):
         st = SimuState(self.models[i])

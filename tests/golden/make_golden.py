@@ -6,8 +6,9 @@ GlobalSimuState) with molflow_sources_gb300.xmlio and stores, per case, the
 model arrays and a subset of the stored results as a compressed .npz.
 
 Run in a checkout next to the reference sources (the reference's parameter catalog,
-copy_to_build/parameter_catalog, is read from the same tree):
-    python tests/golden/make_golden.py /root/reference/tests/TestCases [case ...]
+copy_to_build/parameter_catalog, is read from the same tree); the test-case folder is a
+required argument:
+    python tests/golden/make_golden.py <reference>/tests/TestCases [case ...]
 The .npz files are committed; tests never read the reference tree.
 """
 import json
@@ -89,7 +90,9 @@ def save_case(src_dir, name, keep, catalog):
 
 
 if __name__ == "__main__":
-    src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/tests/TestCases"
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py <reference tests/TestCases folder> [case ...]")
+    src = sys.argv[1]
     # the parameter catalog shipped next to the test cases (copy_to_build/parameter_catalog)
     catalog = xmlio.load_catalog(os.path.join(src, "..", "..", "copy_to_build", "parameter_catalog"))
     only = sys.argv[2:]

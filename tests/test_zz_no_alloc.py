@@ -42,10 +42,15 @@ def test_noalloc_replay_matches_allocating_replay(precision):
         out_f = torch.full((n,), -7, dtype=torch.int32, device="cuda")
         out_t = torch.full((n,), -7.0, dtype=torch.float64, device="cuda")
         nre = C.c_uint64(12345)
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         rc = fn(sim.h, precision, n, d_o.data_ptr(), d_d.data_ptr(), d_l.data_ptr(), out_f.data_ptr(),
                 out_t.data_ptr(), C.byref(nre))
         assert rc == A.MFG_OK
         torch.cuda.synchronize()
+        if call == 1:
+            # the first call looked up the array's address; the second allocates no device memory
+            assert torch.cuda.mem_get_info()[0] == free_before
         got_f = out_f.cpu().numpy()
         got_t = out_t.cpu().numpy()
         assert np.array_equal(got_f, ref_f), "call %d: %d facets differ" % (call, int((got_f != ref_f).sum()))
