@@ -337,7 +337,7 @@ def main():
     ap.add_argument("--ref-step-s", type=float, default=6.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--launch", default="",
-                    help="fixed FP32R launch shape BLOCK,BLOCKS_PER_SM instead of the autotuner's choice")
+                    help="fixed FP32R launch shape BLOCK,BLOCKS_PER_SM[,SMEM_BVH_LEVELS] instead of the autotuner's choice")
     ap.add_argument("--profile-steps", action="store_true",
                     help="bracket the timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     args = ap.parse_args()
@@ -392,8 +392,8 @@ def main():
     sim.ResetSimulation()
 
     if args.launch:
-        b_, k_ = (int(x) for x in args.launch.split(","))
-        tuned = {"block_size": b_, "blocks_per_sm": k_}
+        v_ = [int(x) for x in args.launch.split(",")]
+        tuned = {"block_size": v_[0], "blocks_per_sm": v_[1], "smem_bvh_levels": v_[2] if len(v_) > 2 else -1}
     else:
         # launch shape: trial runs of a quarter step, so that each of the up to 2048 resident
         # threads of an SM traces several particles and the tail of a launch does not decide

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define MFG_ABI_VERSION 4u
+#define MFG_ABI_VERSION 5u
 
 /* ---- status codes (replace the reference's exceptions / MCStepResult,
  *      src/Simulation/Particle.h:24-28, src/Simulation/MolflowSimGeom.cpp:219-247) ---- */
@@ -279,7 +279,9 @@ typedef struct mfg_run_options {
     uint64_t seed;               /* Philox key; replaces MersenneTwister seeding (MolflowSimulation.cpp:44-55) */
     int32_t  block_size;         /* threads per block, 0 = autotuned default */
     int32_t  blocks_per_sm;      /* 0 = occupancy maximum */
-    int32_t  reserved0;          /* set to 0 */
+    int32_t  smem_bvh_levels;    /* FP32R: the first 2^levels FP32 BVH nodes (breadth-first: the top levels) are
+                                    staged in shared memory per block, 1..12; 0 = the autotuned choice (none
+                                    before mfg_autotune); -1 = none */
     double   time_limit_s;       /* kernel self-stops after this wall time (status MFG_ERR_TIMEOUT), 0 = 600 s */
     uint64_t max_steps_per_particle; /* a particle that exceeds this many bounces is dropped and counted, 0 = 2^40 */
     int32_t  use_graph;          /* 1: launch through a captured CUDA graph (captured once per launch shape) */
@@ -320,6 +322,11 @@ int32_t mfg_model_instances(const mfg_model* model);
 int mfg_instance_layout(const mfg_model* model, int32_t i, mfg_state_layout* out);
 /* Derived per-facet geometry as computed by the library (O,U,V,N,nU,nV as 18 doubles per facet, area) for checks. */
 int mfg_model_facet_geometry(const mfg_model* model, double* out18, double* area);
+/* Outgassing totals of the model (CalcTotalOutgassing, MolflowSimGeom.cpp:290-335): molecules desorbed
+ * up to the latest moment (sp.totalDesorbedMolecules), the final outgassing rate in molecules/s
+ * (sp.finalOutgassingRate) and in Pa*m3/s (sp.finalOutgassingRate_Pa_m3_sec).  Any pointer may be NULL. */
+int mfg_model_outgassing(const mfg_model* model, double* total_desorbed_molecules, double* final_rate,
+                         double* final_rate_pa_m3_s);
 /* BVH statistics: node count, depth, leaf count. */
 int mfg_model_bvh_info(const mfg_model* model, int64_t* nodes, int64_t* depth, int64_t* leaves);
 

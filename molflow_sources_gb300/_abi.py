@@ -1,7 +1,7 @@
 """ctypes mirrors of the C structs declared in include/mfg.h."""
 import ctypes as C
 
-MFG_ABI_VERSION = 4
+MFG_ABI_VERSION = 5
 LOG_N = 8   # particle log record: u, v, theta, phi, oriRatio, decay moment, time, speed
 
 MFG_OK = 0
@@ -171,7 +171,7 @@ class RunOptions(C.Structure):
         ("seed", C.c_uint64),
         ("block_size", C.c_int32),
         ("blocks_per_sm", C.c_int32),
-        ("reserved0", C.c_int32),
+        ("smem_bvh_levels", C.c_int32),
         ("time_limit_s", C.c_double),
         ("max_steps_per_particle", C.c_uint64),
         ("use_graph", C.c_int32),

@@ -47,6 +47,7 @@ def build(force=False, verbose=False):
         objs.append(obj)
         cmd = [nvcc()] + ARCH + common + ["-c", os.path.join(CSRC, src), "-o", obj]
         if src.endswith(".cu"):
+            cmd += ["-split-compile=0"]   # the kernel variants are optimised on all host cores
             cmd += ["-Xptxas", "-v"] if verbose else []
         procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
     for cmd, p in procs:

@@ -79,7 +79,7 @@ struct mfg_sim {
     unsigned char* d_run = nullptr;
     size_t run_bytes = 0;
     cudaGraphExec_t graph_exec = nullptr;
-    long long graph_key = -1;
+    long long graph_key[5] = {-1, -1, -1, -1, -1};   // launch shape of the captured graph
     bool running = false;
     mfg_run_stats pending{};
     std::vector<unsigned long long> g_before;
@@ -88,6 +88,7 @@ struct mfg_sim {
     int launches = 0;
     int tuned_block[2] = {0, 0};     // per precision, from mfg_autotune
     int tuned_bps[2] = {0, 0};
+    int tuned_levels[2] = {0, 0};    // top BVH levels staged in shared memory (FP32R)
     std::vector<double> sticking;    // current sticking per facet (mfg_update_sticking)
     // sensitivity state (mfg_sens_*)
     bool sens_ready = false;
@@ -170,6 +171,15 @@ int mfg_model_facet_geometry(const mfg_model* model, double* out18, double* area
         }
         if (area) area[i] = F.area;
     }
+    return MFG_OK;
+}
+
+int mfg_model_outgassing(const mfg_model* model, double* total_desorbed_molecules, double* final_rate,
+                         double* final_rate_pa_m3_s) {
+    if (!model) return fail(MFG_ERR_INVALID_ARGUMENT, "null model");
+    if (total_desorbed_molecules) *total_desorbed_molecules = model->h.total_desorbed_molecules;
+    if (final_rate) *final_rate = model->h.final_outgassing_rate;
+    if (final_rate_pa_m3_s) *final_rate_pa_m3_s = model->h.final_outgassing_rate_pa;
     return MFG_OK;
 }
 
@@ -423,6 +433,8 @@ static const void* kernel_of(int variant) {
         case 4: return (const void*)mfgk::trace_kernel<true, 4>;
         case 6: return (const void*)mfgk::trace_kernel<true, 6>;
         case 8: return (const void*)mfgk::trace_kernel<true, 8>;
+        case 9: return (const void*)mfgk::trace_kernel<true, 4, false, false, 512>;
+        case 10: return (const void*)mfgk::trace_kernel<true, 2, false, false, 1024>;
         case 12: return (const void*)mfgk::trace_kernel<false, 2, true>;
         case 13: return (const void*)mfgk::trace_kernel<true, 3, true>;
         case 100: return (const void*)mfgk::trace_kernel<false, 2, false, true>;
@@ -474,15 +486,26 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     C.inst_first = C.inst_prefix + ni + 1;
     C.abort_flag = s->d_abort;
     if (sens) C.sens = s->sens;
-    size_t fac_bytes = size_t(h.nf) * SF_N * 8;
-    C.smem_facets = fac_bytes <= 32 * 1024 ? 1 : 0;   // leaves room for 4 blocks per SM
-    size_t dyn = (TG_N + (C.smem_facets ? size_t(h.nf) * SF_N : 0)) * 8;
     if (o.block_size == 0 && o.blocks_per_sm == 0 && s->tuned_block[o.precision]) {
         o.block_size = s->tuned_block[o.precision];
         o.blocks_per_sm = s->tuned_bps[o.precision];
     }
+    // staged BVH levels: 0 = the autotuned choice (none before mfg_autotune), -1 = none
+    if (o.smem_bvh_levels == 0) o.smem_bvh_levels = s->tuned_levels[o.precision];
     int block = o.block_size > 0 ? o.block_size : 256;
-    if (block % 32 || block > 256) return fail(MFG_ERR_INVALID_ARGUMENT, "block_size must be a multiple of 32, at most 256");
+    if (block % 32 || (block > 256 && block != 512 && block != 1024) || (block > 256 && (sens || h.has_ext)))
+        return fail(MFG_ERR_INVALID_ARGUMENT,
+                    "block_size must be a multiple of 32 up to 256, or 512 / 1024 (plain FP32R models)");
+    if (block > 256 && o.precision != MFG_PREC_FP32R)
+        return fail(MFG_ERR_INVALID_ARGUMENT, "512- and 1024-thread blocks are compiled for FP32R only");
+    if (o.smem_bvh_levels > 12) return fail(MFG_ERR_INVALID_ARGUMENT, "smem_bvh_levels is at most 12");
+    const int bps_req = block == 512 ? 4 : (block == 1024 ? 2 : std::max(1, int(o.blocks_per_sm)));
+    // moment-0 facet partials in shared memory when they fit the block's share of the SM (228 KB)
+    const size_t fac_bytes = size_t(h.nf) * SF_N * 8;
+    C.smem_facets = fac_bytes <= std::min<size_t>(96 * 1024, 200 * 1024 / size_t(bps_req)) ? 1 : 0;
+    C.n_top = o.precision == MFG_PREC_FP32R && o.smem_bvh_levels > 0
+                  ? int(std::min<size_t>(size_t(1) << o.smem_bvh_levels, h.nodes_c.size())) : 0;
+    size_t dyn = (TG_N + (C.smem_facets ? size_t(h.nf) * SF_N : 0)) * 8 + size_t(C.n_top) * sizeof(NodeC);
     // kernel variant: FP64 compiled for at least 2, 3 or 4 resident blocks per SM (register budgets
     // 128, 80, 64), FP32R for 2, 3, 4, 6 or 8 (128, 80, 64, 40, 32); blocks_per_sm selects the
     // variant.  Models with transparent facets, histograms, low-flux mode, scattering, moving
@@ -494,6 +517,8 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
         variant = o.precision == MFG_PREC_FP32R ? 13 : 12;
     } else if (o.precision == MFG_PREC_FP32R) {
         variant = (b == 3 || b == 4 || b == 6 || b == 8) ? b : (b == 5 ? 4 : (b == 7 ? 6 : (b > 8 ? 8 : 2)));
+        if (block == 512) variant = 9;     // 4 blocks of 512 threads, 32 registers
+        if (block == 1024) variant = 10;   // 2 blocks of 1024 threads, 32 registers
     } else {
         variant = b == 3 ? 203 : (b >= 4 ? 204 : 0);
     }
@@ -519,8 +544,8 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     s->t_start = std::chrono::steady_clock::now();
     if (o.use_graph && !sens) {
         // one captured graph per launch shape: [run descriptor copy, counter reset, tracer]
-        long long key = (long long)variant * 1000003LL + block * 1009LL + grid;
-        if (!s->graph_exec || s->graph_key != key) {
+        const long long key[5] = {variant, block, grid, C.n_top, (long long)dyn};
+        if (!s->graph_exec || !std::equal(key, key + 5, s->graph_key)) {
             if (s->graph_exec) { cudaGraphExecDestroy(s->graph_exec); s->graph_exec = nullptr; }
             cudaGraph_t g = nullptr;
             CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
@@ -531,7 +556,7 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
             e = cudaGraphInstantiate(&s->graph_exec, g, 0);
             cudaGraphDestroy(g);
             if (e != cudaSuccess) { s->graph_exec = nullptr; return cuda_fail(e, "cudaGraphInstantiate"); }
-            s->graph_key = key;
+            std::copy(key, key + 5, s->graph_key);
         }
         CK(cudaEventRecord(s->ev0, s->stream));
         CK(cudaGraphLaunch(s->graph_exec, s->stream));
@@ -631,35 +656,65 @@ int mfg_wait(mfg_sim* s, int64_t timeout_ms, mfg_run_stats* stats) {
 
 int mfg_autotune(mfg_sim* s, uint64_t n_trial, int32_t precision, uint64_t seed, mfg_run_options* best) {
     if (!s || (precision != MFG_PREC_FP64 && precision != MFG_PREC_FP32R)) return fail(MFG_ERR_INVALID_ARGUMENT, "bad argument");
-    const int blocks[] = {256};   // 128-thread blocks at the same register budget hold half the threads
-    const int bps64[] = {2, 3, 4};
-    const int bps32[] = {2, 3, 4, 6, 8};
-    double best_rate = -1;
-    mfg_run_options bo{};
-    for (int b : blocks) {
-        const int* bl = precision == MFG_PREC_FP32R ? bps32 : bps64;
-        int nb = precision == MFG_PREC_FP32R ? int(sizeof(bps32) / sizeof(bps32[0])) : int(sizeof(bps64) / sizeof(bps64[0]));
-        for (int k = 0; k < nb; ++k) {
-            mfg_run_options o{};
-            o.precision = precision;
-            o.seed = seed;
-            o.block_size = b;
-            o.blocks_per_sm = bl[k] ? bl[k] : 0;
-            o.time_limit_s = 60;
-            mfg_run_stats st{};
-            double rate = 0;
-            for (int rep = 0; rep < 2; ++rep) {   // the second run is timed
-                int rc = mfg_run(s, n_trial, &o, &st);
-                if (rc != MFG_OK) return rc;
-                rate = double(st.hits) / (st.kernel_ms * 1e-3 + 1e-12);
-            }
-            if (o.blocks_per_sm == 0) o.blocks_per_sm = 0;
-            if (rate > best_rate) { best_rate = rate; bo = o; }
-        }
+    const mfg::HostModel& h = s->model->h;
+    // candidate launch shapes (threads per block, resident blocks per SM): FP64 at register budgets
+    // of 2, 3 and 4 blocks of 256; FP32R at 2 to 8 blocks of 256, and for plain models the 32-register
+    // budget as 4 blocks of 512 or 2 of 1024 threads (shared-memory stagings then serve more warps)
+    std::vector<std::pair<int, int>> shapes;
+    if (precision == MFG_PREC_FP64) {
+        shapes = {{256, 2}, {256, 3}, {256, 4}};
+    } else {
+        shapes = {{256, 2}, {256, 3}, {256, 4}, {256, 6}, {256, 8}};
+        if (!h.has_ext) { shapes.push_back({512, 4}); shapes.push_back({1024, 2}); }
     }
-    s->tuned_block[precision] = bo.block_size;
-    s->tuned_bps[precision] = bo.blocks_per_sm ? bo.blocks_per_sm : 0;
-    if (best) *best = bo;
+    auto trial = [&](int block, int bps, int levels, double& rate) -> int {
+        mfg_run_options o{};
+        o.precision = precision;
+        o.seed = seed;
+        o.block_size = block;
+        o.blocks_per_sm = bps;
+        o.smem_bvh_levels = levels;
+        o.time_limit_s = 60;
+        mfg_run_stats st{};
+        for (int rep = 0; rep < 2; ++rep) {   // the second run is timed
+            int rc = mfg_run(s, n_trial, &o, &st);
+            if (rc != MFG_OK) return rc;
+            rate = double(st.hits) / (st.kernel_ms * 1e-3 + 1e-12);
+        }
+        return MFG_OK;
+    };
+    // stage 1: every shape without staged BVH levels
+    std::vector<std::pair<double, int>> ranked;
+    for (size_t k = 0; k < shapes.size(); ++k) {
+        double rate = 0;
+        int rc = trial(shapes[k].first, shapes[k].second, -1, rate);
+        if (rc != MFG_OK) return rc;
+        ranked.push_back({rate, int(k)});
+    }
+    std::sort(ranked.begin(), ranked.end(), [](const std::pair<double, int>& a, const std::pair<double, int>& b) { return a.first > b.first; });
+    int best_shape = ranked[0].second, best_levels = -1;
+    double best_rate = ranked[0].first;
+    // stage 2 (FP32R): the two fastest shapes with the top 2^5, 2^7 or 2^9 nodes in shared memory
+    if (precision == MFG_PREC_FP32R)
+        for (size_t r = 0; r < std::min<size_t>(2, ranked.size()); ++r)
+            for (int levels : {5, 7, 9}) {
+                double rate = 0;
+                const auto& sh = shapes[ranked[r].second];
+                int rc = trial(sh.first, sh.second, levels, rate);
+                if (rc != MFG_OK) return rc;
+                if (rate > best_rate) { best_rate = rate; best_shape = ranked[r].second; best_levels = levels; }
+            }
+    s->tuned_block[precision] = shapes[best_shape].first;
+    s->tuned_bps[precision] = shapes[best_shape].second;
+    s->tuned_levels[precision] = best_levels;
+    if (best) {
+        *best = mfg_run_options{};
+        best->precision = precision;
+        best->seed = seed;
+        best->block_size = shapes[best_shape].first;
+        best->blocks_per_sm = shapes[best_shape].second;
+        best->smem_bvh_levels = best_levels;
+    }
     return mfg_reset(s);
 }
 

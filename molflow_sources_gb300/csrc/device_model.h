@@ -307,5 +307,6 @@ struct LaunchCtl {
     const unsigned long long* inst_first;    // Philox counter of each instance's first particle
     const volatile int* abort_flag;          // host-mapped
     int smem_facets;                         // 1: moment-0 facet partials in shared memory
+    int n_top;                               // FP32 BVH nodes [0, n_top) staged in shared memory
     SensCtl sens;                            // used by the sensitivity variant
 };

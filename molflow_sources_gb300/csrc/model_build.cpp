@@ -566,6 +566,8 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
                 if (!(cells[c] >= 0)) { err = "facet " + std::to_string(i + 1) + ": negative outgassing-map cell"; return MFG_ERR_INVALID_MODEL; }
                 tot += cells[c];
             }
+            m.final_outgassing_rate += tot / (kKb * m.temperature[i]);
+            m.final_outgassing_rate_pa += tot;
             if (!(tot > 0)) continue;
             if (m.structure[i] == -1) { err = "facet " + std::to_string(i + 1) + " is in all structures, it cannot desorb"; return MFG_ERR_INVALID_MODEL; }
             for (int c = 0; c < ncell; ++c) {
@@ -579,8 +581,17 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
             continue;
         }
         double w;
-        if (m.facet_id[i] >= 0) w = m.id_cum[m.id_start[m.facet_id[i] + 1] - 1];
-        else w = m.latest * m.outgassing[i];
+        if (m.facet_id[i] >= 0) {
+            w = m.id_cum[m.id_start[m.facet_id[i] + 1] - 1];
+            const int p = m.p_outg[i];
+            const double last = m.par_v[m.par_start[p + 1] - 1] * 0.1;   // mbar*l/s -> Pa*m3/s
+            m.final_outgassing_rate += last / (kKb * m.temperature[i]);
+            m.final_outgassing_rate_pa += last;
+        } else {
+            w = m.latest * m.outgassing[i];
+            m.final_outgassing_rate += m.outgassing[i] / (kKb * m.temperature[i]);
+            m.final_outgassing_rate_pa += m.outgassing[i];
+        }
         w /= (kKb * m.temperature[i]);
         if (!(w > 0)) continue;
         if (m.structure[i] == -1) { err = "facet " + std::to_string(i + 1) + " is in all structures, it cannot desorb"; return MFG_ERR_INVALID_MODEL; }
@@ -591,6 +602,7 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
         if (any_map) m.src_cell.push_back(-1);
     }
     m.src_total = sum;
+    m.total_desorbed_molecules = sum;
 
     // unsupported-on-GPU features
     auto unsupported = [&](const std::string& why) {

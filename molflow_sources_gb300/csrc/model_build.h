@@ -63,6 +63,9 @@ struct HostModel {
     std::vector<double> og_ru, og_rv;
     std::vector<OgDev> og;                // per facet (empty: no maps)
     double src_total = 0;
+    // CalcTotalOutgassing (MolflowSimGeom.cpp:290-335): molecules desorbed up to latestMoment, and the
+    // final outgassing rate in molecules/s and Pa*m3/s (the last value of a time-dependent rate)
+    double total_desorbed_molecules = 0, final_outgassing_rate = 0, final_outgassing_rate_pa = 0;
     // layout
     mfg_state_layout layout{};
     std::vector<int64_t> tex_off, dir_off, ang_off, prof_idx;
@@ -102,6 +105,9 @@ struct HostModel {
         int facet_base = 0, nf = 0, struct_base = 0, nstruct = 1, src_base = 0, nsrc = 0;
         int64_t tex_base = 0, prof_base = 0, ang_base = 0, dir_base = 0;
         double src_total = 0;
+    // CalcTotalOutgassing (MolflowSimGeom.cpp:290-335): molecules desorbed up to latestMoment, and the
+    // final outgassing rate in molecules/s and Pa*m3/s (the last value of a time-dependent rate)
+    double total_desorbed_molecules = 0, final_outgassing_rate = 0, final_outgassing_rate_pa = 0;
         mfg_state_layout layout{};
     };
     std::vector<Instance> instances;

@@ -708,8 +708,8 @@ struct NoTranspList {
 
 // kExt: variant for models with transparent facets or histograms (pass list, flight distance,
 // desorption time and reflection count per particle)
-template <bool kFP32, int kMinBlocks, bool kSens = false, bool kExt = false>
-__global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_constant__ DevModel M, DevTally T, LaunchCtl C) {
+template <bool kFP32, int kMinBlocks, bool kSens = false, bool kExt = false, int kBlock = 256>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_constant__ DevModel M, DevTally T, LaunchCtl C) {
     typedef typename Real_<kFP32>::T R;
     extern __shared__ unsigned long long smem[];
     __shared__ double s_cdf_v[MFG_MAXWELL_N], s_cdf_p[MFG_MAXWELL_N];
@@ -719,6 +719,11 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
     B.sfac = C.smem_facets ? smem + TG_N : nullptr;
     const int nsm = TG_N + (C.smem_facets ? M.nf * SF_N : 0);
     for (int i = threadIdx.x; i < nsm; i += blockDim.x) smem[i] = 0ull;
+    // top levels of the FP32 BVH (breadth-first NodeC records [0, n_top)), after the partials
+    float4* s_top = reinterpret_cast<float4*>(smem + nsm);
+    const int n_top = kFP32 ? C.n_top : 0;
+    for (int i = threadIdx.x; i < 4 * n_top; i += blockDim.x)
+        s_top[i] = __ldg(reinterpret_cast<const float4*>(M.nodes_c) + i);
     for (int i = threadIdx.x; i < MFG_MAXWELL_N; i += blockDim.x) {
         s_cdf_v[i] = M.cdf_v[i];
         s_cdf_p[i] = M.cdf_p[i];
@@ -1010,7 +1015,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
                     const unsigned ml = __ballot_sync(0xffffffffu, live && !node);
                     if ((mn | ml) == 0u) break;
                     const bool leaf_round = __popc(ml) > 3 * __popc(mn);
-                    if (leaf_round ? (live && !node) : node) trav_step<kExt>(M, tv, stk, T.global + TG_STATUS, tlp, ocp);
+                    if (leaf_round ? (live && !node) : node) trav_step<kExt>(M, tv, stk, T.global + TG_STATUS, tlp, ocp, s_top, n_top);
                 }
                 if (!active) continue;
                 h = tv.h;

@@ -287,10 +287,13 @@ __device__ __forceinline__ void trav_init(TravF& s, TravStack& stk, int root, co
     stk.sp = 0;
 }
 
-// one step: visit the node or the leaf list `s.ref`, then set the next ref
+// one step: visit the node or the leaf list `s.ref`, then set the next ref.  The first n_top
+// NodeC records (the top levels of structure 0, breadth-first) may be staged in shared memory at
+// `top`; the others are read from global memory.
 template <bool kTr = true>
 __device__ __forceinline__ void trav_step(const DevModel& M, TravF& s, TravStack& stk, unsigned long long* status,
-                                          TranspList<float>* tl = nullptr, const OpacCtx* oc = nullptr) {
+                                          TranspList<float>* tl = nullptr, const OpacCtx* oc = nullptr,
+                                          const float4* top = nullptr, int n_top = 0) {
     const RayF& ray = s.ray;
     const float dx = ray.dx, dy = ray.dy, dz = ray.dz;
     const float ox = ray.ohx, oy = ray.ohy, oz = ray.ohz;
@@ -302,8 +305,14 @@ __device__ __forceinline__ void trav_step(const DevModel& M, TravF& s, TravStack
     bool ambiguous = false;
     if (ref >= 0) {
         // both children's boxes in one 64-byte node
-        const float4* np = reinterpret_cast<const float4*>(M.nodes_c + ref);
-        const float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
+        float4 q0, q1, q2, q3;
+        if (ref < n_top) {
+            const float4* tp = top + 4 * ref;
+            q0 = tp[0]; q1 = tp[1]; q2 = tp[2]; q3 = tp[3];
+        } else {
+            const float4* np = reinterpret_cast<const float4*>(M.nodes_c + ref);
+            q0 = __ldg(np); q1 = __ldg(np + 1); q2 = __ldg(np + 2); q3 = __ldg(np + 3);
+        }
         const float tcap = h.t + 2.0f * htol;
         float a0 = (q0.x - ox) * ix, a1 = (q0.w - ox) * ix;
         float b0 = (q0.y - oy) * iy, b1 = (q1.x - oy) * iy;

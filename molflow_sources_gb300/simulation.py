@@ -62,6 +62,7 @@ def load_library(build_if_missing=True):
         L.mfg_state_layout_of.argtypes = [vp, C.POINTER(A.StateLayout)]
         L.mfg_model_facet_geometry.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.mfg_model_bvh_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        L.mfg_model_outgassing.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.mfg_sim_create.argtypes = [vp, C.c_int, C.POINTER(vp)]
         L.mfg_sim_destroy.argtypes = [vp]
         L.mfg_sim_destroy.restype = None
@@ -148,6 +149,14 @@ class GpuModel:
         _check(load_library().mfg_model_bvh_info(self.h, C.byref(n), C.byref(d), C.byref(l)))
         return {"nodes": n.value, "depth": d.value, "leaves": l.value}
 
+    def outgassing(self):
+        """CalcTotalOutgassing: molecules desorbed up to the latest moment, final rate in molecules/s
+        and in Pa m3/s."""
+        a, b, c = C.c_double(), C.c_double(), C.c_double()
+        _check(load_library().mfg_model_outgassing(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"total_desorbed_molecules": a.value, "final_outgassing_rate": b.value,
+                "final_outgassing_rate_pa_m3_s": c.value}
+
 
 class GpuSimulation:
     """GPU replacement of MolflowSimulation + its ParticleTracer threads."""
@@ -201,12 +210,13 @@ class GpuSimulation:
 
     # --- ParticleTracer surface (Particle.h:45,86) ---
     def SimulationMCStep(self, n_desorptions, precision=A.PREC_FP64, seed=0x4D6F6C66, block_size=0,
-                         blocks_per_sm=0, time_limit_s=0.0, max_steps=0, use_graph=False):
+                         blocks_per_sm=0, time_limit_s=0.0, max_steps=0, use_graph=False, smem_bvh_levels=0):
         """Desorb and trace n_desorptions particles on the GPU (blocking)."""
         if not time_limit_s:
             time_limit_s = float(os.environ.get("MFG_TIME_LIMIT_S", "0"))
         o = A.RunOptions(precision=precision, seed=seed, block_size=block_size, blocks_per_sm=blocks_per_sm,
-                         time_limit_s=time_limit_s, max_steps_per_particle=max_steps, use_graph=int(use_graph))
+                         time_limit_s=time_limit_s, max_steps_per_particle=max_steps, use_graph=int(use_graph),
+                         smem_bvh_levels=smem_bvh_levels)
         st = A.RunStats()
         rc = load_library().mfg_run(self.h, int(n_desorptions), C.byref(o), C.byref(st))
         self.last_stats = {f: getattr(st, f) for f, _ in A.RunStats._fields_}
@@ -225,7 +235,7 @@ class GpuSimulation:
         """Pick the fastest launch shape for this model (clears tallies); returns it as a dict."""
         o = A.RunOptions()
         _check(load_library().mfg_autotune(self.h, int(n_trial), precision, seed, C.byref(o)))
-        return {"block_size": o.block_size, "blocks_per_sm": o.blocks_per_sm}
+        return {"block_size": o.block_size, "blocks_per_sm": o.blocks_per_sm, "smem_bvh_levels": o.smem_bvh_levels}
 
     def run_async(self, n_desorptions, precision=A.PREC_FP64, seed=0x4D6F6C66, time_limit_s=0.0):
         o = A.RunOptions(precision=precision, seed=seed, time_limit_s=time_limit_s)
@@ -324,7 +334,7 @@ class GpuBatch:
         self.last_stats = None
 
     def run(self, counts, precision=A.PREC_FP32R, seed=0x4D6F6C66, use_graph=False, time_limit_s=0.0,
-            block_size=0, blocks_per_sm=0):
+            block_size=0, blocks_per_sm=0, smem_bvh_levels=0):
         """counts: particles per instance (int applies to all)."""
         if np.isscalar(counts):
             counts = [int(counts)] * len(self.models)
@@ -332,7 +342,7 @@ class GpuBatch:
         if not time_limit_s:
             time_limit_s = float(os.environ.get("MFG_TIME_LIMIT_S", "0"))
         o = A.RunOptions(precision=precision, seed=seed, block_size=block_size, blocks_per_sm=blocks_per_sm,
-                         time_limit_s=time_limit_s, use_graph=int(bool(use_graph)))
+                         time_limit_s=time_limit_s, use_graph=int(bool(use_graph)), smem_bvh_levels=smem_bvh_levels)
         st = A.RunStats()
         rc = load_library().mfg_run_batch(self.h, A.ptr(c, C.c_uint64), C.byref(o), C.byref(st))
         self.last_stats = {f: getattr(st, f) for f, _ in A.RunStats._fields_}
@@ -343,7 +353,7 @@ class GpuBatch:
         """Fastest launch shape for the batch (n_trial particles per instance per trial); clears tallies."""
         o = A.RunOptions()
         _check(load_library().mfg_autotune(self.h, int(n_trial), precision, seed, C.byref(o)))
-        return {"block_size": o.block_size, "blocks_per_sm": o.blocks_per_sm}
+        return {"block_size": o.block_size, "blocks_per_sm": o.blocks_per_sm, "smem_bvh_levels": o.smem_bvh_levels}
 
     def fetch_instance(self, i):
         st = SimuState(self.models[i])

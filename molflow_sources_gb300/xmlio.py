@@ -371,6 +371,18 @@ def load_state(r, m):
                     sub = np.zeros((hh, w))
                     sub[:grid.shape[0], :grid.shape[1]] = grid
                     st.texture[mi, o:o + w * hh, field] = sub.reshape(-1)
+            dn = fr.find("Directions")
+            if dn is not None and L["dir_off"][k] >= 0:   # direction cells (LoaderXML.cpp, "Directions")
+                w, hh = int(L["tex_w"][k]), int(L["tex_h"][k])
+                vv, cn = dn.find("vel.vectors"), dn.find("count")
+                o = L["dir_off"][k]
+                if vv is not None and vv.text:
+                    vecs = [c for c in vv.text.replace("\n", "\t").split("\t") if c.strip()]
+                    for c, item in enumerate(vecs[:w * hh]):
+                        st.direction[mi, o + c, :3] = [float(x) for x in item.split(",")]
+                if cn is not None and cn.text:
+                    vals = np.array(cn.text.split(), dtype=np.float64)[:w * hh]
+                    st.direction[mi, o:o + vals.size, 3] = vals
     # recorded incident-angle maps sit in the geometry's facet nodes (LoaderXML.cpp:1043-1070)
     for k, fnode in enumerate(r.find("Geometry").find("Facets").findall("Facet")):
         am = fnode.find("IncidentAngleMap")

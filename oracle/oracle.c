@@ -1154,6 +1154,24 @@ typedef struct {
     int64_t plog_n;
 } otally;
 
+/* Score-function bookkeeping of one thread (orc_run_sens): the parameters of the current
+ * particle's reflections on parameter facets, and the sums that give d(output)/d(sticking):
+ * A[k][j] = Sum over (output event j, earlier reflection on parameter k) of the event's value,
+ * B[k][j] = Sum over absorptions on parameter k counted to output j, Y[j] = Sum of values. */
+#define ORC_SENS_NOUT 9
+#define ORC_SENS_TRAJ 1024
+typedef struct osens {
+    const int32_t* pof;     /* [nf] parameter index or -1 */
+    const int32_t* gof;     /* [nf] gauge index 0..7 or -1 */
+    const uint8_t* pump;    /* [nf] 1: an absorption counts to the pumped flux */
+    double* A;              /* [np * 9] */
+    double* B;              /* [np * 9] */
+    double Y[ORC_SENS_NOUT];
+    int32_t traj[ORC_SENS_TRAJ];
+    int ntraj;
+    uint64_t overflow;
+} osens;
+
 typedef struct {
     double o[3], d[3];
     double time, velocity, ori, dist, gen_time, decay_at, scatter_at;
@@ -1161,7 +1179,22 @@ typedef struct {
     int tele_from;  /* teleportedFrom: destination of the last teleport, -1 none */
     uint64_t bounces;
     double u, v;   /* facetHitDetails of the current facet */
+    osens* S;      /* score-function bookkeeping, or NULL */
 } opart;
+
+/* output event j of value y: the value, and its score pairs with every earlier reflection on a
+ * parameter facet (decisions after the event do not change it) */
+static void sens_out(osens* S, int j, double y) {
+    S->Y[j] += y;
+    const int n = S->ntraj < ORC_SENS_TRAJ ? S->ntraj : ORC_SENS_TRAJ;
+    for (int e = 0; e < n; ++e) S->A[(size_t)S->traj[e] * ORC_SENS_NOUT + j] += y;
+}
+static void sens_reflect(osens* S, int fi) {
+    const int k = S->pof[fi];
+    if (k < 0) return;
+    if (S->ntraj < ORC_SENS_TRAJ) S->traj[S->ntraj++] = k;
+    else if (S->ntraj == ORC_SENS_TRAJ) { S->overflow++; S->ntraj++; }
+}
 
 /* moment blocks of time t: all moments whose [start,end) window contains t
  * (LookupMomentIndex, Particle.cpp:1364-1379, which returns the single window
@@ -1436,6 +1469,7 @@ static void transparent_pass(const orc_model* M, otally* T, int fi, const ohit* 
     P->u = h->u; P->v = h->v;
     facet_counter(M, T, ms, nms, fi, 1, 0, 0, 2.0 / (P->velocity * df),
                   2.0 * (M->use_maxwell ? 1.0 : 1.1781) * P->velocity * df, P);
+    if (P->S && P->S->gof[fi] >= 0) sens_out(P->S, P->S->gof[fi], 2.0 * P->velocity * df);
     if (F->count & MFG_COUNT_TRANS) texture_hit(M, T, ms, nms, F, P, 1, 2.0, 2.0);
     if ((F->count & MFG_COUNT_DIR) && F->dir_off >= 0) direction_hit(M, T, ms, nms, F, P);
     profile_hit(M, T, ms, nms, F, P, 1, 2.0, 2.0);
@@ -1483,6 +1517,14 @@ static void record_absorb(const orc_model* M, otally* T, int fi, opart* P) {
     int ms[256]; int nms = moments_of(M, P->time, ms, 256);
     double ort = P->velocity * fabs(dot3(P->d, F->N));
     facet_counter(M, T, ms, nms, fi, 1, 0, 1, 2.0 / ort, (M->use_maxwell ? 1.0 : 1.1781) * ort, P);
+    if (P->S) {
+        osens* S = P->S;
+        if (S->gof[fi] >= 0) sens_out(S, S->gof[fi], ort);
+        if (S->pump[fi]) {
+            sens_out(S, ORC_SENS_NOUT - 1, 1.0);
+            if (S->pof[fi] >= 0) S->B[(size_t)S->pof[fi] * ORC_SENS_NOUT + ORC_SENS_NOUT - 1] += 1.0;
+        }
+    }
     force_add(M, T, ms, nms, fi, P, 1.0);
     log_hit(M, T, fi, P);
     profile_hit(M, T, ms, nms, F, P, 1, 2.0, 1.0);
@@ -1569,6 +1611,10 @@ static void perform_bounce(const orc_model* M, otally* T, int fi, rng_t* r, opar
     double vf = M->use_maxwell ? 1.0 : 1.1781;
     int ms[256]; int nms = moments_of(M, P->time, ms, 256);
     facet_counter(M, T, ms, nms, fi, 1, 0, 0, 1.0 / ort, vf * ort, P);
+    if (P->S) {
+        if (P->S->gof[fi] >= 0) sens_out(P->S, P->S->gof[fi], ort);
+        sens_reflect(P->S, fi);
+    }
     force_add(M, T, ms, nms, fi, P, 1.0);
     log_hit(M, T, fi, P);
     P->bounces++;
@@ -1601,13 +1647,14 @@ static void perform_bounce(const orc_model* M, otally* T, int fi, rng_t* r, opar
     if (F->moving) treat_moving(M, P);
     ort = P->velocity * fabs(dot3(P->d, F->N));
     facet_counter(M, T, ms, nms, fi, 0, 0, 0, 1.0 / ort, vf * ort, P);
+    if (P->S && P->S->gof[fi] >= 0) sens_out(P->S, P->S->gof[fi], ort);
     force_add(M, T, ms, nms, fi, P, -1.0);
     if (F->count & MFG_COUNT_REFL) texture_hit(M, T, ms, nms, F, P, 0, 1.0, 1.0);
     profile_hit(M, T, ms, nms, F, P, 0, 1.0, 1.0);
     P->last = fi;
 }
 
-typedef struct { otally T; orc_stats st; } othread;
+typedef struct { otally T; orc_stats st; osens* S; } othread;
 
 static void tally_alloc(const orc_model* M, otally* T) {
     const mfg_state_layout* L = &M->L;
@@ -1661,9 +1708,13 @@ static int perform_scatter(const orc_model* M, otally* T, rng_t* r, opart* P) {
 }
 
 static int trace_particle(const orc_model* M, otally* T, rng_t* r, uint64_t max_steps, orc_stats* st,
-                          int64_t* nrec, int64_t maxrec, double* ro, double* rd, int32_t* rl, int32_t* rh, double* rt) {
+                          int64_t* nrec, int64_t maxrec, double* ro, double* rd, int32_t* rl, int32_t* rh, double* rt,
+                          osens* S) {
     opart P;
+    P.S = NULL;
     if (!start_from_source(M, T, r, &P)) return -1;
+    P.S = S;
+    if (S) S->ntraj = 0;
     st->desorbed++;
     oisect H;
     for (uint64_t step = 0;; ++step) {
@@ -1741,8 +1792,30 @@ int orc_run(orc_model* M, uint64_t n_des, const orc_run_opts* o, mfg_state_view*
     return orc_run_logged(M, n_des, o, view, st, NULL, 0, NULL);
 }
 
+/* sensitivity set-up of a run: facet maps, parameter count and the caller's sums (NULL: none) */
+typedef struct {
+    const int32_t* pof; const int32_t* gof; const uint8_t* pump;
+    int np;
+    double* A; double* B; double* Y; uint64_t* overflow;
+} osens_run;
+
+static int run_impl(orc_model* M, uint64_t n_des, const orc_run_opts* o, mfg_state_view* view, orc_stats* st,
+                    double* log, int64_t log_capacity, int64_t* log_n, const osens_run* sr);
+
 int orc_run_logged(orc_model* M, uint64_t n_des, const orc_run_opts* o, mfg_state_view* view, orc_stats* st,
                    double* log, int64_t log_capacity, int64_t* log_n) {
+    return run_impl(M, n_des, o, view, st, log, log_capacity, log_n, NULL);
+}
+
+int orc_run_sens(orc_model* M, uint64_t n_des, const orc_run_opts* o, mfg_state_view* view, orc_stats* st,
+                 const int32_t* param_of_facet, const int32_t* gauge_of_facet, const uint8_t* pump_of_facet,
+                 int32_t n_params, double* A, double* B, double* Y, uint64_t* overflow) {
+    osens_run sr = {param_of_facet, gauge_of_facet, pump_of_facet, n_params, A, B, Y, overflow};
+    return run_impl(M, n_des, o, view, st, NULL, 0, NULL, &sr);
+}
+
+static int run_impl(orc_model* M, uint64_t n_des, const orc_run_opts* o, mfg_state_view* view, orc_stats* st,
+                    double* log, int64_t log_capacity, int64_t* log_n, const osens_run* sr) {
     if (log_n) *log_n = 0;
     if (M->nsrc == 0) return MFG_ERR_NO_SOURCE;
     int nt = o->n_threads;
@@ -1763,6 +1836,12 @@ int orc_run_logged(orc_model* M, uint64_t n_des, const orc_run_opts* o, mfg_stat
 #endif
         othread* me = &th[tid];
         tally_alloc(M, &me->T);
+        if (sr) {
+            me->S = (osens*)calloc(1, sizeof(osens));
+            me->S->pof = sr->pof; me->S->gof = sr->gof; me->S->pump = sr->pump;
+            me->S->A = (double*)calloc((size_t)sr->np * ORC_SENS_NOUT + 1, sizeof(double));
+            me->S->B = (double*)calloc((size_t)sr->np * ORC_SENS_NOUT + 1, sizeof(double));
+        }
         rng_t r; memset(&r, 0, sizeof r);
         r.mode = o->rng_mode;
         r.key[0] = (uint32_t)o->seed; r.key[1] = (uint32_t)(o->seed >> 32);
@@ -1771,7 +1850,7 @@ int orc_run_logged(orc_model* M, uint64_t n_des, const orc_run_opts* o, mfg_stat
 #pragma omp for schedule(dynamic, 256)
         for (long long i = 0; i < (long long)n_des; ++i) {
             rng_start_particle(&r, o->first_particle + (uint64_t)i);
-            if (trace_particle(M, &me->T, &r, max_steps, &me->st, NULL, 0, NULL, NULL, NULL, NULL, NULL) < 0) err = 1;
+            if (trace_particle(M, &me->T, &r, max_steps, &me->st, NULL, 0, NULL, NULL, NULL, NULL, NULL, me->S) < 0) err = 1;
         }
     }
     double t1 = now_s();
@@ -1799,6 +1878,13 @@ int orc_run_logged(orc_model* M, uint64_t n_des, const orc_run_opts* o, mfg_stat
         st->dropped += th[t].st.dropped; st->rays += th[t].st.rays;
         st->node_visits += th[t].st.node_visits; st->prim_tests += th[t].st.prim_tests;
         tally_free(T);
+        if (th[t].S) {   /* per-thread score sums, added in thread order */
+            osens* S = th[t].S;
+            for (size_t k = 0; k < (size_t)sr->np * ORC_SENS_NOUT; ++k) { sr->A[k] += S->A[k]; sr->B[k] += S->B[k]; }
+            for (int j = 0; j < ORC_SENS_NOUT; ++j) sr->Y[j] += S->Y[j];
+            if (sr->overflow) *sr->overflow += S->overflow;
+            free(S->A); free(S->B); free(S);
+        }
     }
     st->seconds = t1 - t0;
     st->threads = nt;
@@ -1830,7 +1916,7 @@ int64_t orc_record_rays(orc_model* M, uint64_t n_des, uint64_t seed, int64_t max
     int64_t nrec = 0;
     for (uint64_t i = 0; i < n_des && nrec < max_rays; ++i) {
         rng_start_particle(&r, i);
-        trace_particle(M, &T, &r, (uint64_t)1 << 40, &st, &nrec, max_rays, origin, dir, last, hit_facet, hit_t);
+        trace_particle(M, &T, &r, (uint64_t)1 << 40, &st, &nrec, max_rays, origin, dir, last, hit_facet, hit_t, NULL);
     }
     tally_free(&T);
     return nrec;

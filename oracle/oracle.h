@@ -65,6 +65,15 @@ int  orc_run(orc_model* m, uint64_t n_des, const orc_run_opts* o, mfg_state_view
  * threads, up to log_capacity records; *log_n receives the number returned. */
 int  orc_run_logged(orc_model* m, uint64_t n_des, const orc_run_opts* o, mfg_state_view* view, orc_stats* st,
                     double* log, int64_t log_capacity, int64_t* log_n);
+/* orc_run with score-function sensitivity sums (the GPU's mfg_sens_forward bookkeeping): per
+ * facet its parameter index (-1 none), gauge index 0..7 (-1 none) and whether absorptions count
+ * to the pumped flux (output 8).  Adds into A[n_params*9] (Sum over output events and earlier
+ * reflections on parameter k of the event's value), B[n_params*9] (absorptions on parameter k
+ * counted to the pumped flux), Y[9] (Sum of values), *overflow (particles whose reflection list
+ * overflowed).  d output_j / d sticking_k = (-A[k][j]/(1-s_k) + B[k][j]/s_k) / n. */
+int  orc_run_sens(orc_model* m, uint64_t n_des, const orc_run_opts* o, mfg_state_view* view, orc_stats* st,
+                  const int32_t* param_of_facet, const int32_t* gauge_of_facet, const uint8_t* pump_of_facet,
+                  int32_t n_params, double* A, double* B, double* Y, uint64_t* overflow);
 /* Intersect given rays (replay mode). */
 int  orc_replay(orc_model* m, int64_t n, const double* origin, const double* dir, const int32_t* last,
                 int32_t* hit_facet, double* hit_t, orc_stats* st);

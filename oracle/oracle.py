@@ -22,8 +22,8 @@ ORC_RNG_PHILOX, ORC_RNG_MT = 0, 1
 def build(force=False):
     """Compile oracle.c with gcc (OpenMP, no FMA contraction so x86 and Arm agree)."""
     src = os.path.join(HERE, "oracle.c")
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
-            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "oracle.h"))):
+    deps = [src, os.path.join(HERE, "oracle.h"), os.path.join(os.path.dirname(HERE), "include", "mfg.h")]
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(d) for d in deps):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     tmp = LIB + ".tmp%d" % os.getpid()
@@ -61,6 +61,10 @@ def lib():
         L.orc_run.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(OrcRunOpts), C.POINTER(A.StateView), C.POINTER(OrcStats)]
         L.orc_run_logged.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(OrcRunOpts), C.POINTER(A.StateView),
                                      C.POINTER(OrcStats), C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_int64)]
+        L.orc_run_sens.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(OrcRunOpts), C.POINTER(A.StateView),
+                                   C.POINTER(OrcStats), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                   C.POINTER(C.c_uint8), C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                   C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
         L.orc_replay.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                  C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(OrcStats)]
         L.orc_record_rays.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int64, C.POINTER(C.c_double),
@@ -134,6 +138,36 @@ class Oracle:
         if rc != 0:
             raise OracleError(A.STATUS_NAMES.get(rc, rc))
         return st, log[:n.value]
+
+    def run_sens(self, n_des, params, gauges, pumps, seed=0x4D6F6C66, first_particle=0, threads=0):
+        """Trace n_des particles with the score-function bookkeeping of the GPU's sensitivity
+        kernel.  Returns (outputs[9] per desorbed particle, d outputs / d sticking [P, 9])."""
+        nf = self.model.n_facets
+        pof = np.full(nf, -1, np.int32)
+        gof = np.full(nf, -1, np.int32)
+        pump = np.zeros(nf, np.uint8)
+        pof[np.asarray(params)] = np.arange(len(params), dtype=np.int32)
+        gof[np.asarray(gauges)] = np.arange(len(gauges), dtype=np.int32)
+        pump[np.asarray(pumps)] = 1
+        P = len(params)
+        a = np.zeros(P * 9 + 1)
+        b = np.zeros(P * 9 + 1)
+        y = np.zeros(9)
+        ovf = C.c_uint64(0)
+        st = SimuState(self.model)
+        v = st.view()
+        s = OrcStats()
+        o = OrcRunOpts(seed=seed, first_particle=first_particle, n_threads=threads, rng_mode=ORC_RNG_PHILOX)
+        rc = lib().orc_run_sens(self.h, n_des, C.byref(o), C.byref(v), C.byref(s), A.ptr(pof, C.c_int32),
+                                A.ptr(gof, C.c_int32), A.ptr(pump, C.c_uint8), P, A.ptr(a, C.c_double),
+                                A.ptr(b, C.c_double), A.ptr(y, C.c_double), C.byref(ovf))
+        if rc != 0:
+            raise OracleError(A.STATUS_NAMES.get(rc, rc))
+        if ovf.value:
+            raise OracleError("reflection list overflowed for %d particles" % ovf.value)
+        s_k = np.asarray(self.model.sticking, np.float64)[np.asarray(params)][:, None]
+        jac = (-a[:P * 9].reshape(P, 9) / (1.0 - s_k) + b[:P * 9].reshape(P, 9) / s_k) / n_des
+        return y / n_des, jac
 
     def replay(self, origin, direction, last):
         n = len(last)

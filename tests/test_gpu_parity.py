@@ -250,20 +250,29 @@ def test_kernel_time_limit_returns_status_and_context_survives():
 
 
 def test_autotune_and_occupancy_variants_agree(tube):
-    """Every launch shape gives identical FP32R tallies for the same particles."""
+    """Every launch shape (block size, register budget, BVH levels staged in shared memory) gives
+    identical FP32R tallies for the same particles."""
     sim = GpuSimulation(tube)
     ref = None
-    for bps in (2, 3, 4, 6, 8):
+    shapes = [(256, b, -1) for b in (2, 3, 4, 6, 8)] + [(512, 4, -1), (1024, 2, -1), (256, 8, 5), (256, 6, 9),
+                                                       (512, 4, 7), (1024, 2, 12)]
+    for block, bps, lv in shapes:
         sim.ResetSimulation()
         sim.set_particle_offset(0)
-        sim.SimulationMCStep(20000, precision=A.PREC_FP32R, seed=SEED, blocks_per_sm=bps)
+        sim.SimulationMCStep(20000, precision=A.PREC_FP32R, seed=SEED, block_size=block, blocks_per_sm=bps,
+                             smem_bvh_levels=lv)
         st = sim.fetch()
         if ref is None:
             ref = st
-        assert np.array_equal(st.facet_counts, ref.facet_counts)
+        assert np.array_equal(st.facet_counts, ref.facet_counts), (block, bps, lv)
+        assert np.array_equal(st.texture, ref.texture), (block, bps, lv)
     best = sim.autotune(20000)
-    assert best["block_size"] == 256 and best["blocks_per_sm"] in (2, 3, 4, 6, 8)
+    assert (best["block_size"], best["blocks_per_sm"]) in [(b, k) for b, k, _ in shapes]
+    assert best["smem_bvh_levels"] in (-1, 5, 7, 9)
     assert sim.fetch().n_desorbed == 0
+    # the tuned shape is the default afterwards
+    sim.SimulationMCStep(20000, precision=A.PREC_FP32R, seed=SEED)
+    assert sim.last_stats["desorbed"] == 20000
 
 
 def test_unsupported_feature_is_reported():
