@@ -435,8 +435,12 @@ static const void* kernel_of(int variant) {
         case 8: return (const void*)mfgk::trace_kernel<true, 8>;
         case 9: return (const void*)mfgk::trace_kernel<true, 4, false, false, 512>;
         case 10: return (const void*)mfgk::trace_kernel<true, 2, false, false, 1024>;
+        case 18: return (const void*)mfgk::trace_kernel<true, 8, false, false, 256, true>;
+        case 20: return (const void*)mfgk::trace_kernel<true, 2, false, false, 1024, true>;
         case 12: return (const void*)mfgk::trace_kernel<false, 2, true>;
         case 13: return (const void*)mfgk::trace_kernel<true, 3, true>;
+        case 14: return (const void*)mfgk::trace_kernel<true, 2, true>;
+        case 15: return (const void*)mfgk::trace_kernel<true, 4, true>;
         case 100: return (const void*)mfgk::trace_kernel<false, 2, false, true>;
         case 102: return (const void*)mfgk::trace_kernel<true, 2, false, true>;
         case 112: return (const void*)mfgk::trace_kernel<false, 2, true, true>;
@@ -485,7 +489,10 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     C.inst_prefix = reinterpret_cast<const unsigned long long*>(s->d_run + sizeof(RunDesc));
     C.inst_first = C.inst_prefix + ni + 1;
     C.abort_flag = s->d_abort;
-    if (sens) C.sens = s->sens;
+    if (sens) {
+        C.sens = s->sens;
+        C.sens.smem_code = size_t(h.nf) * 4 <= 48 * 1024 ? 1 : 0;   // packed per-facet words in shared memory
+    }
     if (o.block_size == 0 && o.blocks_per_sm == 0 && s->tuned_block[o.precision]) {
         o.block_size = s->tuned_block[o.precision];
         o.blocks_per_sm = s->tuned_bps[o.precision];
@@ -503,9 +510,10 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     // moment-0 facet partials in shared memory when they fit the block's share of the SM (228 KB)
     const size_t fac_bytes = size_t(h.nf) * SF_N * 8;
     C.smem_facets = fac_bytes <= std::min<size_t>(96 * 1024, 200 * 1024 / size_t(bps_req)) ? 1 : 0;
-    C.n_top = o.precision == MFG_PREC_FP32R && o.smem_bvh_levels > 0
+    C.n_top = o.precision == MFG_PREC_FP32R && o.smem_bvh_levels > 0 && !sens
                   ? int(std::min<size_t>(size_t(1) << o.smem_bvh_levels, h.nodes_c.size())) : 0;
-    size_t dyn = (TG_N + (C.smem_facets ? size_t(h.nf) * SF_N : 0)) * 8 + size_t(C.n_top) * sizeof(NodeC);
+    size_t dyn = (TG_N + (C.smem_facets ? size_t(h.nf) * SF_N : 0)) * 8 + size_t(C.n_top) * sizeof(NodeC) +
+                 (sens && C.sens.smem_code ? size_t(h.nf) * 4 : 0);
     // kernel variant: FP64 compiled for at least 2, 3 or 4 resident blocks per SM (register budgets
     // 128, 80, 64), FP32R for 2, 3, 4, 6 or 8 (128, 80, 64, 40, 32); blocks_per_sm selects the
     // variant.  Models with transparent facets, histograms, low-flux mode, scattering, moving
@@ -513,17 +521,25 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     // variants.
     int variant = 0;
     const int b = int(o.blocks_per_sm);
-    if (sens) {
-        variant = o.precision == MFG_PREC_FP32R ? 13 : 12;
+    if (sens) {   // FP32R sensitivity kernel at the register budget of 2, 3 or 4 resident blocks
+        variant = o.precision == MFG_PREC_FP32R ? (b >= 4 ? 15 : (b == 3 ? 13 : 14)) : 12;
     } else if (o.precision == MFG_PREC_FP32R) {
         variant = (b == 3 || b == 4 || b == 6 || b == 8) ? b : (b == 5 ? 4 : (b == 7 ? 6 : (b > 8 ? 8 : 2)));
         if (block == 512) variant = 9;     // 4 blocks of 512 threads, 32 registers
         if (block == 1024) variant = 10;   // 2 blocks of 1024 threads, 32 registers
+        if (C.n_top > 0) {                 // staged BVH levels: compiled for 8 x 256 and 2 x 1024
+            if (variant != 8 && variant != 10)
+                return fail(MFG_ERR_INVALID_ARGUMENT, "smem_bvh_levels is compiled for the 256x8 and 1024x2 launch shapes");
+            variant += 10;
+        }
     } else {
         variant = b == 3 ? 203 : (b >= 4 ? 204 : 0);
     }
-    // extended variants: FP64 100, FP32R 102; with sensitivities FP64 112, FP32R 113
-    if (h.has_ext) variant = sens ? variant + 100 : (o.precision == MFG_PREC_FP64 ? 100 : 102);
+    // extended variants: FP64 100, FP32R 102; with sensitivities FP64 112, FP32R 113 (any budget)
+    if (h.has_ext) {
+        if (C.n_top > 0) return fail(MFG_ERR_INVALID_ARGUMENT, "smem_bvh_levels is compiled for plain models");
+        variant = sens ? (o.precision == MFG_PREC_FP64 ? 112 : 113) : (o.precision == MFG_PREC_FP64 ? 100 : 102);
+    }
     const void* fn = kernel_of(variant);
     CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn)));
     int per_sm = 0;
@@ -694,12 +710,14 @@ int mfg_autotune(mfg_sim* s, uint64_t n_trial, int32_t precision, uint64_t seed,
     std::sort(ranked.begin(), ranked.end(), [](const std::pair<double, int>& a, const std::pair<double, int>& b) { return a.first > b.first; });
     int best_shape = ranked[0].second, best_levels = -1;
     double best_rate = ranked[0].first;
-    // stage 2 (FP32R): the two fastest shapes with the top 2^5, 2^7 or 2^9 nodes in shared memory
-    if (precision == MFG_PREC_FP32R)
-        for (size_t r = 0; r < std::min<size_t>(2, ranked.size()); ++r)
+    // stage 2 (FP32R, plain models): the 8 x 256 and 2 x 1024 shapes with the top 2^5, 2^7 or 2^9
+    // nodes in shared memory
+    if (precision == MFG_PREC_FP32R && !h.has_ext)
+        for (size_t r = 0; r < ranked.size(); ++r)
             for (int levels : {5, 7, 9}) {
-                double rate = 0;
                 const auto& sh = shapes[ranked[r].second];
+                if (!(sh.first == 256 && sh.second == 8) && !(sh.first == 1024 && sh.second == 2)) continue;
+                double rate = 0;
                 int rc = trial(sh.first, sh.second, levels, rate);
                 if (rc != MFG_OK) return rc;
                 if (rate > best_rate) { best_rate = rate; best_shape = ranked[r].second; best_levels = levels; }
@@ -997,7 +1015,12 @@ int mfg_sens_setup(mfg_sim* s, int32_t n_params, const int32_t* param_facets, in
     for (size_t k = 0; k < h.src_facet.size(); ++k) { sof[h.src_facet[k]] = int32_t(k); s->sens_src.push_back(h.src_facet[k]); }
     s->sens_params.assign(param_facets, param_facets + n_params);
     const size_t P = size_t(std::max(n_params, 1)), S = std::max<size_t>(s->sens_src.size(), 1), nf = size_t(h.nf);
-    const size_t off_pof = 0, off_gof = off_pof + 4 * nf, off_sof = off_gof + 4 * nf, off_pump = off_sof + 4 * nf;
+    if (n_params >= (1 << 20) - 1) return fail(MFG_ERR_INVALID_ARGUMENT, "at most 2^20 - 2 parameters");
+    std::vector<int32_t> code(h.nf, 0);   // packed: parameter + 1 (bits 0-19), gauge + 1 (20-23), pump (24)
+    for (int f = 0; f < h.nf; ++f)
+        code[f] = (pof[f] + 1) | ((gof[f] + 1) << 20) | (int32_t(pump[f]) << 24);
+    const size_t off_pof = 0, off_gof = off_pof + 4 * nf, off_sof = off_gof + 4 * nf, off_code = off_sof + 4 * nf;
+    const size_t off_pump = off_code + 4 * nf;
     const size_t off_A = (off_pump + nf + 255) / 256 * 256, off_B = off_A + 8 * P * MFG_SENS_NOUT;
     const size_t off_C = off_B + 8 * P * MFG_SENS_NOUT, off_Y = off_C + 8 * S * MFG_SENS_NOUT;
     const size_t off_cnt = off_Y + 8 * MFG_SENS_NOUT, off_ovf = off_cnt + 8 * S, total = off_ovf + 8;
@@ -1009,6 +1032,8 @@ int mfg_sens_setup(mfg_sim* s, int32_t n_params, const int32_t* param_facets, in
     CK(cudaMemcpy(b + off_gof, gof.data(), 4 * nf, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(b + off_sof, sof.data(), 4 * nf, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(b + off_pump, pump.data(), nf, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b + off_code, code.data(), 4 * nf, cudaMemcpyHostToDevice));
+    s->sens.code = reinterpret_cast<const int32_t*>(b + off_code);
     s->sens.param_of_facet = reinterpret_cast<const int32_t*>(b + off_pof);
     s->sens.gauge_of_facet = reinterpret_cast<const int32_t*>(b + off_gof);
     s->sens.src_of_facet = reinterpret_cast<const int32_t*>(b + off_sof);

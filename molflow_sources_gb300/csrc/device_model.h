@@ -292,6 +292,11 @@ struct SensCtl {
     const int32_t* gauge_of_facet;   // [nf] gauge index 0..7, -1 otherwise
     const uint8_t* pump_of_facet;    // [nf] 1 when an absorption counts to the pumped flux
     const int32_t* src_of_facet;     // [nf] source index for outgassing gradients, -1 otherwise
+    // [nf] the three maps above packed into one word per facet, read once per hit: bits 0-19
+    // parameter index + 1, bits 20-23 gauge index + 1 (0: none), bit 24 pump
+    const int32_t* code;
+    int32_t smem_code;               // 1: the packed words are staged in shared memory
+    int32_t pad_code;
     double* A;                       // [P][9] sum over (output event, earlier reflection on parameter k) of y
     double* B;                       // [P][9] sum over absorptions on parameter k of y
     double* Cs;                      // [S][9] sum of y per source

@@ -112,6 +112,22 @@ __device__ __forceinline__ double interp_x_d(double y, const double* xs, const d
     double w = (y - y0) / (y1 - y0);
     return xs[i] + (xs[i + 1] - xs[i]) * w;
 }
+// The same interval search started from a guide table: g[b] = number of ys <= b / MFG_GUIDE_N,
+// so that y in bucket b starts next to its interval and one or two steps find the index the
+// binary search finds (any start gives the same index, as ys is non-decreasing).
+#define MFG_GUIDE_N 128
+__device__ __forceinline__ float interp_x_guided(float y, const float* xs, const float* ys, const unsigned char* g, int n) {
+    int b = (int)(y * (float)MFG_GUIDE_N);
+    b = min(max(b, 0), MFG_GUIDE_N - 1);
+    int lo = g[b];
+    while (lo > 0 && ys[lo - 1] > y) --lo;
+    while (lo < n && ys[lo] <= y) ++lo;
+    int i = lo - 1;
+    if (i < 0) i = 0;
+    if (i > n - 2) i = n - 2;
+    float w = (y - ys[i]) / (ys[i + 1] - ys[i]);
+    return xs[i] + (xs[i + 1] - xs[i]) * w;
+}
 __device__ __forceinline__ float interp_x_f(float y, const float* xs, const float* ys, int n) {
     int lo = 0, hi = n;
     while (lo < hi) { int mid = (lo + hi) >> 1; if (ys[mid] <= y) lo = mid + 1; else hi = mid; }
@@ -708,12 +724,14 @@ struct NoTranspList {
 
 // kExt: variant for models with transparent facets or histograms (pass list, flight distance,
 // desorption time and reflection count per particle)
-template <bool kFP32, int kMinBlocks, bool kSens = false, bool kExt = false, int kBlock = 256>
+// kTop: variant that reads the top BVH levels staged in shared memory (C.n_top nodes)
+template <bool kFP32, int kMinBlocks, bool kSens = false, bool kExt = false, int kBlock = 256, bool kTop = false>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_constant__ DevModel M, DevTally T, LaunchCtl C) {
     typedef typename Real_<kFP32>::T R;
     extern __shared__ unsigned long long smem[];
     __shared__ double s_cdf_v[MFG_MAXWELL_N], s_cdf_p[MFG_MAXWELL_N];
     __shared__ float s_cdf_vf[MFG_MAXWELL_N], s_cdf_pf[MFG_MAXWELL_N];
+    __shared__ unsigned char s_guide[MFG_GUIDE_N];
     BlockTally B;
     B.sglob = smem;
     B.sfac = C.smem_facets ? smem + TG_N : nullptr;
@@ -721,14 +739,33 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_
     for (int i = threadIdx.x; i < nsm; i += blockDim.x) smem[i] = 0ull;
     // top levels of the FP32 BVH (breadth-first NodeC records [0, n_top)), after the partials
     float4* s_top = reinterpret_cast<float4*>(smem + nsm);
-    const int n_top = kFP32 ? C.n_top : 0;
+    const int n_top = (kFP32 && kTop) ? C.n_top : 0;
     for (int i = threadIdx.x; i < 4 * n_top; i += blockDim.x)
         s_top[i] = __ldg(reinterpret_cast<const float4*>(M.nodes_c) + i);
+    // the sensitivity variants (no staged nodes) stage their packed per-facet words after the partials
+    int* s_ring = reinterpret_cast<int*>(s_top + 4 * n_top);
+    const int* scodes = nullptr;
+    if constexpr (kSens) {
+        if (C.sens.smem_code) {
+            for (int i = threadIdx.x; i < M.nf; i += blockDim.x) s_ring[i] = __ldg(C.sens.code + i);
+            scodes = s_ring;
+        } else {
+            scodes = C.sens.code;
+        }
+    }
+    // packed sensitivity word of a facet: parameter (bits 0-19, +1), gauge (20-23, +1), pump (24)
+    auto scode = [&](int f) -> int { return kSens ? scodes[f] : 0; };
     for (int i = threadIdx.x; i < MFG_MAXWELL_N; i += blockDim.x) {
         s_cdf_v[i] = M.cdf_v[i];
         s_cdf_p[i] = M.cdf_p[i];
         s_cdf_vf[i] = (float)M.cdf_v[i];
         s_cdf_pf[i] = (float)M.cdf_p[i];
+    }
+    for (int b = threadIdx.x; b < MFG_GUIDE_N; b += blockDim.x) {
+        const float yb = (float)b / (float)MFG_GUIDE_N;
+        int c = 0;
+        for (int i = 0; i < MFG_MAXWELL_N; ++i) c += ((float)M.cdf_p[i] <= yb) ? 1 : 0;
+        s_guide[b] = (unsigned char)c;
     }
     __syncthreads();
 
@@ -885,7 +922,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_
             }
             // speed: Maxwell at the facet temperature (desorption and full-accommodation reflection)
             if (law < 3) {
-                if (kFP32) vel = (R)(M.phys_f[fo].sqrtT * interp_x_f((float)rng.next(), s_cdf_vf, s_cdf_pf, MFG_MAXWELL_N));
+                if (kFP32) vel = (R)(M.phys_f[fo].sqrtT * interp_x_guided((float)rng.next(), s_cdf_vf, s_cdf_pf, s_guide, MFG_MAXWELL_N));
                 else vel = (R)(M.phys_d[fo].sqrtT * interp_x_d((double)rng.next(), s_cdf_v, s_cdf_p, MFG_MAXWELL_N));
             } else if (law & 4) {
                 vel = (R)(145.469 * sqrt(M.info2[fo].temperature / M.gas_mass));
@@ -947,7 +984,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_
                     }
                 }
                 if (kSens && !des) {
-                    int g = C.sens.gauge_of_facet[fo];
+                    const int g = ((scode(fo) >> 20) & 15) - 1;
                     if (g >= 0) sens_output(C.sens, traj, ntraj, src_idx, g, (double)ort);   // outgoing half at a gauge
                 }
                 const unsigned long long vf = des ? 2 : 1;   // velocity factor of the 1/v_ort sum
@@ -1074,7 +1111,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_
                 if (!((double)tl.t[k] < travel)) continue;
                 double ort_t = transparent_pass<kFP32>(M, T, B, tl.f[k], tl.t[k], tl.u[k], tl.v[k], P.time, vel, dx, dy, dz);
                 if (kSens) {
-                    int g = C.sens.gauge_of_facet[tl.f[k]];
+                    const int g = ((scode(tl.f[k]) >> 20) & 15) - 1;
                     if (g >= 0) sens_output(C.sens, traj, ntraj, src_idx, g, 2.0 * ort_t);
                 }
             }
@@ -1150,11 +1187,12 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_
             if (In.count & MFG_COUNT_DIR)
                 direction_add(M, T, hf, (double)hu, (double)hv, P.time, ddx * (double)vel, ddy * (double)vel, ddz * (double)vel);
             if (kSens) {
-                int g = C.sens.gauge_of_facet[hf];
+                const int code = scode(hf);
+                const int g = ((code >> 20) & 15) - 1;
                 if (g >= 0) sens_output(C.sens, traj, ntraj, src_idx, g, (double)ort);   // incoming half / absorption
-                int k = C.sens.param_of_facet[hf];
+                const int k = (code & 0xFFFFF) - 1;
                 if (absorb) {
-                    if (C.sens.pump_of_facet[hf]) {
+                    if ((code >> 24) & 1) {
                         sens_output(C.sens, traj, ntraj, src_idx, MFG_SENS_NOUT - 1, 1.0);
                         if (k >= 0) atomicAdd(C.sens.B + (size_t)k * MFG_SENS_NOUT + MFG_SENS_NOUT - 1, 1.0);
                     }
@@ -1265,7 +1303,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_
         pv = hv;
         c_hits += (do_abs ? 1 : 0) + (do_refl ? 1 : 0);
         if (kSens) {
-            int g = C.sens.gauge_of_facet[hf];
+            const int g = ((scode(hf) >> 20) & 15) - 1;
             if (g >= 0) sens_output(C.sens, traj, ntraj, src_idx, g, (double)ort);   // incoming half / absorption
         }
         if (do_abs) {   // RecordAbsorb (Particle.cpp:888-924)
@@ -1282,8 +1320,9 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_
                 direction_add(M, T, hf, (double)hu, (double)hv, P.time, wa * ddx * (double)vel, wa * ddy * (double)vel,
                               wa * ddz * (double)vel);
             if (kSens) {
-                int k = C.sens.param_of_facet[hf];
-                if (C.sens.pump_of_facet[hf]) {
+                const int code = scode(hf);
+                const int k = (code & 0xFFFFF) - 1;
+                if ((code >> 24) & 1) {
                     sens_output(C.sens, traj, ntraj, src_idx, MFG_SENS_NOUT - 1, 1.0);
                     if (k >= 0) atomicAdd(C.sens.B + (size_t)k * MFG_SENS_NOUT + MFG_SENS_NOUT - 1, 1.0);
                 }
@@ -1337,7 +1376,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_
                 direction_add(M, T, hf, (double)hu, (double)hv, P.time, wr * ddx * (double)vel, wr * ddy * (double)vel,
                               wr * ddz * (double)vel);
             if (kSens) {
-                int k = C.sens.param_of_facet[hf];
+                const int k = (scode(hf) & 0xFFFFF) - 1;
                 if (k >= 0) {
                     if (ntraj < MFG_SENS_TRAJ) traj[ntraj++] = k;
                     else if (ntraj == MFG_SENS_TRAJ) { atomicAdd(C.sens.overflow, 1ull); ++ntraj; }

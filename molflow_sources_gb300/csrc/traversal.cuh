@@ -14,15 +14,16 @@
 namespace mfgk {
 
 constexpr int kStack = 64;
-// Traversal stack of one thread (local memory; a shared-memory copy of the first levels was
-// measured slower, 26-36 % under the lockstep traversal, as it takes L1 capacity from the BVH
-// nodes and facet records).
+// Traversal stack of one thread, in local memory.  Keeping its top 8 or 16 entries in shared
+// memory (one bank per lane) measured 2x slower on the beam chamber and 1.5x on the tube (1024 x 2
+// launch shape): the rings' shared memory comes out of the L1 that holds the BVH nodes.
 struct TravStack {
     int sp;
     int loc[kStack];
     __device__ __forceinline__ void push(int v) { loc[sp++] = v; }
     __device__ __forceinline__ int pop() { return loc[--sp]; }
 };
+
 
 // InterpolateY (no extrapolation) for time-dependent parameters
 __device__ __noinline__ double param_at(const DevModel& M, int p, double t) {
@@ -272,7 +273,8 @@ struct TravF {
     bool amb;      // a candidate could be classified differently in exact arithmetic
 };
 
-__device__ __forceinline__ void trav_init(TravF& s, TravStack& stk, int root, const RayF& ray, int last) {
+template <class Stk>
+__device__ __forceinline__ void trav_init(TravF& s, Stk& stk, int root, const RayF& ray, int last) {
     s.ray = ray;
     s.ix = 1.0f / ray.dx;
     s.iy = 1.0f / ray.dy;
@@ -290,8 +292,8 @@ __device__ __forceinline__ void trav_init(TravF& s, TravStack& stk, int root, co
 // one step: visit the node or the leaf list `s.ref`, then set the next ref.  The first n_top
 // NodeC records (the top levels of structure 0, breadth-first) may be staged in shared memory at
 // `top`; the others are read from global memory.
-template <bool kTr = true>
-__device__ __forceinline__ void trav_step(const DevModel& M, TravF& s, TravStack& stk, unsigned long long* status,
+template <bool kTr = true, class Stk = TravStack>
+__device__ __forceinline__ void trav_step(const DevModel& M, TravF& s, Stk& stk, unsigned long long* status,
                                           TranspList<float>* tl = nullptr, const OpacCtx* oc = nullptr,
                                           const float4* top = nullptr, int n_top = 0) {
     const RayF& ray = s.ray;

@@ -73,10 +73,10 @@ class SensitivityFunction:
         _check(L.mfg_sens_setup(sim.h, len(self.params), A.ptr(self.params, C.c_int32), len(self.gauges),
                                 A.ptr(self.gauges, C.c_int32), len(self.pumps), A.ptr(self.pumps, C.c_int32)))
 
-    def forward(self, n, precision=A.PREC_FP32R, seed=0x4D6F6C66):
+    def forward(self, n, precision=A.PREC_FP32R, seed=0x4D6F6C66, block_size=0, blocks_per_sm=0):
         out = np.zeros(N_OUT)
         st = A.RunStats()
-        o = A.RunOptions(precision=precision, seed=seed)
+        o = A.RunOptions(precision=precision, seed=seed, block_size=block_size, blocks_per_sm=blocks_per_sm)
         _check(load_library().mfg_sens_forward(self.sim.h, int(n), C.byref(o), A.ptr(out, C.c_double), C.byref(st)))
         self.last_stats = {f: getattr(st, f) for f, _ in A.RunStats._fields_}
         return out

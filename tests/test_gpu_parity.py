@@ -254,8 +254,8 @@ def test_autotune_and_occupancy_variants_agree(tube):
     identical FP32R tallies for the same particles."""
     sim = GpuSimulation(tube)
     ref = None
-    shapes = [(256, b, -1) for b in (2, 3, 4, 6, 8)] + [(512, 4, -1), (1024, 2, -1), (256, 8, 5), (256, 6, 9),
-                                                       (512, 4, 7), (1024, 2, 12)]
+    shapes = [(256, b, -1) for b in (2, 3, 4, 6, 8)] + [(512, 4, -1), (1024, 2, -1), (256, 8, 5), (256, 8, 9),
+                                                       (1024, 2, 7), (1024, 2, 12)]
     for block, bps, lv in shapes:
         sim.ResetSimulation()
         sim.set_particle_offset(0)

@@ -92,12 +92,20 @@ def test_outgassing_gradient_is_the_conditional_mean(setup):
 
 
 def test_gradient_cost_over_forward(setup):
+    """Kernel time of the forward run with gradients against the plain forward run on the same
+    particles, both at the register budget of 2 resident blocks of 256 threads per SM."""
     m, sim, sf = setup
     n = 4_000_000
-    sim.SimulationMCStep(n, precision=A.PREC_FP32R, seed=SEED)
-    t_fwd = sim.last_stats["kernel_ms"]
-    sf.forward(n, seed=SEED)
-    t_sens = sf.last_stats["kernel_ms"]
+    t_fwd, t_sens = [], []
+    for _ in range(3):
+        sim.ResetSimulation()
+        sim.set_particle_offset(0)
+        sim.SimulationMCStep(n, precision=A.PREC_FP32R, seed=SEED, block_size=256, blocks_per_sm=2)
+        t_fwd.append(sim.last_stats["kernel_ms"])
+        sim.set_particle_offset(0)
+        sf.forward(n, seed=SEED, block_size=256, blocks_per_sm=2)
+        t_sens.append(sf.last_stats["kernel_ms"])
+    t_fwd, t_sens = min(t_fwd), min(t_sens)
     print("sensitivity / forward kernel time: %.3f" % (t_sens / t_fwd))
     assert t_sens / t_fwd < 1.3   # the target cost of the gradients: at most 1.3 forward runs
 
