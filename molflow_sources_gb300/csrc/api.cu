@@ -653,7 +653,7 @@ int mfg_wait(mfg_sim* s, int64_t timeout_ms, mfg_run_stats* stats) {
     st.kernel_launches = s->launches;
     unsigned long long status = g[TG_STATUS];
     st.status = MFG_OK;
-    if (status & (KS_STACK | KS_TRANSP)) st.status = MFG_ERR_LIMIT;
+    if (status & KS_STACK) st.status = MFG_ERR_LIMIT;
     if (status & KS_TIMEOUT) st.status = MFG_ERR_TIMEOUT;
     if (status & KS_ABORTED) st.status = MFG_ERR_ABORTED;
     if (status) {
@@ -662,7 +662,6 @@ int mfg_wait(mfg_sim* s, int64_t timeout_ms, mfg_run_stats* stats) {
         CK(cudaStreamSynchronize(s->stream));
         g_err = st.status == MFG_ERR_TIMEOUT ? "kernel time limit reached; particles in flight were dropped"
               : st.status == MFG_ERR_ABORTED ? "run aborted"
-              : (status & KS_TRANSP) ? "a ray crossed more transparent facets than the pass list holds (32)"
               : "BVH traversal stack overflow";
     }
     if (stats) *stats = st;

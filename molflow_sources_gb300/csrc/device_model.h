@@ -7,7 +7,6 @@
 #pragma once
 #include <stdint.h>
 
-#define MFG_MAX_TRANSPARENT 0   // transparent passes are not traced on the GPU yet
 #define MFG_MAXWELL_N 100
 
 // BVH nodes are stored breadth-first, so the two children of an internal node
@@ -158,7 +157,6 @@ struct __align__(16) FacetInfo2 {
 #define KS_ABORTED 2ull
 #define KS_NO_SOURCE 4ull
 #define KS_STACK 8ull
-#define KS_TRANSP 16ull   // more transparent passes on one ray than the pass list holds
 
 // Angle-map desorption tables of one source facet (built from its recorded incident-angle map,
 // MolflowSimFacet.cpp:90-215): `lo` theta lines below the limit, `hi` above, `w` phi bins; the

@@ -225,6 +225,8 @@ struct BuildNode {
     int left = -1, right = -1, first = 0, count = 0, axis = 0;
 };
 
+constexpr int kMaxBvhDepth = 48;
+
 // Binned SAH build.  With per-facet weights W (the share of the hits a prior run recorded on each
 // facet, RebuildAccelStructure with ProbSplit, MolflowSimGeom.cpp:155-169) the chance that a ray
 // enters a child is taken as the mean of its surface-area fraction and its share of the node's
@@ -248,7 +250,9 @@ int build_rec(std::vector<BuildNode>& out, std::vector<int>& ids, int begin, int
     int me = int(out.size());
     out.push_back(nd);
     int n = end - begin;
-    if (n <= leaf_max) {
+    // a node at the depth cap becomes a leaf whatever its size, so that the traversal stacks (64
+    // entries, one far child per level) cannot overflow on any model
+    if (n <= leaf_max || depth >= kMaxBvhDepth) {
         out[me].first = begin;
         out[me].count = n;
         return me;

@@ -1018,7 +1018,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_
         TranspList<R>* tlp = nullptr;
         const OpacCtx* ocp = nullptr;
         if constexpr (kExt) {
-            tl.n = 0;
+            tl.clear((R)0);
             oc.k0 = rng.k0 ^ (rng.inst * 0x9E3779B9u);
             oc.k1 = rng.k1 ^ 0xA5A5A5A5u;
             oc.p0 = rng.p0;
@@ -1058,9 +1058,11 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_
                 h = tv.h;
                 amb = tv.amb;
             }
-            if (amb || h.f < 0) {
+            bool retrace = amb || h.f < 0;
+            if constexpr (kExt) retrace = retrace || tl.over;   // more passes than the list: all rounds in FP64
+            if (retrace) {
                 ++c_rechk;
-                if constexpr (kExt) tl.n = 0;
+                if constexpr (kExt) tl.clear((R)0);
                 HitD hd = trace_d<R, kExt>(M, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last, T.global + TG_STATUS, tlp,
                                           ocp);
                 hf = hd.f; ht = hd.t; hu = (R)hd.u; hv = (R)hd.v;
@@ -1107,13 +1109,22 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_
                 const double ds = P.scat_at - P.dist;
                 if (ds < travel) { travel = ds; event = 3; }
             }
-            for (int k = 0; k < tl.n; ++k) {
-                if (!((double)tl.t[k] < travel)) continue;
-                double ort_t = transparent_pass<kFP32>(M, T, B, tl.f[k], tl.t[k], tl.u[k], tl.v[k], P.time, vel, dx, dy, dz);
-                if (kSens) {
-                    const int g = ((scode(tl.f[k]) >> 20) & 15) - 1;
-                    if (g >= 0) sens_output(C.sens, traj, ntraj, src_idx, g, 2.0 * ort_t);
+            while (true) {
+                for (int k = 0; k < tl.n; ++k) {
+                    if (!((double)tl.t[k] < travel)) continue;
+                    double ort_t = transparent_pass<kFP32>(M, T, B, tl.f[k], tl.t[k], tl.u[k], tl.v[k], P.time, vel, dx, dy, dz);
+                    if (kSens) {
+                        const int g = ((scode(tl.f[k]) >> 20) & 15) - 1;
+                        if (g >= 0) sens_output(C.sens, traj, ntraj, src_idx, g, 2.0 * ort_t);
+                    }
                 }
+                if (!tl.over) break;
+                // the ray crosses more transparent facets than the list holds: trace it again (FP64,
+                // the same hard hit) for the passes beyond the farthest one taken
+                const R cut = tl.farthest();
+                if (!((double)cut < travel)) break;
+                tl.clear(cut);
+                trace_d<R, kExt>(M, root, P.ox, P.oy, P.oz, ddx, ddy, ddz, P.last, T.global + TG_STATUS, tlp, ocp);
             }
         }
         P.ox = P.ox + travel * ddx;

@@ -45,12 +45,23 @@ __device__ __noinline__ double param_at(const DevModel& M, int p, double t) {
 
 // ---------------------------------------------------------- opacity ----
 #define MFG_MAX_TRANSP 32
-// Transparent passes found during one trace (candidates of RegisterTransparentPass)
+// Transparent passes found during one trace (candidates of RegisterTransparentPass): the nearest
+// MFG_MAX_TRANSP of those beyond distance `tlo`.  When a ray crosses more, `over` is set and the
+// tracer traces the same ray again for the passes beyond the farthest one kept (the hard hit is
+// the same every time), so no pass is lost whatever the number of transparent facets.
 template <class T>
 struct TranspList {
-    int n;
+    int n, over;
+    T tlo;
     int f[MFG_MAX_TRANSP];
     T t[MFG_MAX_TRANSP], u[MFG_MAX_TRANSP], v[MFG_MAX_TRANSP];
+    __device__ __forceinline__ void clear(T from) { n = 0; over = 0; tlo = from; }
+    // distance of the farthest pass kept
+    __device__ __forceinline__ T farthest() const {
+        T m = tlo;
+        for (int k = 0; k < n; ++k) m = t[k] > m ? t[k] : m;
+        return m;
+    }
 };
 // A partial-opacity decision is an order-independent draw per (particle, trace step, facet)
 // from a Philox stream keyed apart from the particle's own stream.
@@ -81,13 +92,20 @@ __device__ __forceinline__ OpacCtx replay_opacity() {
 template <class T>
 __device__ __forceinline__ void add_transp(TranspList<T>* tl, int f, double t, double u, double v,
                                            unsigned long long* status) {
+    (void)status;
     if (!tl) return;
-    if (tl->n < MFG_MAX_TRANSP) {
-        tl->f[tl->n] = f; tl->t[tl->n] = (T)t; tl->u[tl->n] = (T)u; tl->v[tl->n] = (T)v;
-        ++tl->n;
+    const T tt = (T)t;
+    if (!(tt > tl->tlo)) return;   // taken in an earlier round
+    int k = tl->n;
+    if (k == MFG_MAX_TRANSP) {     // full: replace the farthest if this one is nearer
+        tl->over = 1;
+        k = 0;
+        for (int j = 1; j < MFG_MAX_TRANSP; ++j) k = tl->t[j] > tl->t[k] ? j : k;
+        if (!(tt < tl->t[k])) return;
     } else {
-        atomicOr(status, KS_TRANSP);
+        ++tl->n;
     }
+    tl->f[k] = f; tl->t[k] = tt; tl->u[k] = (T)u; tl->v[k] = (T)v;
 }
 
 // -------------------------------------------------- point in polygon ----

@@ -206,3 +206,30 @@ def transparent_tube(transient=False, n_disk=48):
         m.set_moments(np.logspace(-5, -1, 40), 1e-5)
         m.outgassing_param[0] = m.add_param([0.0, 1e-3, 1e-3 * (1 + 1e-9), 10.0], [10.0, 10.0, 0.0, 0.0])
     return m
+
+
+def stacked_disk_tube(n_disks=48, opacity=0.0, n_disk=48, L=10.0):
+    """Config-1 tube (L/R = 10) crossed by `n_disks` two-sided disks spaced evenly along it, all of
+    the given opacity (0: fully transparent): a ray along the tube crosses more transparent facets
+    than one pass list holds."""
+    base = config1_tube(texture_facet=None)
+    V = [base.vertices]
+    facets = [list(f) for f in base.facets]
+    r = 1.0 * math.cos(math.pi / 64) * 0.999
+    ang = np.arange(n_disk) / n_disk * 2 * math.pi
+    nv = len(base.vertices)
+    disks = []
+    for z in (np.arange(n_disks) + 0.5) * (L / n_disks):
+        V.append(np.stack([r * np.cos(ang), r * np.sin(ang), np.full(n_disk, z)], axis=1))
+        disks.append(len(facets))
+        facets.append(list(range(nv, nv + n_disk)))
+        nv += n_disk
+    m = Model(np.concatenate(V), facets)
+    for k in FACET_FIELDS:
+        getattr(m, k)[:base.n_facets] = getattr(base, k)
+    for d in disks:
+        m.is_2sided[d] = 1
+        m.sticking[d] = 0.0
+        m.opacity[d] = opacity
+    m.disks = np.array(disks)
+    return m

@@ -1051,9 +1051,22 @@ int orc_facet_geometry(const orc_model* M, double* o18, double* area) {
 typedef struct { int facet; double t, u, v; } ohit;
 typedef struct {
     int hard; double t, u, v;
-    int ntr; ohit tr[MAX_TRANSP];
+    int ntr; ohit* tr;   /* transparent passes: every one the ray crosses (a per-thread buffer that grows) */
     uint64_t nodes, prims;
 } oisect;
+static _Thread_local ohit* g_tr_buf = NULL;
+static _Thread_local int g_tr_cap = 0;
+static void add_pass(oisect* H, int fi, double t, double u, double v) {
+    if (H->ntr == g_tr_cap) {
+        int cap = g_tr_cap ? 2 * g_tr_cap : MAX_TRANSP;
+        ohit* nb = (ohit*)realloc(g_tr_buf, (size_t)cap * sizeof(ohit));
+        if (!nb) return;   /* out of memory: the pass is dropped */
+        g_tr_buf = nb;
+        g_tr_cap = cap;
+    }
+    H->tr = g_tr_buf;
+    H->tr[H->ntr].facet = fi; H->tr[H->ntr].t = t; H->tr[H->ntr].u = u; H->tr[H->ntr].v = v; H->ntr++;
+}
 
 static double param_at(const orc_model* M, int p, double t) {
     const oparam* P = &M->params[p];
@@ -1095,7 +1108,7 @@ static inline int box_hit(const onode* n, const double* o, const double* inv, do
 
 static void intersect(const orc_model* M, int s, const double* o, const double* d, int last, double time,
                       rng_t* r, uint64_t step, oisect* H) {
-    H->hard = -1; H->t = 1e99; H->ntr = 0;
+    H->hard = -1; H->t = 1e99; H->ntr = 0; H->tr = g_tr_buf;
     if (M->nnodes[s] == 0) return;
     double inv[3] = {1.0 / d[0], 1.0 / d[1], 1.0 / d[2]};
     const onode* nodes = M->nodes[s];
@@ -1118,8 +1131,8 @@ static void intersect(const orc_model* M, int s, const double* o, const double* 
                 int hard = (op >= 1.0) ? 1 : (op <= 0.0 ? 0 : (rnd_opacity(r, step, fi) < op));
                 if (hard) {
                     if (t < H->t || (t == H->t && fi < H->hard)) { H->t = t; H->hard = fi; H->u = u; H->v = v; }
-                } else if (H->ntr < MAX_TRANSP) {
-                    H->tr[H->ntr].facet = fi; H->tr[H->ntr].t = t; H->tr[H->ntr].u = u; H->tr[H->ntr].v = v; H->ntr++;
+                } else {
+                    add_pass(H, fi, t, u, v);
                 }
             }
         } else {
