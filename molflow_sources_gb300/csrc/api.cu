@@ -202,8 +202,9 @@ static int sim_upload(mfg_sim* s) {
     int rc;
 #define UP(vec, field) if ((rc = upload(s->owned, vec, &M.field)) != MFG_OK) return rc
     UP(h.nodes_d, nodes_d);
-    UP(h.nodes_q, nodes_q);
-    UP(h.roots_q, roots_q);
+    UP(h.nodes_c, nodes_c);
+    UP(h.prims_c, prims_c);
+    UP(h.roots_c, roots_c);
     UP(h.roots, roots);
     UP(h.prims, prims);
     UP(h.isect_d, isect_d);
@@ -510,8 +511,8 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     const size_t fac_bytes = size_t(h.nf) * SF_N * 8;
     C.smem_facets = fac_bytes <= std::min<size_t>(96 * 1024, 200 * 1024 / size_t(bps_req)) ? 1 : 0;
     C.n_top = o.precision == MFG_PREC_FP32R && o.smem_bvh_levels > 0 && !sens
-                  ? int(std::min<size_t>(size_t(1) << o.smem_bvh_levels, h.nodes_q.size())) : 0;
-    size_t dyn = (TG_N + (C.smem_facets ? size_t(h.nf) * SF_N : 0)) * 8 + size_t(C.n_top) * sizeof(NodeQ) +
+                  ? int(std::min<size_t>(size_t(1) << o.smem_bvh_levels, h.nodes_c.size())) : 0;
+    size_t dyn = (TG_N + (C.smem_facets ? size_t(h.nf) * SF_N : 0)) * 8 + size_t(C.n_top) * sizeof(NodeC) +
                  (sens && C.sens.smem_code ? size_t(h.nf) * 4 : 0);
     // kernel variant: FP64 compiled for at least 2, 3 or 4 resident blocks per SM (register budgets
     // 128, 80, 64), FP32R for 2, 3, 4, 6 or 8 (128, 80, 64, 40, 32); blocks_per_sm selects the
@@ -1203,7 +1204,7 @@ __global__ void noalloc_pass1(const __grid_constant__ DevModel M, int precision,
         return;
     }
     bool amb = false;
-    mfgk::HitF h = mfgk::trace_f(M, M.roots_q[0], mfgk::make_ray_f(ox, oy, oz, (float)dx, (float)dy, (float)dz), last[i], amb,
+    mfgk::HitF h = mfgk::trace_f(M, M.roots_c[0], mfgk::make_ray_f(ox, oy, oz, (float)dx, (float)dy, (float)dz), last[i], amb,
                                  scratch + 1, nullptr, ocp);
     if (amb || h.f < 0) {   // queue the ray for the FP64 pass
         unsigned long long k = atomicAdd(scratch, 1ull);

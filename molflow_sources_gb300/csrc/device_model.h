@@ -19,30 +19,17 @@ struct __align__(16) NodeD {
     int32_t a, b;
     int32_t pad0, pad1;
 };
-// FP32 traversal node (32 B, two 16-byte loads) holding its two children's boxes, each padded by
-// a scene-relative margin and then quantized outward to 8 bits in the node's own frame: origin o
-// (the lower corner of the two boxes' union) and per axis a power-of-two step 2^(e-127) such that
-// 255 steps cover the union.  A decoded box o + q * step contains the padded box, so a ray that
-// meets a subtree's facets meets its box.  One fetch decides which children to visit, and a missed
-// child costs no fetch.
-//   meta: bytes 0-2 the exponents e of x, y, z; byte 3 flags: bit 0 child 0 is a leaf slot, bit 1
-//         child 1 is a leaf slot, bit 2 child 1 is empty
-//   q:    child 0 lo x y z, hi x y z, child 1 lo x y z, hi x y z
-//   base: the children occupy slots base and base + 1 of the node array
-// Child reference in the traversal: >= 0 a node slot, < 0 the leaf slot -1 - ref.  Every structure
-// starts at a root node whose child 0 is the whole tree and child 1 is empty.
-struct __align__(16) NodeQ {
-    float ox, oy, oz;
-    uint32_t meta;
-    uint8_t q[12];
-    int32_t base;
+// FP32 traversal node holding its two children's boxes, rounded outward and padded by a
+// scene-relative margin (64 B, four 16-byte loads), so one fetch decides which children to visit
+// and a missed child costs no fetch.  Child reference: >= 0 another NodeC, < 0 a leaf whose
+// facets are prims_c[-1 - ref ...] up to a -1 sentinel.  Every structure starts at a root NodeC
+// whose child 0 is the whole tree and child 1 an empty leaf far away.
+struct __align__(16) NodeC {
+    float lo0[3], hi0[3];
+    float lo1[3], hi1[3];
+    int32_t c0, c1;
+    int32_t pad0, pad1;
 };
-#define NQ_LEAF0 1u
-#define NQ_LEAF1 2u
-#define NQ_EMPTY1 4u
-// Leaf slot (32 B, same array): up to 7 facet ids followed by -1; f[7] <= -2 continues the list
-// in slot -2 - f[7]
-struct __align__(16) LeafQ { int32_t f[8]; };
 
 // Facet intersection record FP64 (128 B):
 //  [0..2] N, [3] D = N.O, [4..6] O, [7] flags as integer bits (bit 0 two-sided, bits 1-2 opacity
@@ -190,8 +177,9 @@ struct DevModel {
     int32_t nf, nstruct;
     int32_t n_src, nm;
     const NodeD* nodes_d;
-    const NodeQ* nodes_q;          // FP32 quantized two-child nodes and leaf slots (trace_f)
-    const int32_t* roots_q;        // root node slot per structure
+    const NodeC* nodes_c;          // FP32 two-child nodes (trace_f)
+    const int32_t* prims_c;        // leaf facet lists of nodes_c, each ended by -1
+    const int32_t* roots_c;        // root NodeC per structure
     const int32_t* roots;        // root node per structure
     const int32_t* prims;        // facet ids in leaf order
     const FacetIsectD* isect_d;

@@ -337,39 +337,6 @@ float round_up(double x) {
     return (double(f) < x) ? std::nextafter(f, FLT_MAX) : f;
 }
 
-// Quantize two child boxes (floats, already padded and rounded outward) into a NodeQ: the frame
-// origin is the lower corner of their union, the step per axis the smallest power of two 2^e with
-// 255 steps covering the union's extent; lower bounds round down and upper bounds up to whole
-// steps, all in exact double arithmetic, so each decoded box o + q * 2^e contains its child's box.
-NodeQ quantize_node(const float* lo0, const float* hi0, const float* lo1, const float* hi1, uint32_t flags, int base) {
-    NodeQ q{};
-    float o[3];
-    uint32_t meta = flags << 24;
-    double step[3];
-    for (int a = 0; a < 3; ++a) {
-        const float lo = std::min(lo0[a], lo1[a]), hi = std::max(hi0[a], hi1[a]);
-        o[a] = lo;
-        const double ext = double(hi) - double(lo);
-        int e = -126;
-        while (e < 127 && std::ldexp(255.0, e) < ext) ++e;
-        step[a] = std::ldexp(1.0, e);
-        meta |= uint32_t(e + 127) << (8 * a);
-    }
-    q.ox = o[0]; q.oy = o[1]; q.oz = o[2];
-    q.meta = meta;
-    const float* bl[2] = {lo0, lo1};
-    const float* bh[2] = {hi0, hi1};
-    for (int c = 0; c < 2; ++c)
-        for (int a = 0; a < 3; ++a) {
-            const double ql = std::floor((double(bl[c][a]) - double(o[a])) / step[a]);
-            const double qh = std::ceil((double(bh[c][a]) - double(o[a])) / step[a]);
-            q.q[6 * c + a] = uint8_t(std::min(255.0, std::max(0.0, ql)));
-            q.q[6 * c + 3 + a] = uint8_t(std::min(255.0, std::max(0.0, qh)));
-        }
-    q.base = base;
-    return q;
-}
-
 }  // namespace
 
 int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, int leaf_max) {
@@ -807,9 +774,9 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     m.roots.clear();
     m.prims.clear();
     m.nodes_d.clear();
-    m.nodes_q.clear();
-    m.slot_kind.clear();
-    m.roots_q.clear();
+    m.nodes_c.clear();
+    m.roots_c.clear();
+    m.prims_c.clear();
     m.bvh_depth = 0;
     m.bvh_leaves = 0;
     const double pad64 = 1e-9 * m.scene_scale, pad32 = 2e-6 * m.scene_scale;
@@ -818,24 +785,22 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
         for (int i = 0; i < nf; ++i)
             if (m.structure[i] == -1 || m.structure[i] == s) ids.push_back(i);
         m.roots.push_back(int32_t(m.nodes_d.size()));
+        // root NodeC of the structure: child 0 = the whole tree (filled below), child 1 = an
+        // empty leaf whose box is a point far outside any scene
+        m.roots_c.push_back(int32_t(m.nodes_c.size()));
+        {
+            NodeC r{};
+            for (int a = 0; a < 3; ++a) { r.lo0[a] = r.hi0[a] = r.lo1[a] = r.hi1[a] = 1e30f; }
+            r.c0 = r.c1 = -1 - int32_t(m.prims_c.size());
+            m.prims_c.push_back(-1);
+            m.nodes_c.push_back(r);
+        }
         if (ids.empty()) {   // empty structure: one leaf with no facets and an empty box
             NodeD e{};
             for (int a = 0; a < 3; ++a) { e.lo[a] = 1; e.hi[a] = -1; }
             e.a = int32_t(m.prims.size());
             e.b = -1;
             m.nodes_d.push_back(e);
-            // FP32: a root node whose child 0 is an empty leaf slot and child 1 empty
-            const int slot = int(m.nodes_q.size());
-            m.roots_q.push_back(slot);
-            m.nodes_q.resize(size_t(slot) + 3);
-            m.slot_kind.resize(size_t(slot) + 3, 1);
-            LeafQ E;
-            for (int k = 0; k < 8; ++k) E.f[k] = -1;
-            std::memcpy(&m.nodes_q[slot + 1], &E, sizeof E);
-            std::memcpy(&m.nodes_q[slot + 2], &E, sizeof E);
-            const float z[3] = {0, 0, 0};
-            m.nodes_q[slot] = quantize_node(z, z, z, z, NQ_LEAF0 | NQ_EMPTY1, slot + 1);
-            m.slot_kind[slot] = 0;
             continue;
         }
         std::vector<BuildNode> tree;
@@ -876,64 +841,43 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
             m.nodes_d.push_back(nd);
         }
         for (int i : ids) m.prims.push_back(i);
-        // quantized two-child FP32 layout: breadth-first, the two children of a node in consecutive
-        // slots, leaves as slots of facet ids
+        // two-child FP32 layout, breadth-first over the internal nodes
         {
-            const int croot = int(m.nodes_q.size());
-            m.roots_q.push_back(croot);
-            auto alloc = [&](int n, uint8_t kind) {
-                const int at = int(m.nodes_q.size());
-                m.nodes_q.resize(size_t(at) + size_t(n));
-                m.slot_kind.resize(size_t(at) + size_t(n), kind);
-                return at;
-            };
+            const int croot = m.roots_c.back();
             auto box32 = [&](const BuildNode& b, float* lo, float* hi) {
                 for (int a = 0; a < 3; ++a) { lo[a] = round_down(b.lo[a] - pad32); hi[a] = round_up(b.hi[a] + pad32); }
             };
-            auto write_leaf = [&](int slot, const BuildNode& b) {
-                LeafQ L;
-                for (int k = 0; k < 8; ++k) L.f[k] = -1;
-                int cur = slot, k = 0;
-                for (int i = 0; i < b.count; ++i) {
-                    if (k == 7) {   // continue in a further slot
-                        const int nxt = alloc(1, 1);
-                        L.f[7] = -2 - nxt;
-                        std::memcpy(&m.nodes_q[cur], &L, sizeof L);
-                        m.slot_kind[cur] = 1;
-                        for (int j = 0; j < 8; ++j) L.f[j] = -1;
-                        cur = nxt;
-                        k = 0;
-                    }
-                    L.f[k++] = ids[b.first + i];
+            auto leaf_ref = [&](const BuildNode& b) {
+                const int32_t ref = -1 - int32_t(m.prims_c.size());
+                for (int k = 0; k < b.count; ++k) m.prims_c.push_back(ids[b.first + k]);
+                m.prims_c.push_back(-1);
+                return ref;
+            };
+            std::vector<int> inner;                 // tree indices of internal nodes, BFS order
+            std::vector<int32_t> cidx(tree.size(), -1);
+            if (tree[0].left >= 0) {
+                inner.push_back(0);
+                for (size_t q = 0; q < inner.size(); ++q) {
+                    const BuildNode& b = tree[inner[q]];
+                    for (int c : {b.left, b.right})
+                        if (tree[c].left >= 0) inner.push_back(c);
                 }
-                std::memcpy(&m.nodes_q[cur], &L, sizeof L);
-                m.slot_kind[cur] = 1;
-            };
-            auto write_node = [&](int slot, const BuildNode& c0, const BuildNode* c1, int base) {
-                float lo0[3], hi0[3], lo1[3], hi1[3];
-                box32(c0, lo0, hi0);
-                if (c1) box32(*c1, lo1, hi1);
-                const uint32_t flags = (c0.left < 0 ? NQ_LEAF0 : 0u) | (c1 ? (c1->left < 0 ? NQ_LEAF1 : 0u) : NQ_EMPTY1);
-                m.nodes_q[slot] = quantize_node(lo0, hi0, c1 ? lo1 : lo0, c1 ? hi1 : hi0, flags, base);
-                m.slot_kind[slot] = 0;
-            };
-            alloc(1, 0);
-            const int top = alloc(2, 2);   // the tree's root, and the root node's empty child
-            write_node(croot, tree[0], nullptr, top);
-            {
-                LeafQ E;
-                for (int k = 0; k < 8; ++k) E.f[k] = -1;
-                std::memcpy(&m.nodes_q[top + 1], &E, sizeof E);
             }
-            std::vector<std::pair<int, int>> queue{{0, top}};   // (tree node, slot)
-            for (size_t q = 0; q < queue.size(); ++q) {
-                const int n = queue[q].first, slot = queue[q].second;
-                const BuildNode b = tree[n];
-                if (b.left < 0) { write_leaf(slot, b); continue; }
-                const int cb = alloc(2, 2);
-                write_node(slot, tree[b.left], &tree[b.right], cb);
-                queue.push_back({b.left, cb});
-                queue.push_back({b.right, cb + 1});
+            const int32_t cbase = int32_t(m.nodes_c.size());
+            for (size_t q = 0; q < inner.size(); ++q) cidx[inner[q]] = cbase + int32_t(q);
+            {
+                NodeC& r = m.nodes_c[croot];
+                box32(tree[0], r.lo0, r.hi0);
+                r.c0 = tree[0].left >= 0 ? cidx[0] : leaf_ref(tree[0]);
+            }
+            for (size_t q = 0; q < inner.size(); ++q) {
+                const BuildNode& b = tree[inner[q]];
+                NodeC nc{};
+                box32(tree[b.left], nc.lo0, nc.hi0);
+                box32(tree[b.right], nc.lo1, nc.hi1);
+                nc.c0 = tree[b.left].left >= 0 ? cidx[b.left] : leaf_ref(tree[b.left]);
+                nc.c1 = tree[b.right].left >= 0 ? cidx[b.right] : leaf_ref(tree[b.right]);
+                m.nodes_c.push_back(nc);
             }
         }
     }
@@ -1178,24 +1122,14 @@ int merge_host_models(const std::vector<const HostModel*>& parts, HostModel& out
             out.nodes_d.push_back(nd);
         }
         for (int r : p.roots) out.roots.push_back(r + node_base);
-        const int32_t sbase = int32_t(out.nodes_q.size());
-        for (size_t k = 0; k < p.nodes_q.size(); ++k) {
-            NodeQ nq = p.nodes_q[k];
-            if (p.slot_kind[k] == 0) {
-                nq.base += sbase;
-            } else if (p.slot_kind[k] == 1) {
-                LeafQ L;
-                std::memcpy(&L, &nq, sizeof L);
-                for (int j = 0; j < 8; ++j) {
-                    if (L.f[j] >= 0) L.f[j] += in.facet_base;
-                    else if (L.f[j] <= -2) L.f[j] = -2 - (-2 - L.f[j] + sbase);
-                }
-                std::memcpy(&nq, &L, sizeof L);
-            }
-            out.nodes_q.push_back(nq);
-            out.slot_kind.push_back(p.slot_kind[k]);
+        const int32_t cbase = int32_t(out.nodes_c.size()), pcbase = int32_t(out.prims_c.size());
+        for (NodeC nc : p.nodes_c) {
+            nc.c0 = nc.c0 >= 0 ? nc.c0 + cbase : nc.c0 - pcbase;
+            nc.c1 = nc.c1 >= 0 ? nc.c1 + cbase : nc.c1 - pcbase;
+            out.nodes_c.push_back(nc);
         }
-        for (int r : p.roots_q) out.roots_q.push_back(r + sbase);
+        for (int r : p.roots_c) out.roots_c.push_back(r + cbase);
+        for (int f : p.prims_c) out.prims_c.push_back(f >= 0 ? f + in.facet_base : -1);
         for (int f : p.prims) out.prims.push_back(f + in.facet_base);
         out.isect_d.insert(out.isect_d.end(), p.isect_d.begin(), p.isect_d.end());
         out.isect_f.insert(out.isect_f.end(), p.isect_f.begin(), p.isect_f.end());

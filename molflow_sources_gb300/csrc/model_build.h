@@ -73,9 +73,8 @@ struct HostModel {
     std::vector<double> tex_inc;          // 1/(cell area * sides) per texture cell
     // BVH (all structures concatenated, breadth-first per structure)
     std::vector<NodeD> nodes_d;
-    std::vector<NodeQ> nodes_q;           // FP32 quantized two-child nodes and leaf slots
-    std::vector<uint8_t> slot_kind;       // per slot of nodes_q: 0 node, 1 leaf slot, 2 unused
-    std::vector<int32_t> roots_q;
+    std::vector<NodeC> nodes_c;           // FP32 two-child layout
+    std::vector<int32_t> roots_c, prims_c;
     std::vector<int32_t> roots, prims;
     int64_t bvh_depth = 0, bvh_leaves = 0;
     // device records

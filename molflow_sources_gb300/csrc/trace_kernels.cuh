@@ -737,13 +737,13 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_
     B.sfac = C.smem_facets ? smem + TG_N : nullptr;
     const int nsm = TG_N + (C.smem_facets ? M.nf * SF_N : 0);
     for (int i = threadIdx.x; i < nsm; i += blockDim.x) smem[i] = 0ull;
-    // top levels of the FP32 BVH (breadth-first node slots [0, n_top), 32 B each), after the partials
-    uint4* s_top = reinterpret_cast<uint4*>(smem + nsm);
+    // top levels of the FP32 BVH (breadth-first NodeC records [0, n_top)), after the partials
+    float4* s_top = reinterpret_cast<float4*>(smem + nsm);
     const int n_top = (kFP32 && kTop) ? C.n_top : 0;
-    for (int i = threadIdx.x; i < 2 * n_top; i += blockDim.x)
-        s_top[i] = __ldg(reinterpret_cast<const uint4*>(M.nodes_q) + i);
+    for (int i = threadIdx.x; i < 4 * n_top; i += blockDim.x)
+        s_top[i] = __ldg(reinterpret_cast<const float4*>(M.nodes_c) + i);
     // the sensitivity variants (no staged nodes) stage their packed per-facet words after the partials
-    int* s_ring = reinterpret_cast<int*>(s_top + 2 * n_top);
+    int* s_ring = reinterpret_cast<int*>(s_top + 4 * n_top);
     const int* scodes = nullptr;
     if constexpr (kSens) {
         if (C.sens.smem_code) {
@@ -1039,7 +1039,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_
                 // beam chamber, +41 % on the tube.  Idle lanes take part in the votes.
                 TravF tv;
                 TravStack stk;
-                if (active) trav_init(tv, stk, M.roots_q[P.structure], make_ray_f(P.ox, P.oy, P.oz, (float)dx, (float)dy, (float)dz), P.last);
+                if (active) trav_init(tv, stk, M.roots_c[P.structure], make_ray_f(P.ox, P.oy, P.oz, (float)dx, (float)dy, (float)dz), P.last);
                 else tv.ref = kTrDone;
                 // Node and leaf steps run in separate rounds: a lane that reaches a leaf list waits
                 // until the lanes at leaves outnumber those at nodes three to one, then the leaf
@@ -1465,7 +1465,7 @@ __global__ void replay_kernel(const __grid_constant__ DevModel M, int precision,
         hit_t[i] = h.f >= 0 ? h.t : -1.0;
     } else {
         bool amb = false;
-        HitF h = trace_f(M, M.roots_q[0], make_ray_f(ox, oy, oz, (float)dx, (float)dy, (float)dz), last[i], amb, status,
+        HitF h = trace_f(M, M.roots_c[0], make_ray_f(ox, oy, oz, (float)dx, (float)dy, (float)dz), last[i], amb, status,
                          nullptr, ocp);
         if (amb || h.f < 0) {
             atomicAdd(rechecks, 1ull);

@@ -277,8 +277,8 @@ __device__ __forceinline__ RayF make_ray_f(double ox, double oy, double oz, floa
 
 // FacetIsectF layout: [N0 N1 N2 Olo0 | Ohi0 Ohi1 Ohi2 Olo1 | Us0 Us1 Us2 Olo2 | Vs0 Vs1 Vs2 flags]
 
-// Resumable FP32 traversal of one ray: the ref to visit next (a node slot >= 0, a leaf slot
-// -1 - slot < 0, or kTrDone) and the best hit so far with its error bound; the stack is kept
+// Resumable FP32 traversal of one ray: the ref to visit next (a NodeC index >= 0, a leaf list
+// -1-first < 0, or kTrDone) and the best hit so far with its error bound; the stack is kept
 // apart, so that the scalar state can stay in registers.  A warp can step its lanes' traversals
 // together and stop them at any step.
 constexpr int kTrDone = -0x7fffffff - 1;
@@ -297,7 +297,7 @@ __device__ __forceinline__ void trav_init(TravF& s, Stk& stk, int root, const Ra
     s.ix = 1.0f / ray.dx;
     s.iy = 1.0f / ray.dy;
     s.iz = 1.0f / ray.dz;
-    s.ref = root;   // the structure's root node slot
+    s.ref = root;   // the structure's root NodeC
     s.last = last;
     s.h.f = -1;
     s.h.t = 3.0e38f;
@@ -307,18 +307,13 @@ __device__ __forceinline__ void trav_init(TravF& s, Stk& stk, int root, const Ra
     stk.sp = 0;
 }
 
-// byte k of a quantized-box word, as a float
-__device__ __forceinline__ float qbyte(uint32_t w, int k) { return (float)((w >> (8 * k)) & 0xffu); }
-// entry k (0..3) of an int4
-__device__ __forceinline__ int sel4(const int4& v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); }
-
-// one step: visit the node or the leaf slot `s.ref`, then set the next ref.  The first n_top node
-// slots (the top levels of structure 0, breadth-first) may be staged in shared memory at `top`; the
-// others are read from global memory.
+// one step: visit the node or the leaf list `s.ref`, then set the next ref.  The first n_top
+// NodeC records (the top levels of structure 0, breadth-first) may be staged in shared memory at
+// `top`; the others are read from global memory.
 template <bool kTr = true, class Stk = TravStack>
 __device__ __forceinline__ void trav_step(const DevModel& M, TravF& s, Stk& stk, unsigned long long* status,
                                           TranspList<float>* tl = nullptr, const OpacCtx* oc = nullptr,
-                                          const uint4* top = nullptr, int n_top = 0) {
+                                          const float4* top = nullptr, int n_top = 0) {
     const RayF& ray = s.ray;
     const float dx = ray.dx, dy = ray.dy, dz = ray.dz;
     const float ox = ray.ohx, oy = ray.ohy, oz = ray.ohz;
@@ -329,38 +324,28 @@ __device__ __forceinline__ void trav_step(const DevModel& M, TravF& s, Stk& stk,
     int ref = s.ref;
     bool ambiguous = false;
     if (ref >= 0) {
-        // both children's boxes in one 32-byte node, 8-bit offsets in the node's frame:
-        // t = (o + q * step - ray origin) / d = q * (step / d) + (o - ray origin) / d
-        uint4 a, b;
+        // both children's boxes in one 64-byte node
+        float4 q0, q1, q2, q3;
         if (ref < n_top) {
-            const uint4* tp = top + 2 * ref;
-            a = tp[0];
-            b = tp[1];
+            const float4* tp = top + 4 * ref;
+            q0 = tp[0]; q1 = tp[1]; q2 = tp[2]; q3 = tp[3];
         } else {
-            const uint4* np = reinterpret_cast<const uint4*>(M.nodes_q + ref);
-            a = __ldg(np);
-            b = __ldg(np + 1);
+            const float4* np = reinterpret_cast<const float4*>(M.nodes_c + ref);
+            q0 = __ldg(np); q1 = __ldg(np + 1); q2 = __ldg(np + 2); q3 = __ldg(np + 3);
         }
-        const uint32_t meta = a.w;
-        const float Ax = (__uint_as_float(a.x) - ox) * ix, Bx = __uint_as_float((meta & 0xffu) << 23) * ix;
-        const float Ay = (__uint_as_float(a.y) - oy) * iy, By = __uint_as_float(((meta >> 8) & 0xffu) << 23) * iy;
-        const float Az = (__uint_as_float(a.z) - oz) * iz, Bz = __uint_as_float(((meta >> 16) & 0xffu) << 23) * iz;
         const float tcap = h.t + 2.0f * htol;
-        float a0 = fmaf(qbyte(b.x, 0), Bx, Ax), a1 = fmaf(qbyte(b.x, 3), Bx, Ax);
-        float b0 = fmaf(qbyte(b.x, 1), By, Ay), b1 = fmaf(qbyte(b.y, 0), By, Ay);
-        float c0 = fmaf(qbyte(b.x, 2), Bz, Az), c1 = fmaf(qbyte(b.y, 1), Bz, Az);
+        float a0 = (q0.x - ox) * ix, a1 = (q0.w - ox) * ix;
+        float b0 = (q0.y - oy) * iy, b1 = (q1.x - oy) * iy;
+        float c0 = (q0.z - oz) * iz, c1 = (q1.y - oz) * iz;
         const float tmin0 = fmaxf(fmaxf(fminf(a0, a1), fminf(b0, b1)), fmaxf(fminf(c0, c1), 0.0f));
         const float tmax0 = fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fminf(fmaxf(c0, c1), tcap));
-        a0 = fmaf(qbyte(b.y, 2), Bx, Ax); a1 = fmaf(qbyte(b.z, 1), Bx, Ax);
-        b0 = fmaf(qbyte(b.y, 3), By, Ay); b1 = fmaf(qbyte(b.z, 2), By, Ay);
-        c0 = fmaf(qbyte(b.z, 0), Bz, Az); c1 = fmaf(qbyte(b.z, 3), Bz, Az);
+        a0 = (q1.z - ox) * ix; a1 = (q2.y - ox) * ix;
+        b0 = (q1.w - oy) * iy; b1 = (q2.z - oy) * iy;
+        c0 = (q2.x - oz) * iz; c1 = (q2.w - oz) * iz;
         const float tmin1 = fmaxf(fmaxf(fminf(a0, a1), fminf(b0, b1)), fmaxf(fminf(c0, c1), 0.0f));
         const float tmax1 = fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fminf(fmaxf(c0, c1), tcap));
-        const uint32_t fl = meta >> 24;
-        const bool hit0 = tmin0 <= tmax0 * 1.0000005f;
-        const bool hit1 = tmin1 <= tmax1 * 1.0000005f && !(fl & NQ_EMPTY1);
-        const int base = (int)b.w;
-        const int r0 = (fl & NQ_LEAF0) ? -1 - base : base, r1 = (fl & NQ_LEAF1) ? -2 - base : base + 1;
+        const bool hit0 = tmin0 <= tmax0 * 1.0000005f, hit1 = tmin1 <= tmax1 * 1.0000005f;
+        const int r0 = __float_as_int(q3.x), r1 = __float_as_int(q3.y);
         if (hit0 && hit1) {
             // nearer box first
             const bool first0 = tmin0 <= tmin1;
@@ -375,19 +360,8 @@ __device__ __forceinline__ void trav_step(const DevModel& M, TravF& s, Stk& stk,
         s.ref = ref;
         return;
     }
-    // leaf slot: up to 7 facet ids then -1, or in entry 7 the slot where the list continues
-    const int4* lp = reinterpret_cast<const int4*>(M.nodes_q + (-1 - ref));
-    int4 la = __ldg(lp), lb = __ldg(lp + 1);
-    for (int k = 0;; ++k) {
-        if (k == 7) {
-            if (lb.w > -2) break;
-            lp = reinterpret_cast<const int4*>(M.nodes_q + (-2 - lb.w));
-            la = __ldg(lp);
-            lb = __ldg(lp + 1);
-            k = -1;
-            continue;
-        }
-        const int f = k < 4 ? sel4(la, k) : sel4(lb, k - 4);
+    for (int k = -1 - ref;; ++k) {
+        const int f = M.prims_c[k];
         if (f < 0) break;
         if (f == last) continue;
         const FacetIsectF& R = M.isect_f[f];

@@ -18,8 +18,6 @@ static inline double __longlong_as_double(long long i) { double x; std::memcpy(&
 static inline float __uint_as_float(unsigned u) { float x; std::memcpy(&x, &u, sizeof x); return x; }
 static inline unsigned __umulhi(unsigned a, unsigned b) { return (unsigned)(((unsigned long long)a * b) >> 32); }
 static inline float4 __ldg(const float4* p) { return *p; }
-static inline uint4 __ldg(const uint4* p) { return *p; }
-static inline int4 __ldg(const int4* p) { return *p; }
 static inline int __float_as_int(float x) { int i; std::memcpy(&i, &x, sizeof i); return i; }
 static inline unsigned long long atomicOr(unsigned long long* p, unsigned long long v) {
     unsigned long long o = *p; *p |= v; return o;
@@ -36,8 +34,9 @@ extern "C" int trav_run(const mfg_model_desc* d, int64_t n, const double* o, con
     std::memset(&M, 0, sizeof M);
     M.nf = h.nf;
     M.nodes_d = h.nodes_d.data();
-    M.nodes_q = h.nodes_q.data();
-    M.roots_q = h.roots_q.data();
+    M.nodes_c = h.nodes_c.data();
+    M.prims_c = h.prims_c.data();
+    M.roots_c = h.roots_c.data();
     M.roots = h.roots.data();
     M.prims = h.prims.data();
     M.isect_d = h.isect_d.data();
@@ -56,7 +55,7 @@ extern "C" int trav_run(const mfg_model_desc* d, int64_t n, const double* o, con
         const double* p = o + 3 * i;
         const double* q = dir + 3 * i;
         bool a = false;
-        mfgk::HitF hf = mfgk::trace_f(M, h.roots_q[0], mfgk::make_ray_f(p[0], p[1], p[2], float(q[0]), float(q[1]), float(q[2])),
+        mfgk::HitF hf = mfgk::trace_f(M, h.roots_c[0], mfgk::make_ray_f(p[0], p[1], p[2], float(q[0]), float(q[1]), float(q[2])),
                                       last[i], a, &status);
         mfgk::HitD hd = mfgk::trace_d(M, h.roots[0], p[0], p[1], p[2], double(float(q[0])), double(float(q[1])),
                                       double(float(q[2])), last[i], &status);
