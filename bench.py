@@ -134,6 +134,29 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def measure_l2_copy_gbs(torch, mib=24, reps=200):
+    """Read + write bandwidth of a device copy whose buffers (2 x 24 MiB) stay in the 129 MB L2:
+    the measured L2 peak the traversal's L2 traffic is set against (best of 3 timings)."""
+    n = mib << 20
+    a = torch.empty(n, dtype=torch.uint8, device="cuda")
+    b = torch.empty(n, dtype=torch.uint8, device="cuda")
+    a.fill_(1)
+    for _ in range(10):
+        b.copy_(a)
+    best = None
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            b.copy_(a)
+        e1.record()
+        torch.cuda.synchronize()
+        gbs = 2.0 * n * reps / (e0.elapsed_time(e1) * 1e-3) / 1e9
+        best = gbs if best is None or gbs > best else best
+    del a, b
+    return best
+
+
 def oracle_visit_counts(model, n=2000):
     """Mean BVH nodes visited and facets tested per ray, counted by the instrumented CPU oracle."""
     from oracle.oracle import Oracle
@@ -463,11 +486,20 @@ def main():
     mean_launch_s = dev_s / args.steps
     achieved = (hits / args.steps) * bph / mean_launch_s / 1e9
     traffic = None
+    l2 = None
     tp = os.path.join(ROOT, "profiles", "traffic_%s.json" % args.workload)
     if os.path.exists(tp):
         with open(tp) as f:
             tj = json.load(f)
         traffic = tj.get("dram_bytes_per_hit", 0) * hits / args.steps
+        if tj.get("l2_bytes_per_hit"):
+            # L2 side of the roofline: the kernel's L2 bytes per hit (ncu, lts__t_sectors x 32 B,
+            # scaled by hits) at this run's hit rate, against an L2-resident copy measured here
+            l2_peak = measure_l2_copy_gbs(torch)
+            l2_ach = tj["l2_bytes_per_hit"] * (hits / args.steps) / mean_launch_s / 1e9
+            l2 = {"achieved": l2_ach, "peak": l2_peak, "unit": "GB/s", "frac": l2_ach / l2_peak,
+                  "bytes_per_hit": tj["l2_bytes_per_hit"], "peak_kind": "measured L2-resident copy",
+                  "ncu_l2_throughput_pct_of_peak": tj.get("l2_throughput_pct")}
     cpu = None if args.no_cpu_baseline else cpu_baseline(model)
     L = model.layout()
     d2h = 8 * (A.G_N + L["blocks"] * model.n_facets * (A.FC_N + A.FS_N) + L["blocks"] * L["texture_cells"] * 3 +
@@ -492,7 +524,9 @@ def main():
         "model_load_s": load_s,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "bytes_per_hit": bph, "nodes_per_ray": nodes, "facets_per_ray": prims,
-                     "peak_kind": peak_kind},
+                     "peak_kind": peak_kind, "l2": l2,
+                     "limiter": "latency: L1 misses of BVH nodes and facet records and local-memory (stack and "
+                                "spill) loads; DRAM and L2 both well below their peaks"},
         "clocks": clocks,
         "cpu_baseline": cpu,
     }

@@ -492,8 +492,6 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     if (sens) {
         C.sens = s->sens;
         C.sens.smem_code = size_t(h.nf) * 4 <= 48 * 1024 ? 1 : 0;   // packed per-facet words in shared memory
-        C.sens.n_params = int32_t(s->sens_params.size());
-        C.sens.smem_pump = s->sens_params.size() * 4 <= 32 * 1024 ? 1 : 0;   // pumped-flux counts per block
     }
     if (o.block_size == 0 && o.blocks_per_sm == 0 && s->tuned_block[o.precision]) {
         o.block_size = s->tuned_block[o.precision];
@@ -515,8 +513,7 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     C.n_top = o.precision == MFG_PREC_FP32R && o.smem_bvh_levels > 0 && !sens
                   ? int(std::min<size_t>(size_t(1) << o.smem_bvh_levels, h.nodes_c.size())) : 0;
     size_t dyn = (TG_N + (C.smem_facets ? size_t(h.nf) * SF_N : 0)) * 8 + size_t(C.n_top) * sizeof(NodeC) +
-                 (sens && C.sens.smem_code ? size_t(h.nf) * 4 : 0) +
-                 (sens && C.sens.smem_pump ? s->sens_params.size() * 4 : 0);
+                 (sens && C.sens.smem_code ? size_t(h.nf) * 4 : 0);
     // kernel variant: FP64 compiled for at least 2, 3 or 4 resident blocks per SM (register budgets
     // 128, 80, 64), FP32R for 2, 3, 4, 6 or 8 (128, 80, 64, 40, 32); blocks_per_sm selects the
     // variant.  Models with transparent facets, histograms, low-flux mode, scattering, moving

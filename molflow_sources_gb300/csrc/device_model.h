@@ -294,9 +294,7 @@ struct SensCtl {
     // parameter index + 1, bits 20-23 gauge index + 1 (0: none), bit 24 pump
     const int32_t* code;
     int32_t smem_code;               // 1: the packed words are staged in shared memory
-    int32_t smem_pump;               // 1: the pumped-flux column of A is counted in shared memory
-    int32_t n_params;
-    int32_t pad_sens;
+    int32_t pad_code;
     double* A;                       // [P][9] sum over (output event, earlier reflection on parameter k) of y
     double* B;                       // [P][9] sum over absorptions on parameter k of y
     double* Cs;                      // [S][9] sum of y per source

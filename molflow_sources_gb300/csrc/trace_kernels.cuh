@@ -710,26 +710,6 @@ __device__ __noinline__ void reflect_general(const DevModel& M, int fo, bool fli
 
 // output event of the sensitivity variant: y adds to output j, to the score sums of every
 // earlier reflection on a parameter facet, and to the particle's source
-// pumped-flux output event (y = 1): the column of A is a count of (absorption, earlier reflection
-// on parameter k) pairs, kept per block in shared-memory counters when they fit and flushed at the
-// end (exact, as the counts are integers), else added to A directly
-__device__ __noinline__ void sens_pump(const SensCtl& S, const int* traj, int ntraj, int src, unsigned* s_pump) {
-    atomicAdd(S.Y + MFG_SENS_NOUT - 1, 1.0);
-    if (src >= 0) atomicAdd(S.Cs + (size_t)src * MFG_SENS_NOUT + MFG_SENS_NOUT - 1, 1.0);
-    const int n = ntraj < MFG_SENS_TRAJ ? ntraj : MFG_SENS_TRAJ;
-    for (int e = 0; e < n; ++e) {
-        const int k = traj[e];
-        if (s_pump) {
-            const unsigned old = atomicAdd(s_pump + k, 1u);
-            if (old + 1u >= 0x80000000u) {   // move a large partial count to the global sum
-                const unsigned x = atomicExch(s_pump + k, 0u);
-                atomicAdd(S.A + (size_t)k * MFG_SENS_NOUT + MFG_SENS_NOUT - 1, (double)x);
-            }
-        } else {
-            atomicAdd(S.A + (size_t)k * MFG_SENS_NOUT + MFG_SENS_NOUT - 1, 1.0);
-        }
-    }
-}
 __device__ __noinline__ void sens_output(const SensCtl& S, const int* traj, int ntraj, int src, int j, double y) {
     atomicAdd(S.Y + j, y);
     const int n = ntraj < MFG_SENS_TRAJ ? ntraj : MFG_SENS_TRAJ;
@@ -775,14 +755,6 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_
     }
     // packed sensitivity word of a facet: parameter (bits 0-19, +1), gauge (20-23, +1), pump (24)
     auto scode = [&](int f) -> int { return kSens ? scodes[f] : 0; };
-    // pumped-flux counts per parameter, after the staged words
-    unsigned* s_pump = nullptr;
-    if constexpr (kSens) {
-        if (C.sens.smem_pump) {
-            s_pump = reinterpret_cast<unsigned*>(s_ring + (C.sens.smem_code ? M.nf : 0));
-            for (int i = threadIdx.x; i < C.sens.n_params; i += blockDim.x) s_pump[i] = 0u;
-        }
-    }
     for (int i = threadIdx.x; i < MFG_MAXWELL_N; i += blockDim.x) {
         s_cdf_v[i] = M.cdf_v[i];
         s_cdf_p[i] = M.cdf_p[i];
@@ -1232,7 +1204,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_
                 const int k = (code & 0xFFFFF) - 1;
                 if (absorb) {
                     if ((code >> 24) & 1) {
-                        sens_pump(C.sens, traj, ntraj, src_idx, s_pump);
+                        sens_output(C.sens, traj, ntraj, src_idx, MFG_SENS_NOUT - 1, 1.0);
                         if (k >= 0) atomicAdd(C.sens.B + (size_t)k * MFG_SENS_NOUT + MFG_SENS_NOUT - 1, 1.0);
                     }
                 } else if (k >= 0) {
@@ -1362,7 +1334,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_
                 const int code = scode(hf);
                 const int k = (code & 0xFFFFF) - 1;
                 if ((code >> 24) & 1) {
-                    sens_pump(C.sens, traj, ntraj, src_idx, s_pump);
+                    sens_output(C.sens, traj, ntraj, src_idx, MFG_SENS_NOUT - 1, 1.0);
                     if (k >= 0) atomicAdd(C.sens.B + (size_t)k * MFG_SENS_NOUT + MFG_SENS_NOUT - 1, 1.0);
                 }
             }
@@ -1454,11 +1426,6 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_
     sadd(B.sglob + TG_DIST_LO, c_dist, T.global + TG_DIST_LO);
     sadd(B.sglob + TG_DISTF_LO, c_distf, T.global + TG_DISTF_LO);
     __syncthreads();
-    if constexpr (kSens) {
-        if (s_pump)
-            for (int k = threadIdx.x; k < C.sens.n_params; k += blockDim.x)
-                if (s_pump[k]) atomicAdd(C.sens.A + (size_t)k * MFG_SENS_NOUT + MFG_SENS_NOUT - 1, (double)s_pump[k]);
-    }
     if (threadIdx.x < TG_N) {
         int i = threadIdx.x;
         unsigned long long v = B.sglob[i];

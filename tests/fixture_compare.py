@@ -5,11 +5,11 @@ larger of its batch-means error and the Poisson error of the null hypothesis (th
 the two rates), and the reference's own error is that of the same per-particle variance over
 its (larger) number of desorptions.  The family threshold covers every non-empty cell.
 
-Against a stored state a relative systematic allowance `rel_sys` (1 %) is added in quadrature:
-the restatement's RNG and intersection code are not the reference's, and the reference's own
-acceptance rule for these comparisons (GlobalSimuState::Compare, MolflowSimGeom.cpp:559-1148,
-called with 0.9 % global and 7 % per-facet relative thresholds in tests/testsuite.cpp:460) is
-far looser.  Comparisons of the GPU with the oracle use no allowance.
+No systematic allowance is added by default (`rel_sys` = 0): the comparisons are the 3-standard-
+error rule of the combined estimate.  A case with a measured, named cause of a systematic
+difference may pass a relative allowance `rel_sys`, added in quadrature (the reference's own
+acceptance rule, GlobalSimuState::Compare, MolflowSimGeom.cpp:559-1148, called with 0.9 % global
+and 7 % per-facet relative thresholds in tests/testsuite.cpp:460, is far looser).
 """
 import math
 
@@ -38,10 +38,12 @@ def zscores(per, n_per_batch, ref, ref_desorbed, rel_sys=0.0):
     return z, int(mask.sum())
 
 
-def assert_hits_agree(per, n_per_batch, ref, ref_desorbed, extra=0.0, rel_sys=0.01):
+def assert_hits_agree(per, n_per_batch, ref, ref_desorbed, extra=0.0, rel_sys=0.0, label=""):
     z, k = zscores(per, n_per_batch, ref, ref_desorbed, rel_sys)
     thr = z_threshold(max(k, 1)) + extra
     worst = np.unravel_index(np.argmax(np.abs(z)), z.shape)
+    if label:
+        print("%s: max |z| %.2f against %.2f over %d cells (rel_sys %g)" % (label, np.abs(z).max(), thr, k, rel_sys))
     assert np.abs(z).max() < thr, ("max |z| %.2f >= %.2f at (moment, facet) %s: run %.5g, stored %.5g"
                                    % (np.abs(z).max(), thr, worst, per.mean(0)[worst], (ref / ref_desorbed)[worst]))
     return np.abs(z).max(), thr

@@ -36,6 +36,14 @@ CASES = {   # test case -> desorptions per batch
 }
 
 
+# Cases whose stored state differs from this tracer by a measured systematic amount, with the
+# relative allowance that covers it.  02b: 0.2 % more hits per desorption over the whole model
+# (facet 103, time-dependent opacity, 8 sigma at 1.6e6 particles); the stored state lies between
+# reading the opacity at the ray's start time (the present reference source, Particle.cpp:245 with
+# MolflowSimGeom.cpp:23-29) and at the crossing time, 0.55 of the way, on every quantity.
+REL_SYS = {"02b-timedependent_with_three_parameters": 0.003}
+
+
 @pytest.mark.parametrize("case", sorted(CASES))
 def test_gpu_hits_per_moment_match_stored_state(case):
     m, ref, _ = golden_util.load(case)
@@ -50,15 +58,20 @@ def test_gpu_hits_per_moment_match_stored_state(case):
     assert all(s.global_[A.G_NBLEAK] == 0 for s in states) or ref["ref_global"][A.G_NBLEAK] > 0
     ref_hits = ref["ref_hits_moments"] if "ref_hits_moments" in ref else ref["ref_facet_counts"][None, :, A.FC_NBMCHIT]
     per = hit_rates(states)[:, :ref_hits.shape[0]]
-    assert_hits_agree(per, n, ref_hits.astype(np.float64), ref["ref_global"][A.G_NBDESORBED])
+    rs = REL_SYS.get(case, 0.0)
+    assert_hits_agree(per, n, ref_hits.astype(np.float64), ref["ref_global"][A.G_NBDESORBED], rel_sys=rs,
+                      label=case + " hits")
     tex = sorted(int(k[8:]) for k in ref if k.startswith("ref_tex_"))
     if tex:   # texture hit counts of the stored facets, every cell
         pt = np.array([np.concatenate([s.texture_of(f)[..., 0].ravel() for f in tex]) / n for s in states])[:, None, :]
         rt = np.concatenate([ref["ref_tex_%d" % f][..., 0].ravel() for f in tex])[None, :]
-        assert_hits_agree(pt, n, rt.astype(np.float64), ref["ref_global"][A.G_NBDESORBED])
+        assert_hits_agree(pt, n, rt.astype(np.float64), ref["ref_global"][A.G_NBDESORBED], rel_sys=rs,
+                          label=case + " textures")
     if "ref_histogram" in ref:   # bounce / distance / time histograms of absorptions, every moment
         ph = np.array([s.histogram / n for s in states])
-        assert_hits_agree(ph, n, ref["ref_histogram"].astype(np.float64), ref["ref_global"][A.G_NBDESORBED])
+        assert_hits_agree(ph, n, ref["ref_histogram"].astype(np.float64), ref["ref_global"][A.G_NBDESORBED], rel_sys=rs,
+                          label=case + " histograms")
     if "ref_anglemap" in ref:
         pa = np.array([s.anglemap.astype(np.float64) / n for s in states])[:, None, :]
-        assert_hits_agree(pa, n, ref["ref_anglemap"].astype(np.float64)[None, :], ref["ref_global"][A.G_NBDESORBED])
+        assert_hits_agree(pa, n, ref["ref_anglemap"].astype(np.float64)[None, :], ref["ref_global"][A.G_NBDESORBED],
+                          rel_sys=rs, label=case + " angle map")
