@@ -3,7 +3,10 @@
 The run is split into batches (independent particle ranges); a rate's standard error is the
 larger of its batch-means error and the Poisson error of the null hypothesis (the larger of
 the two rates), and the reference's own error is that of the same per-particle variance over
-its (larger) number of desorptions.  The family threshold covers every non-empty cell.
+its (larger) number of desorptions.  The family threshold covers every non-empty cell.  It is
+the normal quantile unless `student` is set; then, since the standard error comes from the batch
+means, it is Student's t quantile with one degree of freedom fewer than the batches (the normal
+quantile is the stricter of the two and rejects a correct run more often).
 
 No systematic allowance is added by default (`rel_sys` = 0): the comparisons are the 3-standard-
 error rule of the combined estimate.  A case with a measured, named cause of a systematic
@@ -38,9 +41,9 @@ def zscores(per, n_per_batch, ref, ref_desorbed, rel_sys=0.0):
     return z, int(mask.sum())
 
 
-def assert_hits_agree(per, n_per_batch, ref, ref_desorbed, extra=0.0, rel_sys=0.0, label=""):
+def assert_hits_agree(per, n_per_batch, ref, ref_desorbed, extra=0.0, rel_sys=0.0, label="", student=False):
     z, k = zscores(per, n_per_batch, ref, ref_desorbed, rel_sys)
-    thr = z_threshold(max(k, 1)) + extra
+    thr = z_threshold(max(k, 1), df=per.shape[0] - 1 if student else None) + extra
     worst = np.unravel_index(np.argmax(np.abs(z)), z.shape)
     if label:
         print("%s: max |z| %.2f against %.2f over %d cells (rel_sys %g)" % (label, np.abs(z).max(), thr, k, rel_sys))

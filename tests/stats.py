@@ -4,9 +4,14 @@ import math
 import numpy as np
 
 
-def z_threshold(k=1, p=0.0027):
+def z_threshold(k=1, p=0.0027, df=None):
     """Two-sided |z| threshold at family-wise level p over k comparisons (Bonferroni);
-    k=1 gives 3.0 (the 3-sigma rule)."""
+    k=1 gives 3.0 (the 3-sigma rule).  With `df`, the statistic's standard error is itself
+    estimated from df+1 batch means, and the threshold is Student's t quantile with df degrees
+    of freedom (the same level; the normal quantile would reject too often)."""
+    if df is not None:
+        from scipy.stats import t
+        return float(t.isf(p / (2.0 * max(k, 1)), df))
     from scipy.stats import norm
     return float(norm.isf(p / (2.0 * max(k, 1))))
 
