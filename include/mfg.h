@@ -327,6 +327,23 @@ int mfg_model_facet_geometry(const mfg_model* model, double* out18, double* area
  * (sp.finalOutgassingRate) and in Pa*m3/s (sp.finalOutgassingRate_Pa_m3_sec).  Any pointer may be NULL. */
 int mfg_model_outgassing(const mfg_model* model, double* total_desorbed_molecules, double* final_rate,
                          double* final_rate_pa_m3_s);
+/* ---- MolFlow+ files on the host (LoaderXML.cpp:31-1130): a .xml file, or the .xml inside a
+ *      .zip (the form the reference saves and its test cases use), read into a model descriptor
+ *      that the handle owns (valid until mfg_xml_close), plus the file's stored results. ---- */
+typedef struct mfg_xml mfg_xml;
+int mfg_xml_open(const char* path, mfg_xml** out);
+/* The same with a parameter catalog folder (LoadParameterCatalog, MolflowSimGeom.cpp:1250-1319): its
+ * .csv parameters ("[catalog] <file name>", file-name order) follow the file's own parameters, as
+ * the reference inserts them; facets may refer to them by name or index.  NULL: no catalog. */
+int mfg_xml_open_catalog(const char* path, const char* catalog_dir, mfg_xml** out);
+const mfg_model_desc* mfg_xml_desc(const mfg_xml* file);
+/* 1 when the file holds stored results (a MolflowResults element), else 0. */
+int32_t mfg_xml_has_results(const mfg_xml* file);
+/* Stored results (MolflowResults, LoaderXML.cpp:366-760) into a view laid out for `model`, a model
+ * created from mfg_xml_desc of the same file: every array of the view is cleared, then filled. */
+int mfg_xml_read_state(const mfg_xml* file, const mfg_model* model, mfg_state_view* out);
+void mfg_xml_close(mfg_xml* file);
+
 /* BVH statistics: node count, depth, leaf count. */
 int mfg_model_bvh_info(const mfg_model* model, int64_t* nodes, int64_t* depth, int64_t* leaves);
 

@@ -80,6 +80,34 @@ struct HostState {
     }
 };
 
+// A MolFlow+ file (.xml, or the .xml inside a .zip; LoaderXML.cpp:31-1130): the model descriptor
+// it holds (valid while the object lives) and its stored results.  `catalog_dir`: a parameter
+// catalog folder whose parameters follow the file's own (LoadParameterCatalog), or null.
+class XmlFile {
+public:
+    explicit XmlFile(const std::string& path, const char* catalog_dir = nullptr) {
+        check(mfg_xml_open_catalog(path.c_str(), catalog_dir, &f_));
+    }
+    ~XmlFile() { mfg_xml_close(f_); }
+    XmlFile(const XmlFile&) = delete;
+    XmlFile& operator=(const XmlFile&) = delete;
+    const mfg_model_desc& desc() const { return *mfg_xml_desc(f_); }
+    bool has_results() const { return mfg_xml_has_results(f_) != 0; }
+    mfg_xml* handle() const { return f_; }
+
+private:
+    mfg_xml* f_ = nullptr;
+};
+
+// The stored results of `file` laid out for `model` (a model created from file.desc()).
+inline void ReadStoredResults(const XmlFile& file, const mfg_model* model, HostState& out) {
+    mfg_state_layout L{};
+    check(mfg_state_layout_of(model, &L));
+    out.resize(L);
+    mfg_state_view v = out.view();
+    check(mfg_xml_read_state(file.handle(), model, &v));
+}
+
 class GpuSimulation {
 public:
     explicit GpuSimulation(int device = 0) : device_(device) {}
@@ -93,6 +121,14 @@ public:
         check(mfg_model_create(&desc, &model_));
         check(mfg_sim_create(model_, device_, &sim_));
         check(mfg_state_layout_of(model_, &layout_));
+    }
+    // LoadSimulation from a MolFlow+ file; with `stored`, the file's results (when it holds
+    // some) are read into it, the state a saved run resumes from.  Returns whether it held results.
+    bool LoadSimulation(const XmlFile& file, HostState* stored = nullptr) {
+        LoadSimulation(file.desc());
+        if (!stored || !file.has_results()) return false;
+        ReadStoredResults(file, model_, *stored);
+        return true;
     }
     void ResetSimulation() { check(mfg_reset(sim_)); }
     const mfg_state_layout& layout() const { return layout_; }

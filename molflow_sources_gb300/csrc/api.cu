@@ -19,6 +19,7 @@
 #include "../../include/mfg.h"
 #include "model_build.h"
 #include "trace_kernels.cuh"
+#include "xml_model.h"
 
 namespace {
 
@@ -182,6 +183,44 @@ int mfg_model_outgassing(const mfg_model* model, double* total_desorbed_molecule
     if (final_rate_pa_m3_s) *final_rate_pa_m3_s = model->h.final_outgassing_rate_pa;
     return MFG_OK;
 }
+
+// ---- MolFlow+ files on the host (LoaderXML.cpp:31-1130) ----
+struct mfg_xml {
+    mfgx::XmlModel m;
+};
+
+int mfg_xml_open(const char* path, mfg_xml** out) { return mfg_xml_open_catalog(path, nullptr, out); }
+
+int mfg_xml_open_catalog(const char* path, const char* catalog_dir, mfg_xml** out) {
+    if (!path || !out) return fail(MFG_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    auto* f = new mfg_xml();
+    std::string err;
+    if (!f->m.load(path, err, catalog_dir)) {
+        delete f;
+        return fail(MFG_ERR_INVALID_ARGUMENT, std::string(path) + ": " + err);
+    }
+    *out = f;
+    return MFG_OK;
+}
+
+const mfg_model_desc* mfg_xml_desc(const mfg_xml* file) { return file ? &file->m.desc : nullptr; }
+
+int32_t mfg_xml_has_results(const mfg_xml* file) {
+    return file && file->m.doc.root() && file->m.doc.root()->child("MolflowResults") ? 1 : 0;
+}
+
+int mfg_xml_read_state(const mfg_xml* file, const mfg_model* model, mfg_state_view* out) {
+    if (!file || !model || !out) return fail(MFG_ERR_INVALID_ARGUMENT, "null argument");
+    if (model->h.nf != file->m.desc.n_facets)
+        return fail(MFG_ERR_INVALID_ARGUMENT, "the model has " + std::to_string(model->h.nf) + " facets, the file " +
+                                                  std::to_string(file->m.desc.n_facets));
+    std::string err;
+    const int rc = mfgx::read_results(file->m.doc.root(), model->h, out, err);
+    return rc == MFG_OK ? MFG_OK : fail(rc, err);
+}
+
+void mfg_xml_close(mfg_xml* file) { delete file; }
 
 int mfg_model_bvh_info(const mfg_model* model, int64_t* nodes, int64_t* depth, int64_t* leaves) {
     if (!model) return fail(MFG_ERR_INVALID_ARGUMENT, "null model");
@@ -1145,7 +1184,7 @@ int mfg_replay(mfg_sim* s, int32_t precision, int64_t n, const double* origin, c
     cudaMemcpyAsync(d_d, direction, 24 * n, cudaMemcpyHostToDevice, s->stream);
     cudaMemcpyAsync(d_l, last_facet, 4 * n, cudaMemcpyHostToDevice, s->stream);
     cudaMemsetAsync(d_r, 0, 16, s->stream);
-    int block = 128;
+    const int block = mfgk::kReplayBlock;
     long long grid = (n + block - 1) / block;
     mfgk::replay_kernel<<<unsigned(grid), block, 0, s->stream>>>(s->dm, precision, n, d_o, d_d, d_l, d_f, d_t, d_r,
                                                                 d_r + 1);
@@ -1187,25 +1226,34 @@ namespace {
 std::mutex g_noalloc_mu;
 unsigned long long* g_noalloc_addr[256];   // device address of g_noalloc_scratch, per device
 
-__global__ void noalloc_pass1(const __grid_constant__ DevModel M, int precision, long long n, const double* origin,
-                              const double* dir, const int* last, int* hit_f, double* hit_t,
-                              unsigned long long* scratch) {
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double ox = origin[3 * i], oy = origin[3 * i + 1], oz = origin[3 * i + 2];
-    double dx = dir[3 * i], dy = dir[3 * i + 1], dz = dir[3 * i + 2];
+// FP32R: lockstep traversal of the warp's rays (lanes past the end take part in the votes)
+__global__ void __launch_bounds__(mfgk::kReplayBlock, 4) noalloc_pass1(const __grid_constant__ DevModel M, int precision,
+                              long long n, const double* origin, const double* dir, const int* last, int* hit_f,
+                              double* hit_t, unsigned long long* scratch) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = i < n;
     int root = M.roots[0];
     const mfgk::OpacCtx oc = mfgk::replay_opacity();
     const mfgk::OpacCtx* ocp = M.has_transparent ? &oc : nullptr;
     if (precision == MFG_PREC_FP64) {
-        mfgk::HitD h = mfgk::trace_d<double>(M, root, ox, oy, oz, dx, dy, dz, last[i], scratch + 1, nullptr, ocp);
+        if (!active) return;
+        mfgk::HitD h = mfgk::trace_d<double>(M, root, origin[3 * i], origin[3 * i + 1], origin[3 * i + 2], dir[3 * i],
+                                             dir[3 * i + 1], dir[3 * i + 2], last[i], scratch + 1, nullptr, ocp);
         hit_f[i] = h.f;
         hit_t[i] = h.f >= 0 ? h.t : -1.0;
         return;
     }
+    double ox = 0, oy = 0, oz = 0, dx = 1, dy = 0, dz = 0;
+    int li = -1;
+    if (active) {
+        ox = origin[3 * i]; oy = origin[3 * i + 1]; oz = origin[3 * i + 2];
+        dx = dir[3 * i]; dy = dir[3 * i + 1]; dz = dir[3 * i + 2];
+        li = last[i];
+    }
     bool amb = false;
-    mfgk::HitF h = mfgk::trace_f(M, M.roots_c[0], mfgk::make_ray_f(ox, oy, oz, (float)dx, (float)dy, (float)dz), last[i], amb,
-                                 scratch + 1, nullptr, ocp);
+    mfgk::HitF h = mfgk::trace_f_lockstep(M, active, M.roots_c[0], mfgk::make_ray_f(ox, oy, oz, (float)dx, (float)dy, (float)dz),
+                                          li, amb, scratch + 1, ocp);
+    if (!active) return;
     if (amb || h.f < 0) {   // queue the ray for the FP64 pass
         unsigned long long k = atomicAdd(scratch, 1ull);
         scratch[2 + k] = (unsigned long long)i;
@@ -1263,7 +1311,7 @@ extern "C" int mfg_replay_noalloc(mfg_sim* s, int32_t precision, int64_t n, cons
         scratch = g_noalloc_addr[s->device];
     }
     CK(cudaMemsetAsync(scratch, 0, 2 * sizeof(unsigned long long), s->stream));   // queue counter and status
-    const int block = 128;
+    const int block = mfgk::kReplayBlock;
     const unsigned grid = unsigned((n + block - 1) / block);
     noalloc_pass1<<<grid, block, 0, s->stream>>>(s->dm, precision, n, d_origin, d_direction, d_last, d_hit_facet,
                                                   d_hit_t, scratch);

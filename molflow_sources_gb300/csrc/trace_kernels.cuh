@@ -1452,37 +1452,51 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_
 }
 
 // ------------------------------------------------------------ replay ----
-__global__ void replay_kernel(const __grid_constant__ DevModel M, int precision, long long n, const double* origin,
-                              const double* dir, const int* last, int* hit_f, double* hit_t,
-                              unsigned long long* rechecks, unsigned long long* status) {
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double ox = origin[3 * i], oy = origin[3 * i + 1], oz = origin[3 * i + 2];
-    double dx = dir[3 * i], dy = dir[3 * i + 1], dz = dir[3 * i + 2];
-    int root = M.roots[0];
+// One ray per thread.  FP32R: the warp traverses its lanes' rays in lockstep (every lane takes
+// part in the votes, also those past the end), then an ambiguous or missing hit goes to the FP64
+// traversal.  256 threads, at least 4 blocks per SM (64 registers): the traversal alone runs
+// without spills at that budget.
+constexpr int kReplayBlock = 256;
+__global__ void __launch_bounds__(kReplayBlock, 4) replay_kernel(const __grid_constant__ DevModel M, int precision,
+                              long long n, const double* origin, const double* dir, const int* last, int* hit_f,
+                              double* hit_t, unsigned long long* rechecks, unsigned long long* status) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = i < n;
+    const int root = M.roots[0];
     const OpacCtx oc = replay_opacity();
     const OpacCtx* ocp = M.has_transparent ? &oc : nullptr;
     if (precision == 0) {
+        if (!active) return;
+        const double ox = origin[3 * i], oy = origin[3 * i + 1], oz = origin[3 * i + 2];
+        const double dx = dir[3 * i], dy = dir[3 * i + 1], dz = dir[3 * i + 2];
         HitD h = trace_d<double>(M, root, ox, oy, oz, dx, dy, dz, last[i], status, nullptr, ocp);
         hit_f[i] = h.f;
         hit_t[i] = h.f >= 0 ? h.t : -1.0;
+        return;
+    }
+    double ox = 0, oy = 0, oz = 0, dx = 1, dy = 0, dz = 0;
+    int li = -1;
+    if (active) {
+        ox = origin[3 * i]; oy = origin[3 * i + 1]; oz = origin[3 * i + 2];
+        dx = dir[3 * i]; dy = dir[3 * i + 1]; dz = dir[3 * i + 2];
+        li = last[i];
+    }
+    bool amb = false;
+    const HitF h = trace_f_lockstep(M, active, M.roots_c[0], make_ray_f(ox, oy, oz, (float)dx, (float)dy, (float)dz), li,
+                                    amb, status, ocp);
+    if (!active) return;
+    if (amb || h.f < 0) {
+        atomicAdd(rechecks, 1ull);
+        HitD hd = trace_d<double>(M, root, ox, oy, oz, dx, dy, dz, li, status, nullptr, ocp);
+        hit_f[i] = hd.f;
+        hit_t[i] = hd.f >= 0 ? hd.t : -1.0;
     } else {
-        bool amb = false;
-        HitF h = trace_f(M, M.roots_c[0], make_ray_f(ox, oy, oz, (float)dx, (float)dy, (float)dz), last[i], amb, status,
-                         nullptr, ocp);
-        if (amb || h.f < 0) {
-            atomicAdd(rechecks, 1ull);
-            HitD hd = trace_d<double>(M, root, ox, oy, oz, dx, dy, dz, last[i], status, nullptr, ocp);
-            hit_f[i] = hd.f;
-            hit_t[i] = hd.f >= 0 ? hd.t : -1.0;
-        } else {
-            const FacetIsectD& Rh = M.isect_d[h.f];
-            double den = Rh.v[0] * dx + Rh.v[1] * dy + Rh.v[2] * dz;
-            double num = Rh.v[3] - (Rh.v[0] * ox + Rh.v[1] * oy + Rh.v[2] * oz);
-            double r = num - (double)h.t * den;
-            hit_f[i] = h.f;
-            hit_t[i] = (double)h.t + (double)((float)r / (float)den);
-        }
+        const FacetIsectD& Rh = M.isect_d[h.f];
+        double den = Rh.v[0] * dx + Rh.v[1] * dy + Rh.v[2] * dz;
+        double num = Rh.v[3] - (Rh.v[0] * ox + Rh.v[1] * oy + Rh.v[2] * oz);
+        double r = num - (double)h.t * den;
+        hit_f[i] = h.f;
+        hit_t[i] = (double)h.t + (double)((float)r / (float)den);
     }
 }
 

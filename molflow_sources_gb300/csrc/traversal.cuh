@@ -443,6 +443,34 @@ __device__ __forceinline__ void trav_step(const DevModel& M, TravF& s, Stk& stk,
     s.ref = stk.sp == 0 ? kTrDone : stk.pop();
 }
 
+// Lockstep FP32 traversal of one ray per lane, for kernels whose lanes trace independent rays
+// (replay): every lane of the warp calls it, lanes without a ray with `active` false.  The warp
+// visits one node or one leaf list per lane and step and votes after each step; node and leaf
+// steps run in separate rounds, a leaf round once the lanes at leaves outnumber those at nodes
+// three to one (the tracer's own traversal loop does the same).  Device code only (warp votes).
+#ifdef __CUDACC__
+template <bool kTr = true>
+__device__ __forceinline__ HitF trace_f_lockstep(const DevModel& M, bool active, int root, const RayF& ray, int last,
+                                                 bool& ambiguous, unsigned long long* status,
+                                                 const OpacCtx* oc = nullptr) {
+    TravF s;
+    TravStack stk;
+    if (active) trav_init(s, stk, root, ray, last);
+    else s.ref = kTrDone;
+    while (true) {
+        const bool live = s.ref != kTrDone;
+        const bool node = live && s.ref >= 0;
+        const unsigned mn = __ballot_sync(0xffffffffu, node);
+        const unsigned ml = __ballot_sync(0xffffffffu, live && !node);
+        if ((mn | ml) == 0u) break;
+        const bool leaf_round = __popc(ml) > 3 * __popc(mn);
+        if (leaf_round ? (live && !node) : node) trav_step<kTr>(M, s, stk, status, nullptr, oc);
+    }
+    ambiguous = active && s.amb;
+    return s.h;
+}
+#endif
+
 // FP32 traversal with per-candidate error bounds.  Returns the hit and sets
 // `ambiguous` when a candidate could be classified differently in exact
 // arithmetic (near an edge, near the origin, or too close to the best hit).

@@ -22,19 +22,21 @@ def reduce_state(state, group=None, dst=None):
     With dst set, only that rank is guaranteed to hold the sum (reduce), else all (all_reduce)."""
     import torch
     import torch.distributed as dist
+    # NCCL reduces device tensors only: stage each array through this rank's GPU
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend(group) == "nccl" else torch.device("cpu")
     for name in ("global_", "facet_counts", "facet_sums", "texture", "profile", "direction", "anglemap"):
         arr = getattr(state, name)
         if arr.size == 0:
             continue
         if arr.dtype == np.uint64:
-            t = torch.from_numpy(arr.view(np.int64).copy())
+            t = torch.from_numpy(arr.view(np.int64).copy()).to(dev)
         else:
-            t = torch.from_numpy(np.ascontiguousarray(arr, dtype=np.float64).copy())
+            t = torch.from_numpy(np.ascontiguousarray(arr, dtype=np.float64).copy()).to(dev)
         if dst is None:
             dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
         else:
             dist.reduce(t, dst=dst, op=dist.ReduceOp.SUM, group=group)
-        out = t.numpy()
+        out = t.cpu().numpy()
         if arr.dtype == np.uint64:
             arr[...] = out.view(np.uint64)
         else:
