@@ -134,29 +134,6 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def measure_l2_copy_gbs(torch, mib=24, reps=200):
-    """Read + write bandwidth of a device copy whose buffers (2 x 24 MiB) stay in the 129 MB L2:
-    the measured L2 peak the traversal's L2 traffic is set against (best of 3 timings)."""
-    n = mib << 20
-    a = torch.empty(n, dtype=torch.uint8, device="cuda")
-    b = torch.empty(n, dtype=torch.uint8, device="cuda")
-    a.fill_(1)
-    for _ in range(10):
-        b.copy_(a)
-    best = None
-    for _ in range(3):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(reps):
-            b.copy_(a)
-        e1.record()
-        torch.cuda.synchronize()
-        gbs = 2.0 * n * reps / (e0.elapsed_time(e1) * 1e-3) / 1e9
-        best = gbs if best is None or gbs > best else best
-    del a, b
-    return best
-
-
 def oracle_visit_counts(model, n=2000):
     """Mean BVH nodes visited and facets tested per ray, counted by the instrumented CPU oracle."""
     from oracle.oracle import Oracle
@@ -501,14 +478,18 @@ def main():
         with open(tp) as f:
             tj = json.load(f)
         traffic = tj.get("dram_bytes_per_hit", 0) * hits / args.steps
-        if tj.get("l2_bytes_per_hit"):
-            # L2 side of the roofline: the kernel's L2 bytes per hit (ncu, lts__t_sectors x 32 B,
-            # scaled by hits) at this run's hit rate, against an L2-resident copy measured here
-            l2_peak = measure_l2_copy_gbs(torch)
+        if tj.get("l2_bytes_per_hit") and tj.get("l2_throughput_pct") and tj.get("capture_ms"):
+            # L2 side of the roofline: the kernel's L2 bytes per hit (ncu lts__t_sectors x 32 B) at this
+            # run's hit rate, against the L2 peak implied by the same capture (its L2 bytes per second
+            # divided by its lts__throughput fraction of peak)
+            cap_gbs = tj["l2_bytes_per_hit"] * tj["hits_in_capture"] / (tj["capture_ms"] * 1e-3) / 1e9
+            l2_peak = cap_gbs / (tj["l2_throughput_pct"] / 100.0)
             l2_ach = tj["l2_bytes_per_hit"] * (hits / args.steps) / mean_launch_s / 1e9
             l2 = {"achieved": l2_ach, "peak": l2_peak, "unit": "GB/s", "frac": l2_ach / l2_peak,
-                  "bytes_per_hit": tj["l2_bytes_per_hit"], "peak_kind": "measured L2-resident copy",
-                  "ncu_l2_throughput_pct_of_peak": tj.get("l2_throughput_pct")}
+                  "bytes_per_hit": tj["l2_bytes_per_hit"],
+                  "peak_kind": "ncu: the capture's L2 bytes per second over its lts__throughput fraction",
+                  "ncu_l2_throughput_pct_of_peak": tj["l2_throughput_pct"],
+                  "ncu_l1_throughput_pct_of_peak": tj.get("l1_throughput_pct")}
     cpu = None if args.no_cpu_baseline else cpu_baseline(model)
     L = model.layout()
     d2h = 8 * (A.G_N + L["blocks"] * model.n_facets * (A.FC_N + A.FS_N) + L["blocks"] * L["texture_cells"] * 3 +

@@ -343,6 +343,12 @@ int32_t mfg_xml_has_results(const mfg_xml* file);
  * created from mfg_xml_desc of the same file: every array of the view is cleared, then filled. */
 int mfg_xml_read_state(const mfg_xml* file, const mfg_model* model, mfg_state_view* out);
 void mfg_xml_close(mfg_xml* file);
+/* SaveGeometry + SaveSimulationState (WriterXML.cpp:72-903): the model `desc` (as `model` was created
+ * from it) and the results in `state` (a view laid out for `model`; NULL: geometry and settings only)
+ * as a MolFlow+ file; a path ending in ".zip" gets one stored .xml entry.  `param_names`: n_params
+ * names of the time-dependent parameters, or NULL ("param<i>"). */
+int mfg_xml_save(const char* path, const mfg_model_desc* desc, const mfg_model* model, const mfg_state_view* state,
+                 const char* const* param_names);
 
 /* BVH statistics: node count, depth, leaf count. */
 int mfg_model_bvh_info(const mfg_model* model, int64_t* nodes, int64_t* depth, int64_t* leaves);

@@ -130,6 +130,15 @@ public:
         ReadStoredResults(file, model_, *stored);
         return true;
     }
+    // SaveGeometry + SaveSimulationState (WriterXML.cpp:72-903): the loaded model (`desc`, as given
+    // to LoadSimulation) and `state` (null: geometry and settings only) as a MolFlow+ file; a path
+    // ending in ".zip" gets one .xml entry.  `param_names`: n_params names, or null.
+    void SaveSimulationState(const std::string& path, const mfg_model_desc& desc, HostState* state,
+                             const char* const* param_names = nullptr) const {
+        mfg_state_view v{};
+        if (state) v = state->view();
+        check(mfg_xml_save(path.c_str(), &desc, model_, state ? &v : nullptr, param_names));
+    }
     void ResetSimulation() { check(mfg_reset(sim_)); }
     const mfg_state_layout& layout() const { return layout_; }
 

@@ -20,6 +20,7 @@
 #include "model_build.h"
 #include "trace_kernels.cuh"
 #include "xml_model.h"
+#include "xml_writer.h"
 
 namespace {
 
@@ -221,6 +222,20 @@ int mfg_xml_read_state(const mfg_xml* file, const mfg_model* model, mfg_state_vi
 }
 
 void mfg_xml_close(mfg_xml* file) { delete file; }
+
+int mfg_xml_save(const char* path, const mfg_model_desc* desc, const mfg_model* model, const mfg_state_view* state,
+                 const char* const* param_names) {
+    if (!path || !desc || !model) return fail(MFG_ERR_INVALID_ARGUMENT, "null argument");
+    if (desc->n_facets != model->h.nf)
+        return fail(MFG_ERR_INVALID_ARGUMENT, "the descriptor has " + std::to_string(desc->n_facets) + " facets, the model " +
+                                                  std::to_string(model->h.nf));
+    std::vector<std::string> names;
+    if (param_names)
+        for (int p = 0; p < desc->n_params; ++p) names.push_back(param_names[p] ? param_names[p] : "");
+    std::string err;
+    if (!mfgx::write_file(path, *desc, model->h, state, names, err)) return fail(MFG_ERR_INVALID_ARGUMENT, err);
+    return MFG_OK;
+}
 
 int mfg_model_bvh_info(const mfg_model* model, int64_t* nodes, int64_t* depth, int64_t* leaves) {
     if (!model) return fail(MFG_ERR_INVALID_ARGUMENT, "null model");

@@ -1,6 +1,7 @@
 // Reads a MolFlow+ file through the C++ adapter (mfg::XmlFile) and prints what the host sees:
 // facet and moment counts, the stored global counters and the sums of the stored facet counters.
-// Usage: xml_check <file.xml|file.zip> [catalog folder]
+// With a third argument, writes the model and the stored results back to that path (mfg_xml_save).
+// Usage: xml_check <file.xml|file.zip> [catalog folder or ""] [output file]
 #include <cstdio>
 
 #include "mfg_simulation.hpp"
@@ -8,7 +9,7 @@
 int main(int argc, char** argv) {
     if (argc < 2) return 2;
     try {
-        mfg::XmlFile file(argv[1], argc > 2 ? argv[2] : nullptr);
+        mfg::XmlFile file(argv[1], argc > 2 && argv[2][0] ? argv[2] : nullptr);
         const mfg_model_desc& d = file.desc();
         mfg_model* model = nullptr;
         mfg::check(mfg_model_create(&d, &model));
@@ -24,6 +25,11 @@ int main(int argc, char** argv) {
             }
             std::printf("global %.17g %.17g %.17g facet_hits %llu facet_des %llu\n", st.global[MFG_G_NBMCHIT],
                         st.global[MFG_G_NBDESORBED], st.global[MFG_G_NBLEAK], hits, des);
+            if (argc > 3) {
+                mfg_state_view v = st.view();
+                mfg::check(mfg_xml_save(argv[3], &d, model, &v, nullptr));
+                std::printf("saved %s\n", argv[3]);
+            }
         }
         mfg_model_destroy(model);
     } catch (const mfg::Error& e) {
