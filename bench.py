@@ -525,6 +525,11 @@ def main():
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+    if not gate["pass"]:
+        # the metric is defined at the same 3-sigma transmission: a run that misses it is not a result
+        sys.stderr.write("transmission gate failed: FP32R %.6g against FP64 %.6g (z = %.2f)\n"
+                         % (gate["fp32r"], gate["fp64"], gate["z"]))
+        return 3
     return 0
 
 
