@@ -241,6 +241,21 @@ def run_batch(args, torch, dist, rank, world, local, W, n_step):
         des += st["desorbed"]
         launches += st["kernel_launches"]
     clocks = sampler.stop()
+    # end to end: the public batch call with its per-instance particle counts from host memory, then
+    # every instance's GlobalSimuState read back to host memory (mfg_fetch_instance), every step
+    e2e_hits, d2h = 0, 0
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    for k in range(args.steps):
+        st = batch.run(n_step, precision=A.PREC_FP32R, seed=seed, use_graph=True, **tuned)
+        e2e_hits += st["hits"]
+        d2h = 0
+        for i in range(len(models)):
+            si = batch.fetch_instance(i)
+            d2h += sum(getattr(si, a).nbytes for a in ("global_", "facet_counts", "facet_sums", "texture", "profile",
+                                                       "direction", "anglemap", "histogram"))
+    torch.cuda.synchronize()
+    e2e_rate = e2e_hits / (time.perf_counter() - t2)
     # separate launches: one simulation per instance, each stepped on its own with the same
     # desorptions per instance as the batch step, through a captured graph as well (the first
     # step of each captures it), at the launch shape the batch uses
@@ -267,7 +282,8 @@ def run_batch(args, torch, dist, rank, world, local, W, n_step):
                                   "desorptions_per_instance": n_step, "launches": len(models),
                                   "launch": "CUDA graph per instance"},
             "gpu_launches": launches, "model_load_s": load_s, "clocks": clocks,
-            "e2e": {"value": rate, "unit": "hits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "e2e": {"value": e2e_rate, "unit": "hits/s", "h2d_bytes_per_step": 8 * len(models) + 96,
+                    "d2h_bytes_per_step": int(d2h), "api": "mfg_run_batch + mfg_fetch_instance of every instance"},
             "cpu_baseline": None}
     if rank == 0:
         print(json.dumps(line), flush=True)
