@@ -170,6 +170,69 @@ def cpu_baseline(model, target_s=12.0):
             "seconds": s["seconds"]}
 
 
+def other_workloads(torch, local, steps=2):
+    """Short device-time measurements of configs 1, 3, 4 and 5 beside the headline (each at its own
+    autotuned launch shape, the full step sizes of their own bench lines, `steps` timed steps after
+    one warm-up, L2 not flushed): hits/s, and for config 5 the gradient run's cost over the forward
+    run.  `python bench.py --workload cN` gives each one's full line."""
+    from molflow_sources_gb300 import _abi as A
+    from molflow_sources_gb300.simulation import GpuBatch, GpuSimulation
+    seed = 0x4D6F6C66
+    out = {}
+
+    def timed(run, n):
+        run(max(n // 10, 1000))
+        torch.cuda.synchronize()
+        ms = hits = 0.0
+        for _ in range(steps):
+            st = run(n)
+            ms += st["kernel_ms"]
+            hits += st["hits"]
+        return hits / (ms / 1e3), ms / steps
+
+    for wl in ("c1", "c3", "c5"):
+        try:
+            m = make_model(wl)
+            sim = GpuSimulation(m, device=local)
+            n = WORKLOADS[wl]["step"]
+            shape = sim.autotune(max(n // 20, 10000), precision=A.PREC_FP32R, seed=seed)
+
+            def fwd(k):
+                sim.SimulationMCStep(k, precision=A.PREC_FP32R, seed=seed, **shape)
+                return sim.last_stats
+            rate, ms = timed(fwd, n)
+            out[wl] = {"workload": WORKLOADS[wl]["name"], "hits_per_s": rate, "ms_per_step": ms,
+                       "desorptions_per_step": n, "launch_shape": shape}
+            if wl == "c5":
+                from molflow_sources_gb300.sensitivity import SensitivityFunction
+                sf = SensitivityFunction(sim, m.neg, m.gauges, m.neg)
+
+                def grad(k):
+                    sf.forward(k, seed=seed)
+                    return sf.last_stats
+                srate, sms = timed(grad, n)
+                out[wl].update({"hits_per_s": srate, "ms_per_step": sms, "forward_hits_per_s": rate,
+                                "gradient_cost_over_forward": rate / srate, "launch_shape": "sensitivity kernel default"})
+            sim.close()
+        except Exception as e:   # a side measurement never breaks the headline line
+            out[wl] = {"error": str(e)[:200]}
+    try:
+        from molflow_sources_gb300 import batch_workloads as BW
+        batch = GpuBatch(BW.config4_batch(), device=local)
+        n = WORKLOADS["c4"]["step"]
+        shape = batch.autotune(max(n // 20, 1000), precision=A.PREC_FP32R, seed=seed)
+
+        def brun(k):
+            return batch.run(k, precision=A.PREC_FP32R, seed=seed, use_graph=True, **shape)
+        rate, ms = timed(brun, n)
+        out["c4"] = {"workload": WORKLOADS["c4"]["name"], "hits_per_s": rate, "ms_per_step": ms,
+                     "desorptions_per_instance_per_step": n, "launch_shape": shape}
+        batch.close()
+    except Exception as e:
+        out["c4"] = {"error": str(e)[:200]}
+    return out
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -354,6 +417,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--launch", default="",
                     help="fixed FP32R launch shape BLOCK,BLOCKS_PER_SM[,SMEM_BVH_LEVELS] instead of the autotuner's choice")
+    ap.add_argument("--no-others", action="store_true",
+                    help="skip the short measurements of configs 1, 3, 4 and 5 in the config-2 line")
     ap.add_argument("--profile-steps", action="store_true",
                     help="bracket the timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     args = ap.parse_args()
@@ -507,6 +572,7 @@ def main():
                   "ncu_l2_throughput_pct_of_peak": tj["l2_throughput_pct"],
                   "ncu_l1_throughput_pct_of_peak": tj.get("l1_throughput_pct")}
     cpu = None if args.no_cpu_baseline else cpu_baseline(model)
+    others = other_workloads(torch, local) if (args.workload == "c2" and world == 1 and not args.no_others) else None
     L = model.layout()
     d2h = 8 * (A.G_N + L["blocks"] * model.n_facets * (A.FC_N + A.FS_N) + L["blocks"] * L["texture_cells"] * 3 +
                L["blocks"] * L["profile_facets"] * 300 + L["anglemap_cells"])
@@ -537,6 +603,7 @@ def main():
                                 "issue slots 49 %, L2 41 %, DRAM 26 % of their peaks"},
         "clocks": clocks,
         "cpu_baseline": cpu,
+        "other_workloads": others,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:
