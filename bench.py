@@ -195,7 +195,7 @@ def other_workloads(torch, local, steps=2):
             m = make_model(wl)
             sim = GpuSimulation(m, device=local)
             n = WORKLOADS[wl]["step"]
-            shape = sim.autotune(max(n // 20, 10000), precision=A.PREC_FP32R, seed=seed)
+            shape = sim.autotune(max(n // 4, 10000), precision=A.PREC_FP32R, seed=seed)   # as the main line
 
             def fwd(k):
                 sim.SimulationMCStep(k, precision=A.PREC_FP32R, seed=seed, **shape)
