@@ -54,6 +54,21 @@ def build(force=False, verbose=False):
         out, _ = p.communicate()
         if verbose or p.returncode:
             sys.stderr.write(out.decode(errors="replace"))
+        crashed = p.returncode < 0 or p.returncode in (134, 139) or b"Segmentation fault" in out or b"core dumped" in out
+        if p.returncode and crashed:
+            # the compiler itself crashed (a signal, not a diagnostic): once more on one thread, then
+            # with the node fetches as two 16-byte loads (MFG_NO_V8), the form every toolchain takes
+            retries = ([c for c in cmd if c != "-split-compile=0"],
+                       [c for c in cmd if c != "-split-compile=0"] + ["-DMFG_NO_V8"])
+            for again in retries:
+                sys.stderr.write("compiler crashed (status %d); retrying: %s\n" % (p.returncode, " ".join(again)))
+                r = subprocess.run(again, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+                if r.returncode == 0:
+                    break
+                sys.stderr.write(r.stdout.decode(errors="replace"))
+            else:
+                raise RuntimeError("compile failed: " + " ".join(cmd))
+            continue
         if p.returncode:
             raise RuntimeError("compile failed: " + " ".join(cmd))
     tmp = LIB + ".tmp%d" % os.getpid()
