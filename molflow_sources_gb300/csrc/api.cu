@@ -280,6 +280,7 @@ static int sim_upload(mfg_sim* s) {
     UP(h.og, og);
     UP(h.mstart, mstart);
     UP(h.mend, mend);
+    UP(h.mguide, mguide);
     UP(h.id_start, id_start);
     UP(h.id_t, id_t);
     UP(h.id_cum, id_cum);
@@ -296,6 +297,10 @@ static int sim_upload(mfg_sim* s) {
     M.src_total = h.src_total;
     M.latest = h.latest;
     M.maxwin = h.maxwin;
+    M.mg_t0 = h.mg_t0;
+    M.mg_l0 = h.mg_l0;
+    M.mg_scale = h.mg_scale;
+    M.mg_n = int32_t(h.mguide.size());
     for (int i = 0; i < MFG_MAXWELL_N; ++i) { M.cdf_v[i] = h.cdf_v[i]; M.cdf_p[i] = h.cdf_p[i]; }
     M.gas_mass = h.gas_mass;
     M.ort_factor = h.use_maxwell ? 1.0 : 1.1781;
@@ -547,7 +552,10 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
         C.sens = s->sens;
         C.sens.smem_code = size_t(h.nf) * 4 <= 48 * 1024 ? 1 : 0;   // packed per-facet words in shared memory
     }
-    if (o.block_size == 0 && o.blocks_per_sm == 0 && s->tuned_block[o.precision]) {
+    // the autotuned shape, unless it is one the sensitivity variants are not compiled for (512- and
+    // 1024-thread blocks): those runs keep their default shape
+    if (o.block_size == 0 && o.blocks_per_sm == 0 && s->tuned_block[o.precision] &&
+        !(sens && s->tuned_block[o.precision] > 256)) {
         o.block_size = s->tuned_block[o.precision];
         o.blocks_per_sm = s->tuned_bps[o.precision];
     }

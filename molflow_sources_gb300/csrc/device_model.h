@@ -204,6 +204,12 @@ struct DevModel {
     const double* mstart;        // moment window starts (sorted)
     const double* mend;
     double maxwin;
+    // guide to the moment search: mguide[b] = number of window starts <= 2^(mg_l0 + b / mg_scale),
+    // a lower bound of the search's answer for times in bucket b (null: binary search)
+    const int32_t* mguide;
+    double mg_t0;                // 2^mg_l0, the first bucket's start
+    float mg_l0, mg_scale;
+    int32_t mg_n;
     // integrated desorption tables (concatenated)
     const int32_t* id_start;
     const double* id_t;

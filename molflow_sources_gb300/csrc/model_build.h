@@ -49,6 +49,9 @@ struct HostModel {
     double latest = 0;
     std::vector<double> mstart, mend;
     double maxwin = 0;
+    std::vector<int32_t> mguide;          // log-time guide to the moment search (empty: none)
+    double mg_t0 = 0;
+    float mg_l0 = 0, mg_scale = 0;
     double cdf_v[MFG_MAXWELL_N], cdf_p[MFG_MAXWELL_N];
     std::vector<int32_t> par_start;       // time-dependent parameters
     std::vector<double> par_t, par_v;

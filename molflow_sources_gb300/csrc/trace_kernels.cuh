@@ -97,8 +97,18 @@ __device__ __forceinline__ unsigned long long qf(float x, float scale) {
 template <class F>
 __device__ __forceinline__ void for_moments(const DevModel& M, double t, F f) {
     if (M.nm == 0) return;
-    int lo = 0, hi = M.nm;   // first start > t
-    while (lo < hi) { int mid = (lo + hi) >> 1; if (M.mstart[mid] <= t) lo = mid + 1; else hi = mid; }
+    int lo = 0;   // first start > t
+    if (M.mguide) {   // guide entry one bucket low (a lower bound), then forward steps
+        if (t > M.mg_t0) {
+            int b = (int)((log2f((float)t) - M.mg_l0) * M.mg_scale) - 1;
+            b = min(max(b, 0), M.mg_n - 1);
+            lo = M.mguide[b];
+        }
+        while (lo < M.nm && M.mstart[lo] <= t) ++lo;
+    } else {
+        int hi = M.nm;
+        while (lo < hi) { int mid = (lo + hi) >> 1; if (M.mstart[mid] <= t) lo = mid + 1; else hi = mid; }
+    }
     for (int k = lo - 1; k >= 0 && M.mstart[k] > t - M.maxwin - 1e-300; --k)
         if (M.mstart[k] <= t && t < M.mend[k]) f(k + 1);
 }

@@ -230,3 +230,20 @@ def test_sensitivity_setup_refuses_low_flux_models():
         SensitivityFunction(sim, m.neg, m.gauges, m.neg)
     assert e.value.code == A.MFG_ERR_UNSUPPORTED_FEATURE
     sim.close()
+
+
+def test_gradients_after_autotune(setup):
+    """An autotuned plain shape (512- or 1024-thread blocks) does not carry over to the sensitivity
+    kernel, which keeps a compiled shape; the outputs are those of an untuned run."""
+    m, sim, sf = setup
+    sim.ResetSimulation()
+    sim.autotune(200000, precision=A.PREC_FP32R, seed=SEED)
+    n = 200000
+    sim.ResetSimulation()
+    sim.set_particle_offset(0)
+    y_tuned = sf.forward(n, precision=A.PREC_FP32R, seed=SEED)
+    sim.ResetSimulation()
+    sim.set_particle_offset(0)
+    y_plain = sf.forward(n, precision=A.PREC_FP32R, seed=SEED, block_size=256, blocks_per_sm=2)
+    # the same particles; FP64 output sums added in another order
+    np.testing.assert_allclose(y_tuned, y_plain, rtol=1e-9, atol=0)
