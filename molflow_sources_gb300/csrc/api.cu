@@ -832,10 +832,30 @@ static int fetch_range(mfg_sim* s, mfg_state_view* v, int fb, int nf, int64_t tb
     unsigned long long* const pr = tx + s->n_texture;
     unsigned long long* const am = pr + s->n_profile;
     CK(cudaMemcpyAsync(g, s->dt.global, TG_N * 8, cudaMemcpyDeviceToHost, s->stream));
-    if (s->n_facet) CK(cudaMemcpyAsync(fa, s->dt.facet, s->n_facet * 8, cudaMemcpyDeviceToHost, s->stream));
-    if (s->n_texture && v->texture) CK(cudaMemcpyAsync(tx, s->dt.texture, s->n_texture * 8, cudaMemcpyDeviceToHost, s->stream));
-    if (s->n_profile && v->profile) CK(cudaMemcpyAsync(pr, s->dt.profile, s->n_profile * 8, cudaMemcpyDeviceToHost, s->stream));
-    if (s->n_anglemap && v->anglemap) CK(cudaMemcpyAsync(am, s->dt.anglemap, s->n_anglemap * 8, cudaMemcpyDeviceToHost, s->stream));
+    // the stage mirrors the device arrays; one instance of a batch copies only its own rows of each
+    // moment block (a copy per block and array, into the same stage offsets)
+    auto rows = [&](unsigned long long* dst, const unsigned long long* src, size_t total, size_t block, size_t first,
+                    size_t count, size_t width) -> int {
+        if (!total || !count) return MFG_OK;
+        if (whole) {
+            CK(cudaMemcpyAsync(dst, src, total * 8, cudaMemcpyDeviceToHost, s->stream));
+            return MFG_OK;
+        }
+        for (size_t m = 0; m < B; ++m) {
+            const size_t o = (m * block + first) * width;
+            CK(cudaMemcpyAsync(dst + o, src + o, count * width * 8, cudaMemcpyDeviceToHost, s->stream));
+        }
+        return MFG_OK;
+    };
+    int rc;
+    if ((rc = rows(fa, s->dt.facet, s->n_facet, NF, size_t(fb), size_t(nf), TF_N)) != MFG_OK) return rc;
+    if (v->texture && (rc = rows(tx, s->dt.texture, s->n_texture, NT, size_t(tb), size_t(nt), TT_N)) != MFG_OK) return rc;
+    if (v->profile && (rc = rows(pr, s->dt.profile, s->n_profile, NP, size_t(pb) * MFG_PROFILE_SIZE,
+                                 size_t(np) * MFG_PROFILE_SIZE, TT_N)) != MFG_OK)
+        return rc;
+    if (s->n_anglemap && v->anglemap && na > 0)
+        CK(cudaMemcpyAsync(am + (whole ? 0 : ab), s->dt.anglemap + (whole ? 0 : ab), (whole ? s->n_anglemap : size_t(na)) * 8,
+                           cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     uint64_t sh = 0, sd = 0, sa = 0;
     for (int i = 0; i < nf; ++i) {
