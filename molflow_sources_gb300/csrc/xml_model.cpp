@@ -25,7 +25,11 @@ double to_d(const char* s) { return std::strtod(s, nullptr); }
 long long to_i(const char* s) {
     if (std::strcmp(s, "true") == 0) return 1;
     if (std::strcmp(s, "false") == 0) return 0;
-    return (long long)std::strtod(s, nullptr);
+    const double v = std::strtod(s, nullptr);
+    if (!(v == v)) return 0;   // not a number
+    if (v >= 9.2e18) return 9200000000000000000LL;   // out of range: clamped, not undefined
+    if (v <= -9.2e18) return -9200000000000000000LL;
+    return (long long)v;
 }
 double fa(const XNode* n, const char* a, double def = 0.0) {
     const char* v = n ? n->attr(a) : nullptr;

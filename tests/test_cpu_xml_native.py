@@ -311,3 +311,26 @@ def test_native_writer_and_reader_outgassing_map(tmp_path):
         np.testing.assert_array_equal(_arr(cd.outgassing_map, n, np.float64), _arr(pd.outgassing_map, n, np.float64))
     finally:
         L.mfg_xml_close(h)
+
+
+def test_native_reader_old_formats(tmp_path):
+    """Files of older versions: parameters referred to by index only (no names), the reflection
+    given as a type (0 diffuse, 1 specular) instead of the diffuse/specular split, and a single
+    outgassing-map ratio; the C++ reader takes them like the Python reader."""
+    import re
+    L = _lib()
+    m, _, _ = golden_util.load("02-timedependent_with_two_parameters")
+    path = str(tmp_path / "old.xml")
+    xmlwriter.save(path, m)
+    text = open(path, encoding="utf-8").read()
+    text = re.sub(r' (stickingParam|opacityParam|outgassingParam|OutgassingParam)="[^"]*"', "", text)
+    text = re.sub(r' diffusePart="[^"]*" specularPart="[^"]*" cosineExponent="[^"]*"', "", text)
+    text = text.replace('<Reflection type="0"', '<Reflection type="1"', 3)   # three specular facets
+    open(path, "w", encoding="utf-8").write(text)
+    m2, _, _ = xmlio.load(path)
+    assert (m2.refl_specular == 1.0).sum() == 3
+    h = _open(L, path)
+    try:
+        _assert_desc_equal(L.mfg_xml_desc(h).contents, m2.desc())
+    finally:
+        L.mfg_xml_close(h)
