@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define MFG_ABI_VERSION 5u
+#define MFG_ABI_VERSION 6u
 
 /* ---- status codes (replace the reference's exceptions / MCStepResult,
  *      src/Simulation/Particle.h:24-28, src/Simulation/MolflowSimGeom.cpp:219-247) ---- */
@@ -285,6 +285,8 @@ typedef struct mfg_run_options {
     double   time_limit_s;       /* kernel self-stops after this wall time (status MFG_ERR_TIMEOUT), 0 = 600 s */
     uint64_t max_steps_per_particle; /* a particle that exceeds this many bounces is dropped and counted, 0 = 2^40 */
     int32_t  use_graph;          /* 1: launch through a captured CUDA graph (captured once per launch shape) */
+    int32_t  particles_per_request; /* particle ids a warp takes from the shared work queue per request,
+                                    32..65536; 0 = the autotuned choice (64 before mfg_autotune) */
 } mfg_run_options;
 
 /* Run statistics of the last run (filled by mfg_run / mfg_wait). */

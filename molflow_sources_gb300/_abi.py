@@ -1,7 +1,7 @@
 """ctypes mirrors of the C structs declared in include/mfg.h."""
 import ctypes as C
 
-MFG_ABI_VERSION = 5
+MFG_ABI_VERSION = 6
 LOG_N = 8   # particle log record: u, v, theta, phi, oriRatio, decay moment, time, speed
 
 MFG_OK = 0
@@ -175,6 +175,7 @@ class RunOptions(C.Structure):
         ("time_limit_s", C.c_double),
         ("max_steps_per_particle", C.c_uint64),
         ("use_graph", C.c_int32),
+        ("particles_per_request", C.c_int32),
     ]
 
 

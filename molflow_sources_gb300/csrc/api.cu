@@ -81,7 +81,7 @@ struct mfg_sim {
     unsigned char* d_run = nullptr;
     size_t run_bytes = 0;
     cudaGraphExec_t graph_exec = nullptr;
-    long long graph_key[5] = {-1, -1, -1, -1, -1};   // launch shape of the captured graph
+    long long graph_key[6] = {-1, -1, -1, -1, -1, -1};   // launch shape of the captured graph
     bool running = false;
     mfg_run_stats pending{};
     std::vector<unsigned long long> g_before;
@@ -91,6 +91,7 @@ struct mfg_sim {
     int tuned_block[2] = {0, 0};     // per precision, from mfg_autotune
     int tuned_bps[2] = {0, 0};
     int tuned_levels[2] = {0, 0};    // top BVH levels staged in shared memory (FP32R)
+    int tuned_chunk[2] = {0, 0};     // particle ids per work-queue request
     std::vector<double> sticking;    // current sticking per facet (mfg_update_sticking)
     // sensitivity state (mfg_sens_*)
     bool sens_ready = false;
@@ -568,6 +569,10 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     if (block > 256 && o.precision != MFG_PREC_FP32R)
         return fail(MFG_ERR_INVALID_ARGUMENT, "512- and 1024-thread blocks are compiled for FP32R only");
     if (o.smem_bvh_levels > 12) return fail(MFG_ERR_INVALID_ARGUMENT, "smem_bvh_levels is at most 12");
+    if (o.particles_per_request == 0) o.particles_per_request = s->tuned_chunk[o.precision] ? s->tuned_chunk[o.precision] : 64;
+    if (o.particles_per_request < 32 || o.particles_per_request > 65536)
+        return fail(MFG_ERR_INVALID_ARGUMENT, "particles_per_request must be 32..65536");
+    C.chunk = o.particles_per_request;
     const int bps_req = block == 512 ? 4 : (block == 1024 ? 2 : std::max(1, int(o.blocks_per_sm)));
     // moment-0 facet partials in shared memory when they fit the block's share of the SM (228 KB)
     const size_t fac_bytes = size_t(h.nf) * SF_N * 8;
@@ -622,8 +627,8 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
     s->t_start = std::chrono::steady_clock::now();
     if (o.use_graph && !sens) {
         // one captured graph per launch shape: [run descriptor copy, counter reset, tracer]
-        const long long key[5] = {variant, block, grid, C.n_top, (long long)dyn};
-        if (!s->graph_exec || !std::equal(key, key + 5, s->graph_key)) {
+        const long long key[6] = {variant, block, grid, C.n_top, (long long)dyn, C.chunk};
+        if (!s->graph_exec || !std::equal(key, key + 6, s->graph_key)) {
             if (s->graph_exec) { cudaGraphExecDestroy(s->graph_exec); s->graph_exec = nullptr; }
             cudaGraph_t g = nullptr;
             CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
@@ -634,7 +639,7 @@ static int launch_run(mfg_sim* s, const uint64_t* counts, const mfg_run_options*
             e = cudaGraphInstantiate(&s->graph_exec, g, 0);
             cudaGraphDestroy(g);
             if (e != cudaSuccess) { s->graph_exec = nullptr; return cuda_fail(e, "cudaGraphInstantiate"); }
-            std::copy(key, key + 5, s->graph_key);
+            std::copy(key, key + 6, s->graph_key);
         }
         CK(cudaEventRecord(s->ev0, s->stream));
         CK(cudaGraphLaunch(s->graph_exec, s->stream));
@@ -744,13 +749,14 @@ int mfg_autotune(mfg_sim* s, uint64_t n_trial, int32_t precision, uint64_t seed,
         shapes = {{256, 2}, {256, 3}, {256, 4}, {256, 6}, {256, 8}};
         if (!h.has_ext) { shapes.push_back({512, 4}); shapes.push_back({1024, 2}); }
     }
-    auto trial = [&](int block, int bps, int levels, double& rate) -> int {
+    auto trial = [&](int block, int bps, int levels, double& rate, int chunk = 64) -> int {
         mfg_run_options o{};
         o.precision = precision;
         o.seed = seed;
         o.block_size = block;
         o.blocks_per_sm = bps;
         o.smem_bvh_levels = levels;
+        o.particles_per_request = chunk;
         o.time_limit_s = 60;
         mfg_run_stats st{};
         for (int rep = 0; rep < 2; ++rep) {   // the second run is timed
@@ -783,9 +789,18 @@ int mfg_autotune(mfg_sim* s, uint64_t n_trial, int32_t precision, uint64_t seed,
                 if (rc != MFG_OK) return rc;
                 if (rate > best_rate) { best_rate = rate; best_shape = ranked[r].second; best_levels = levels; }
             }
+    // stage 3: particles per work-queue request at the chosen shape (64 is the default)
+    int best_chunk = 64;
+    for (int chunk : {32, 256}) {
+        double rate = 0;
+        int rc = trial(shapes[best_shape].first, shapes[best_shape].second, best_levels, rate, chunk);
+        if (rc != MFG_OK) return rc;
+        if (rate > best_rate) { best_rate = rate; best_chunk = chunk; }
+    }
     s->tuned_block[precision] = shapes[best_shape].first;
     s->tuned_bps[precision] = shapes[best_shape].second;
     s->tuned_levels[precision] = best_levels;
+    s->tuned_chunk[precision] = best_chunk;
     if (best) {
         *best = mfg_run_options{};
         best->precision = precision;
@@ -793,6 +808,7 @@ int mfg_autotune(mfg_sim* s, uint64_t n_trial, int32_t precision, uint64_t seed,
         best->block_size = shapes[best_shape].first;
         best->blocks_per_sm = shapes[best_shape].second;
         best->smem_bvh_levels = best_levels;
+        best->particles_per_request = best_chunk;
     }
     return mfg_reset(s);
 }

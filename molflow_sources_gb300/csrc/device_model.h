@@ -317,5 +317,6 @@ struct LaunchCtl {
     const volatile int* abort_flag;          // host-mapped
     int smem_facets;                         // 1: moment-0 facet partials in shared memory
     int n_top;                               // FP32 BVH nodes [0, n_top) staged in shared memory
+    int chunk;                               // particle ids a warp takes per work-queue request (>= 32)
     SensCtl sens;                            // used by the sensitivity variant
 };

@@ -789,7 +789,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) trace_kernel(const __grid_
     const int lane = threadIdx.x & 31;
     const unsigned lane_lt = (1u << lane) - 1u;
     unsigned long long pool_next = 0, pool_end = 0;   // warp pool of particle ids
-    const unsigned long long chunk = 64;
+    const unsigned long long chunk = (unsigned long long)C.chunk;   // >= 32: one request serves a warp
 
     const unsigned long long n_total = C.run->n_total;
     const unsigned long long max_steps = C.run->max_steps;

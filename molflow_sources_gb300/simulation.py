@@ -210,13 +210,14 @@ class GpuSimulation:
 
     # --- ParticleTracer surface (Particle.h:45,86) ---
     def SimulationMCStep(self, n_desorptions, precision=A.PREC_FP64, seed=0x4D6F6C66, block_size=0,
-                         blocks_per_sm=0, time_limit_s=0.0, max_steps=0, use_graph=False, smem_bvh_levels=0):
+                         blocks_per_sm=0, time_limit_s=0.0, max_steps=0, use_graph=False, smem_bvh_levels=0,
+                         particles_per_request=0):
         """Desorb and trace n_desorptions particles on the GPU (blocking)."""
         if not time_limit_s:
             time_limit_s = float(os.environ.get("MFG_TIME_LIMIT_S", "0"))
         o = A.RunOptions(precision=precision, seed=seed, block_size=block_size, blocks_per_sm=blocks_per_sm,
                          time_limit_s=time_limit_s, max_steps_per_particle=max_steps, use_graph=int(use_graph),
-                         smem_bvh_levels=smem_bvh_levels)
+                         smem_bvh_levels=smem_bvh_levels, particles_per_request=particles_per_request)
         st = A.RunStats()
         rc = load_library().mfg_run(self.h, int(n_desorptions), C.byref(o), C.byref(st))
         self.last_stats = {f: getattr(st, f) for f, _ in A.RunStats._fields_}
@@ -235,7 +236,8 @@ class GpuSimulation:
         """Pick the fastest launch shape for this model (clears tallies); returns it as a dict."""
         o = A.RunOptions()
         _check(load_library().mfg_autotune(self.h, int(n_trial), precision, seed, C.byref(o)))
-        return {"block_size": o.block_size, "blocks_per_sm": o.blocks_per_sm, "smem_bvh_levels": o.smem_bvh_levels}
+        return {"block_size": o.block_size, "blocks_per_sm": o.blocks_per_sm, "smem_bvh_levels": o.smem_bvh_levels,
+                "particles_per_request": o.particles_per_request}
 
     def run_async(self, n_desorptions, precision=A.PREC_FP64, seed=0x4D6F6C66, time_limit_s=0.0):
         o = A.RunOptions(precision=precision, seed=seed, time_limit_s=time_limit_s)
@@ -334,7 +336,7 @@ class GpuBatch:
         self.last_stats = None
 
     def run(self, counts, precision=A.PREC_FP32R, seed=0x4D6F6C66, use_graph=False, time_limit_s=0.0,
-            block_size=0, blocks_per_sm=0, smem_bvh_levels=0):
+            block_size=0, blocks_per_sm=0, smem_bvh_levels=0, particles_per_request=0):
         """counts: particles per instance (int applies to all)."""
         if np.isscalar(counts):
             counts = [int(counts)] * len(self.models)
@@ -342,7 +344,8 @@ class GpuBatch:
         if not time_limit_s:
             time_limit_s = float(os.environ.get("MFG_TIME_LIMIT_S", "0"))
         o = A.RunOptions(precision=precision, seed=seed, block_size=block_size, blocks_per_sm=blocks_per_sm,
-                         time_limit_s=time_limit_s, use_graph=int(bool(use_graph)), smem_bvh_levels=smem_bvh_levels)
+                         time_limit_s=time_limit_s, use_graph=int(bool(use_graph)), smem_bvh_levels=smem_bvh_levels,
+                         particles_per_request=particles_per_request)
         st = A.RunStats()
         rc = load_library().mfg_run_batch(self.h, A.ptr(c, C.c_uint64), C.byref(o), C.byref(st))
         self.last_stats = {f: getattr(st, f) for f, _ in A.RunStats._fields_}
@@ -353,7 +356,8 @@ class GpuBatch:
         """Fastest launch shape for the batch (n_trial particles per instance per trial); clears tallies."""
         o = A.RunOptions()
         _check(load_library().mfg_autotune(self.h, int(n_trial), precision, seed, C.byref(o)))
-        return {"block_size": o.block_size, "blocks_per_sm": o.blocks_per_sm, "smem_bvh_levels": o.smem_bvh_levels}
+        return {"block_size": o.block_size, "blocks_per_sm": o.blocks_per_sm, "smem_bvh_levels": o.smem_bvh_levels,
+                "particles_per_request": o.particles_per_request}
 
     def fetch_instance(self, i):
         st = SimuState(self.models[i])

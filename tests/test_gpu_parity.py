@@ -250,25 +250,29 @@ def test_kernel_time_limit_returns_status_and_context_survives():
 
 
 def test_autotune_and_occupancy_variants_agree(tube):
-    """Every launch shape (block size, register budget, BVH levels staged in shared memory) gives
-    identical FP32R tallies for the same particles."""
+    """Every launch shape (block size, register budget, BVH levels staged in shared memory, particles
+    per work-queue request) gives identical FP32R tallies for the same particles."""
     sim = GpuSimulation(tube)
     ref = None
-    shapes = [(256, b, -1) for b in (2, 3, 4, 6, 8)] + [(512, 4, -1), (1024, 2, -1), (256, 8, 5), (256, 8, 9),
-                                                       (1024, 2, 7), (1024, 2, 12)]
-    for block, bps, lv in shapes:
+    shapes = [(256, b, -1, 0) for b in (2, 3, 4, 6, 8)] + [(512, 4, -1, 0), (1024, 2, -1, 0), (256, 8, 5, 0),
+                                                          (256, 8, 9, 0), (1024, 2, 7, 0), (1024, 2, 12, 0),
+                                                          (1024, 2, -1, 32), (256, 4, -1, 256), (1024, 2, -1, 65536)]
+    for block, bps, lv, ppr in shapes:
         sim.ResetSimulation()
         sim.set_particle_offset(0)
         sim.SimulationMCStep(20000, precision=A.PREC_FP32R, seed=SEED, block_size=block, blocks_per_sm=bps,
-                             smem_bvh_levels=lv)
+                             smem_bvh_levels=lv, particles_per_request=ppr)
         st = sim.fetch()
         if ref is None:
             ref = st
-        assert np.array_equal(st.facet_counts, ref.facet_counts), (block, bps, lv)
-        assert np.array_equal(st.texture, ref.texture), (block, bps, lv)
+        assert np.array_equal(st.facet_counts, ref.facet_counts), (block, bps, lv, ppr)
+        assert np.array_equal(st.texture, ref.texture), (block, bps, lv, ppr)
+    with pytest.raises(MfgError):
+        sim.SimulationMCStep(100, precision=A.PREC_FP32R, seed=SEED, particles_per_request=16)
     best = sim.autotune(20000)
-    assert (best["block_size"], best["blocks_per_sm"]) in [(b, k) for b, k, _ in shapes]
+    assert (best["block_size"], best["blocks_per_sm"]) in [(b, k) for b, k, _, _ in shapes]
     assert best["smem_bvh_levels"] in (-1, 5, 7, 9)
+    assert best["particles_per_request"] in (32, 64, 256)
     assert sim.fetch().n_desorbed == 0
     # the tuned shape is the default afterwards
     sim.SimulationMCStep(20000, precision=A.PREC_FP32R, seed=SEED)
