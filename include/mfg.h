@@ -345,6 +345,13 @@ int32_t mfg_xml_has_results(const mfg_xml* file);
  * created from mfg_xml_desc of the same file: every array of the view is cleared, then filled. */
 int mfg_xml_read_state(const mfg_xml* file, const mfg_model* model, mfg_state_view* out);
 void mfg_xml_close(mfg_xml* file);
+/* GlobalSimuState::Compare (MolflowSimGeom.cpp:559-1148), the test suite's acceptance rule (called
+ * with 0.009 and 0.07, tests/testsuite.cpp:460): two results laid out for `model` (every array of its
+ * layout present) -> counts[0..2] = global, facet and fine error counts (facet and fine -1 when the
+ * states have no desorptions); a run passes when the first two are 0.  `messages` (may be NULL)
+ * receives one line per difference, global and facet ones first, cut to buflen - 1 bytes. */
+int mfg_compare_states(const mfg_model* model, const mfg_state_view* a, const mfg_state_view* b, double glob_threshold,
+                       double loc_threshold, int64_t counts[3], char* messages, size_t buflen);
 /* SaveGeometry + SaveSimulationState (WriterXML.cpp:72-903): the model `desc` (as `model` was created
  * from it) and the results in `state` (a view laid out for `model`; NULL: geometry and settings only)
  * as a MolFlow+ file; a path ending in ".zip" gets one stored .xml entry.  `param_names`: n_params

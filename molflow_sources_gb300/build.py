@@ -14,9 +14,9 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libmfg.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["api.cu", "model_build.cpp", "xml_file.cpp", "xml_model.cpp", "xml_writer.cpp"]
+SOURCES = ["api.cu", "model_build.cpp", "xml_file.cpp", "xml_model.cpp", "xml_writer.cpp", "compare.cpp"]
 DEPS = SOURCES + ["trace_kernels.cuh", "traversal.cuh", "philox.cuh", "anglemap_gen.cuh", "device_model.h",
-                  "model_build.h", "xml_file.h", "xml_model.h", "xml_writer.h"]
+                  "model_build.h", "xml_file.h", "xml_model.h", "xml_writer.h", "compare.h"]
 
 
 def nvcc():

@@ -21,6 +21,7 @@
 #include "trace_kernels.cuh"
 #include "xml_model.h"
 #include "xml_writer.h"
+#include "compare.h"
 
 namespace {
 
@@ -223,6 +224,28 @@ int mfg_xml_read_state(const mfg_xml* file, const mfg_model* model, mfg_state_vi
 }
 
 void mfg_xml_close(mfg_xml* file) { delete file; }
+
+int mfg_compare_states(const mfg_model* model, const mfg_state_view* a, const mfg_state_view* b, double glob_threshold,
+                       double loc_threshold, int64_t counts[3], char* messages, size_t buflen) {
+    if (!model || !a || !b || !counts) return fail(MFG_ERR_INVALID_ARGUMENT, "null argument");
+    const mfg_state_layout& L = model->h.layout;
+    for (const mfg_state_view* v : {a, b})
+        if (!v->global || !v->facet_counts || !v->facet_sums || (L.n_texture && !v->texture) || (L.n_profile && !v->profile) ||
+            (L.n_direction && !v->direction) || (L.n_histogram && !v->histogram))
+            return fail(MFG_ERR_INVALID_ARGUMENT, "a compared view lacks an array of the model's layout");
+    const mfgx::CompareResult r = mfgx::compare_states(model->h, *a, *b, glob_threshold, loc_threshold);
+    counts[0] = r.global;
+    counts[1] = r.facet;
+    counts[2] = r.fine;
+    if (messages && buflen) {
+        std::string all;
+        for (const std::string& m : r.messages) { all += m; all += '\n'; }
+        const size_t n = std::min(all.size(), buflen - 1);
+        std::memcpy(messages, all.data(), n);
+        messages[n] = '\0';
+    }
+    return MFG_OK;
+}
 
 int mfg_xml_save(const char* path, const mfg_model_desc* desc, const mfg_model* model, const mfg_state_view* state,
                  const char* const* param_names) {
