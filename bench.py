@@ -557,6 +557,7 @@ def main():
     achieved = (hits / args.steps) * bph / mean_launch_s / 1e9
     traffic = None
     l2 = None
+    warp_eff = None
     tp = os.path.join(ROOT, "profiles", "traffic_%s.json" % args.workload)
     if os.path.exists(tp):
         with open(tp) as f:
@@ -574,6 +575,11 @@ def main():
                   "peak_kind": "ncu: the capture's L2 bytes per second over its lts__throughput fraction",
                   "ncu_l2_throughput_pct_of_peak": tj["l2_throughput_pct"],
                   "ncu_l1_throughput_pct_of_peak": tj.get("l1_throughput_pct")}
+        if tj.get("threads_per_warp_instruction"):
+            # warp execution efficiency of the captured launch: active threads per issued warp instruction
+            warp_eff = {"threads_per_instruction": tj["threads_per_warp_instruction"],
+                        "efficiency": tj["threads_per_warp_instruction"] / 32.0,
+                        "source": "ncu smsp__thread_inst_executed_per_inst_executed.ratio"}
     cpu = None if args.no_cpu_baseline else cpu_baseline(model)
     others = other_workloads(torch, local) if (args.workload == "c2" and world == 1 and not args.no_others) else None
     L = model.layout()
@@ -600,7 +606,7 @@ def main():
         "model_load_s": load_s,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "bytes_per_hit": bph, "nodes_per_ray": nodes, "facets_per_ray": prims,
-                     "peak_kind": peak_kind, "l2": l2,
+                     "peak_kind": peak_kind, "l2": l2, "warp_execution": warp_eff,
                      "limiter": "L1/TEX throughput and load latency: the L1 is the busiest unit (74 % of its peak "
                                 "on the beam chamber, with 2.3 local-memory requests, stack and spills, per global one), "
                                 "issue slots 49 %, L2 41 %, DRAM 26 % of their peaks"},
