@@ -27,10 +27,11 @@ struct TravStack {
 
 // One 32-byte read-only load (two float4) per thread: half the L1 requests of two 16-byte loads
 // for the scattered BVH node fetches (+3 % hits/s on the beam chamber, +2 % on the tube, +8 % for
-// the traversal alone).  MFG_NO_V8 builds the two 16-byte loads instead.
+// the traversal alone), with the hint to keep the nodes in L1 and L2 ahead of the spilled
+// registers and stacks (+0.5 %).  MFG_NO_V8 builds the two 16-byte loads instead.
 __device__ __forceinline__ void ldg_v8(const void* p, float4& a, float4& b) {
 #if defined(__CUDA_ARCH__) && !defined(MFG_NO_V8)
-    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+    asm("ld.global.nc.L1::evict_last.L2::evict_last.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
         : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w) : "l"(p));
 #else
     a = __ldg(reinterpret_cast<const float4*>(p));
