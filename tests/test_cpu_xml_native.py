@@ -190,7 +190,7 @@ def test_native_reader_parameter_catalog(tmp_path):
     cat = tmp_path / "catalog"
     cat.mkdir()
     (cat / "b_rate.csv").write_text("0.002, 0.5\n0.001,0.25\n\n0.003,0.75\n")
-    (cat / "a_temp.csv").write_text("﻿0,300\n1,400\n")
+    (cat / "a_temp.csv").write_text("\ufeff0,300\n1,400\n")   # with a byte-order mark
     m, _, _ = golden_util.load("02-timedependent_with_two_parameters")
     path = str(tmp_path / "m.xml")
     xmlwriter.save(path, m)
