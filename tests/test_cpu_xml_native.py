@@ -334,3 +334,31 @@ def test_native_reader_old_formats(tmp_path):
         _assert_desc_equal(L.mfg_xml_desc(h).contents, m2.desc())
     finally:
         L.mfg_xml_close(h)
+
+
+def test_native_reader_xml_syntax(tmp_path):
+    """The XML forms a file may use: a declaration, comments, CDATA text, character and entity
+    references in attributes, single-quoted attributes, self-closing and empty elements."""
+    L = _lib()
+    m, _, _ = golden_util.load("B02-lr10_pipe_tex")
+    path = str(tmp_path / "s.xml")
+    xmlwriter.save(path, m)
+    text = open(path, encoding="utf-8").read()
+    text = text.replace("<Geometry>", "<!-- a comment <Geometry> -->\n<Geometry>", 1)
+    text = text.replace('<Vertex id="0" x="', "<Vertex id='0' x=\"", 1)
+    text = text.replace('<Structure id="0" name="structure 1" />',
+                        '<Structure id="0" name="&lt;main&gt; &amp; &#233;&#x41;"></Structure>', 1)
+    text = text.replace("<Interface />", "<Interface><![CDATA[ <not> parsed & kept ]]></Interface>", 1)
+    for form in ("<!-- a comment", "<Vertex id='0'", "&#x41;", "<![CDATA["):
+        assert form in text, form
+    open(path, "w", encoding="utf-8").write(text)
+    m2, _, _ = xmlio.load(path)
+    h = _open(L, path)
+    try:
+        _assert_desc_equal(L.mfg_xml_desc(h).contents, m2.desc())
+    finally:
+        L.mfg_xml_close(h)
+    bad = tmp_path / "bad2.xml"
+    bad.write_text("<A><B x=1/></A>")
+    with pytest.raises(MfgError, match="unquoted"):
+        _open(L, str(bad))
