@@ -346,7 +346,7 @@ __device__ __forceinline__ void polar_dir(const DevModel& M, int f, R ct, R r2, 
 }
 
 // Desorption time from a facet's integrated desorption table (Physics.cpp:11-19)
-__device__ __noinline__ double desorption_time(const DevModel& M, int idt, double r) {
+__device__ __forceinline__ double desorption_time(const DevModel& M, int idt, double r) {
     int s = M.id_start[idt], e = M.id_start[idt + 1];
     return interp_x_d(r * M.id_cum[e - 1], M.id_t + s, M.id_cum + s, e - s);
 }
@@ -683,11 +683,12 @@ __device__ __noinline__ void teleport_to(const DevModel& M, const DevTally& T, c
 
 // General relaunch (any accommodation, temperature parameter, sojourn time, reflection
 // mix): UpdateVelocity, sojourn, diffuse / specular / cos^N direction, with the random
-// numbers drawn in the order of PerformBounce (Particle.cpp:769-802).
+// numbers drawn in the order of PerformBounce (Particle.cpp:769-802).  Inlined: +3 to +5 %
+// hits/s on the 200k-facet chamber and the 1000-facet tube against a call.
 template <bool kFP32, class Rng, class R>
-__device__ __noinline__ void reflect_general(const DevModel& M, int fo, bool flip, Rng& rng, double& time, R& vel,
-                                             R& dx, R& dy, R& dz, const double* cv, const double* cp,
-                                             const float* cvf, const float* cpf) {
+__device__ __forceinline__ void reflect_general(const DevModel& M, int fo, bool flip, Rng& rng, double& time, R& vel,
+                                                R& dx, R& dy, R& dz, const double* cv, const double* cp,
+                                                const float* cvf, const float* cpf) {
     const FacetInfo& In = M.info[fo];
     const FacetPhysD& Ph = M.phys_d[fo];
     const FacetIsectD& Rr = M.isect_d[fo];
