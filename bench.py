@@ -607,9 +607,9 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "bytes_per_hit": bph, "nodes_per_ray": nodes, "facets_per_ray": prims,
                      "peak_kind": peak_kind, "l2": l2, "warp_execution": warp_eff,
-                     "limiter": "L1/TEX throughput and load latency: the L1 is the busiest unit (66 % of its peak "
+                     "limiter": "L1/TEX throughput and load latency: the L1 is the busiest unit (67 % of its peak "
                                 "on the beam chamber, with 3.2 local-memory requests, stack and spills, per global one), "
-                                "issue slots 50 %, L2 40 %, DRAM about 25 % of their peaks"},
+                                "issue slots 52 %, L2 40 %, DRAM about 22 % of their peaks"},
         "clocks": clocks,
         "cpu_baseline": cpu,
         "other_workloads": others,

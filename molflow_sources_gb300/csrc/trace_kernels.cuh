@@ -684,7 +684,8 @@ __device__ __noinline__ void teleport_to(const DevModel& M, const DevTally& T, c
 // General relaunch (any accommodation, temperature parameter, sojourn time, reflection
 // mix): UpdateVelocity, sojourn, diffuse / specular / cos^N direction, with the random
 // numbers drawn in the order of PerformBounce (Particle.cpp:769-802).  Inlined: +3 to +5 %
-// hits/s on the 200k-facet chamber and the 1000-facet tube against a call.
+// hits/s on a 200k-facet chamber and on a 66-facet tube against a call (the register allocation
+// of the whole loop, also where this law never runs).
 template <bool kFP32, class Rng, class R>
 __device__ __forceinline__ void reflect_general(const DevModel& M, int fo, bool flip, Rng& rng, double& time, R& vel,
                                                 R& dx, R& dy, R& dz, const double* cv, const double* cp,
