@@ -8,7 +8,7 @@ facet counts are 0; "fine" differences (textures, profiles, directions, facet hi
 reported only.  The sample-size cut-offs (6400 counts for histogram bins and facet counters,
 40000 Monte Carlo hits per facet and moment, 100 for a smoothed profile bin, 640 for a texture
 cell), the per-moment threshold max(local, 1/sqrt(hits)), the 40x looser velocity thresholds and
-the scales are the reference's, so that a result judged here is judged as the suite would.
+the scales are the reference's, so that a result accepted here is accepted by the suite too.
 
 Restated details of the reference:
 * IsEqual(a, b, tol) lives in the absent shared MathTools; it is taken as a relative comparison,
