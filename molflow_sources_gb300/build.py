@@ -1,8 +1,8 @@
 """Build the CUDA library in-tree: molflow_sources_gb300/_build/libmfg.so (sm_103a).
 
-Two translation units compiled in parallel with nvcc (the host-side model
-builder as plain C++, the kernels + C ABI as CUDA), linked with the static
-CUDA runtime.  No cmake.
+Six translation units compiled in parallel with nvcc (the kernels + C ABI as
+CUDA; the host-side model builder, the XML/ZIP reader and writer and the
+results comparison as plain C++), linked with the static CUDA runtime.  No cmake.
 """
 import os
 import shutil
