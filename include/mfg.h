@@ -42,6 +42,10 @@ extern "C" {
 #define MFG_ERR_NO_DEVICE            9
 #define MFG_ERR_LIMIT               10  /* a size exceeds a documented limit */
 
+/* Size limits of a model (MFG_ERR_LIMIT past them): structures; texture, direction and angle-map
+ * cells and histogram bins of one moment block, each at most 2^31-1 (32-bit device offsets). */
+#define MFG_MAX_STRUCTURES       65536
+
 /* desorption types, src/MolflowTypes.h:17-21 */
 #define MFG_DES_NONE      0
 #define MFG_DES_UNIFORM   1
@@ -158,7 +162,7 @@ typedef struct mfg_model_desc {
     double   half_life;                /* sp.halfLife s */
     int32_t  low_flux_mode;            /* otfParams.lowFluxMode */
     double   low_flux_cutoff;          /* otfParams.lowFluxCutoff */
-    int32_t  n_structures;             /* sh.nbSuper (>=1) */
+    int32_t  n_structures;             /* sh.nbSuper (>=1, at most MFG_MAX_STRUCTURES) */
 
     /* time moments (tdParams.moments): centre and window, sorted by centre */
     int32_t  n_moments;

@@ -15,6 +15,7 @@ MFG_ERR_INVALID_ARGUMENT = 7
 MFG_ERR_BUSY = 8
 MFG_ERR_NO_DEVICE = 9
 MFG_ERR_LIMIT = 10
+MFG_MAX_STRUCTURES = 65536
 
 STATUS_NAMES = {
     0: "MFG_OK", 1: "MFG_ERR_INVALID_MODEL", 2: "MFG_ERR_NO_SOURCE", 3: "MFG_ERR_TIMEOUT",

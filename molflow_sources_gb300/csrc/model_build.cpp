@@ -377,6 +377,7 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     const int nf = d->n_facets;
     m.nf = nf;
     m.nstruct = d->n_structures > 0 ? d->n_structures : 1;
+    if (m.nstruct > MFG_MAX_STRUCTURES) { err = "more than " + std::to_string(MFG_MAX_STRUCTURES) + " structures"; return MFG_ERR_LIMIT; }
     m.facets.resize(nf);
     const int32_t* fs = d->facet_vertex_start;
     if (fs[0] != 0) { err = "facet_vertex_start[0] must be 0"; return MFG_ERR_INVALID_MODEL; }
@@ -658,7 +659,13 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     L.n_moments = m.nm;
     m.tex_off.assign(nf, -1); m.dir_off.assign(nf, -1); m.ang_off.assign(nf, -1); m.prof_idx.assign(nf, -1);
     m.tex_w.assign(nf, 0); m.tex_h.assign(nf, 0);
+    // the device addresses texture, direction and angle-map cells with 32-bit offsets
+    constexpr int64_t kMaxCells = 2147483647;
     for (int i = 0; i < nf; ++i) {
+        if (!(m.texw_p[i] >= 0 && m.texh_p[i] >= 0 && m.texw_p[i] < double(kMaxCells) && m.texh_p[i] < double(kMaxCells))) {
+            err = "texture size out of range on facet " + std::to_string(i + 1);
+            return MFG_ERR_INVALID_MODEL;
+        }
         if (m.texw_p[i] * m.texh_p[i] > 0) {
             m.tex_w[i] = std::max(1, int(std::ceil(m.texw_p[i] - 1e-9)));
             m.tex_h[i] = std::max(1, int(std::ceil(m.texh_p[i] - 1e-9)));
@@ -671,7 +678,11 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
         if (m.profile_type[i] != MFG_PROFILE_NONE) m.prof_idx[i] = L.profile_facets++;
         if (m.am_record[i] && m.am_phi[i] > 0 && m.am_lo[i] >= 0 && m.am_hi[i] >= 0 && m.am_lo[i] + m.am_hi[i] > 0) {
             m.ang_off[i] = L.anglemap_cells;
-            L.anglemap_cells += int64_t(m.am_phi[i]) * (m.am_lo[i] + m.am_hi[i]);
+            L.anglemap_cells += int64_t(m.am_phi[i]) * (int64_t(m.am_lo[i]) + m.am_hi[i]);
+        }
+        if (L.texture_cells > kMaxCells || L.direction_cells > kMaxCells || L.anglemap_cells > kMaxCells) {
+            err = "more than 2^31-1 texture, direction or angle-map cells (at facet " + std::to_string(i + 1) + ")";
+            return MFG_ERR_LIMIT;
         }
     }
     const int64_t B = 1 + m.nm;
@@ -693,9 +704,13 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
             if (m.desorb_type[i] != MFG_DES_ANGLEMAP) continue;
             if (m.am_of_facet.empty()) m.am_of_facet.assign(nf, -1);
             const int w = m.am_phi[i], lo = m.am_lo[i], hi = m.am_hi[i];
-            if (!(w > 0 && lo >= 0 && hi >= 0 && lo + hi > 0) || !d->desorb_anglemap) {
+            if (!(w > 0 && lo >= 0 && hi >= 0 && int64_t(lo) + hi > 0) || !d->desorb_anglemap) {
                 err = "facet " + std::to_string(i + 1) + " desorbs by angle map but has no recorded angle map";
                 return MFG_ERR_INVALID_MODEL;
+            }
+            if (2 * int64_t(w) * (int64_t(lo) + hi) + (int64_t(lo) + hi) + 8 + int64_t(m.am_pool.size()) > kMaxCells) {
+                err = "facet " + std::to_string(i + 1) + ": angle-map desorption tables past 2^31-1 entries";
+                return MFG_ERR_LIMIT;
             }
             const uint64_t* pdf = d->desorb_anglemap + cursor;
             cursor += size_t(w) * (lo + hi);
@@ -748,27 +763,48 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     }
     // histograms: global set at offset 0, then each recording facet's (bounce, distance, time);
     // bin counts restated from the sizes the reference stores with its histograms
-    auto hist_of = [](const mfg_histogram_params& p, HistDev& h) {
+    // (false for a bin size that is not positive or a bin count past 2^30)
+    auto hist_of = [](const mfg_histogram_params& p, HistDev& h) -> bool {
         h = HistDev{};
         h.off = -1;
         h.record = p.record;
-        if (!p.record) return;
+        if (!p.record) return true;
+        constexpr double kMaxBins = 1073741824.0;
         h.bounce_bin = p.bounce_binsize ? p.bounce_binsize : 1;
         h.dist_bin = p.distance_binsize;
         h.time_bin = p.time_binsize;
-        if (p.record & MFG_HIST_BOUNCE) h.nb = int32_t(p.bounce_max / h.bounce_bin + 2);
-        if (p.record & MFG_HIST_DISTANCE) h.nd = int32_t(size_t(p.distance_max / p.distance_binsize) + 1);
-        if (p.record & MFG_HIST_TIME) h.nt = int32_t(size_t(p.time_max / p.time_binsize) + 1);
+        if (p.record & MFG_HIST_BOUNCE) {
+            if (double(p.bounce_max / h.bounce_bin) >= kMaxBins) return false;
+            h.nb = int32_t(p.bounce_max / h.bounce_bin + 2);
+        }
+        if (p.record & MFG_HIST_DISTANCE) {
+            const double n = p.distance_max / p.distance_binsize;
+            if (!(p.distance_binsize > 0 && p.distance_max >= 0 && n < kMaxBins)) return false;
+            h.nd = int32_t(size_t(n) + 1);
+        }
+        if (p.record & MFG_HIST_TIME) {
+            const double n = p.time_max / p.time_binsize;
+            if (!(p.time_binsize > 0 && p.time_max >= 0 && n < kMaxBins)) return false;
+            h.nt = int32_t(size_t(n) + 1);
+        }
+        return true;
     };
     int64_t hb = 0;
-    hist_of(d->global_histogram, m.ghist);
-    if (m.ghist.record) { m.ghist.off = 0; hb = m.ghist.nb + m.ghist.nd + m.ghist.nt; }
+    if (!hist_of(d->global_histogram, m.ghist)) { err = "global histogram: bin size or range out of range"; return MFG_ERR_INVALID_MODEL; }
+    if (m.ghist.record) { m.ghist.off = 0; hb = int64_t(m.ghist.nb) + m.ghist.nd + m.ghist.nt; }
     m.fhist.clear();
     if (d->facet_histogram) {
         m.fhist.resize(nf);
         for (int i = 0; i < nf; ++i) {
-            hist_of(d->facet_histogram[i], m.fhist[i]);
-            if (m.fhist[i].record) { m.fhist[i].off = int32_t(hb); hb += m.fhist[i].nb + m.fhist[i].nd + m.fhist[i].nt; }
+            if (!hist_of(d->facet_histogram[i], m.fhist[i])) {
+                err = "histogram of facet " + std::to_string(i + 1) + ": bin size or range out of range";
+                return MFG_ERR_INVALID_MODEL;
+            }
+            if (m.fhist[i].record) {
+                m.fhist[i].off = int32_t(hb);
+                hb += int64_t(m.fhist[i].nb) + m.fhist[i].nd + m.fhist[i].nt;
+                if (hb > kMaxCells) { err = "more than 2^31-1 histogram bins (at facet " + std::to_string(i + 1) + ")"; return MFG_ERR_LIMIT; }
+            }
         }
     }
     L.histogram_bins = hb;

@@ -9,6 +9,7 @@
 #include "xml_model.h"
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdlib>
 #include <cstdio>
@@ -38,6 +39,16 @@ double fa(const XNode* n, const char* a, double def = 0.0) {
 long long ia(const XNode* n, const char* a, long long def = 0) {
     const char* v = n ? n->attr(a) : nullptr;
     return v ? to_i(v) : def;
+}
+// integer attribute clamped to the 32-bit range of the descriptor's fields
+int32_t ia32(const XNode* n, const char* a, long long def = 0) {
+    return int32_t(std::min<long long>(std::max<long long>(ia(n, a, def), INT32_MIN), INT32_MAX));
+}
+// count stored as a number: not a number or negative -> 0, past 2^64 -> 2^64-1
+uint64_t to_u64(double v) {
+    if (!(v > 0)) return 0;
+    if (v >= 18446744073709551615.0) return UINT64_MAX;
+    return uint64_t(v);
 }
 const XNode* kid(const XNode* n, const char* tag) { return n ? n->child(tag) : nullptr; }
 
@@ -196,7 +207,7 @@ bool XmlModel::load(const std::string& path, std::string& err, const char* catal
     for (const XNode* f : facets) {
         const XNode* ind = f->child("Indices");
         if (ind)
-            for (const XNode* i : ind->children("Indice")) fv_index.push_back(int32_t(ia(i, "vertex")));
+            for (const XNode* i : ind->children("Indice")) fv_index.push_back(ia32(i, "vertex"));
         fv_start.push_back(int32_t(fv_index.size()));
     }
     // reference defaults (MolflowSimulationModel / facet settings)
@@ -256,7 +267,7 @@ bool XmlModel::load(const std::string& path, std::string& err, const char* catal
             out = int32_t(it - param_names.begin());
             return true;
         }
-        out = int32_t(ia(n, "parameterId", -1));
+        out = ia32(n, "parameterId", -1);
         return true;
     };
 
@@ -279,7 +290,7 @@ bool XmlModel::load(const std::string& path, std::string& err, const char* catal
         is_2sided[k] = uint8_t(ia(op, "is2sided"));
         outgassing[k] = fa(og, "constValue");
         if (!param_ref(og, "OutgassingParam", outgassing_param[k])) return false;
-        desorb_type[k] = int32_t(ia(og, "desType"));
+        desorb_type[k] = ia32(og, "desType");
         desorb_exponent[k] = fa(og, "desExponent");
         temperature[k] = fa(te, "value", 293.15);
         if (!param_ref(te, "tempParam", temperature_param[k])) return false;
@@ -296,18 +307,18 @@ bool XmlModel::load(const std::string& path, std::string& err, const char* catal
         enable_sojourn[k] = uint8_t(ia(rf, "enableSojournTime"));
         sojourn_freq[k] = fa(rf, "sojournFreq");
         sojourn_e[k] = fa(rf, "sojournE");
-        structure[k] = int32_t(ia(su, "inStructure"));
-        link_dest[k] = int32_t(ia(su, "linksTo"));
-        teleport_dest[k] = int32_t(ia(f->child("Teleport"), "target"));
+        structure[k] = ia32(su, "inStructure");
+        link_dest[k] = ia32(su, "linksTo");
+        teleport_dest[k] = ia32(f->child("Teleport"), "target");
         is_moving[k] = uint8_t(ia(f->child("Motion"), "isMoving"));
         if (rec) {
-            profile_type[k] = int32_t(ia(rec->child("Profile"), "type"));
+            profile_type[k] = ia32(rec->child("Profile"), "type");
             if (const XNode* am = rec->child("IncidentAngleMap")) {
                 am_record[k] = uint8_t(ia(am, "record"));
-                am_phi_width[k] = int32_t(ia(am, "phiWidth"));
+                am_phi_width[k] = ia32(am, "phiWidth");
                 am_theta_limit[k] = fa(am, "thetaLimit", 1.570796326);
-                am_lower[k] = int32_t(ia(am, "thetaLowerRes"));
-                am_higher[k] = int32_t(ia(am, "thetaHigherRes"));
+                am_lower[k] = ia32(am, "thetaLowerRes");
+                am_higher[k] = ia32(am, "thetaHigherRes");
             }
         }
         // a recorded angle map in the facet node sets the map parameters and is the source of
@@ -315,10 +326,10 @@ bool XmlModel::load(const std::string& path, std::string& err, const char* catal
         // (LoaderXML.cpp:1043-1073)
         const XNode* gam = f->child("IncidentAngleMap");
         if (gam && gam->child("map") && gam->attr("angleMapThetaLimit")) {
-            am_phi_width[k] = int32_t(ia(gam, "angleMapPhiWidth"));
+            am_phi_width[k] = ia32(gam, "angleMapPhiWidth");
             am_theta_limit[k] = fa(gam, "angleMapThetaLimit");
-            am_lower[k] = int32_t(ia(gam, "angleMapThetaLowerRes"));
-            am_higher[k] = int32_t(ia(gam, "angleMapThetaHigherRes"));
+            am_lower[k] = ia32(gam, "angleMapThetaLowerRes");
+            am_higher[k] = ia32(gam, "angleMapThetaHigherRes");
             if (desorb_type[k] == MFG_DES_ANGLEMAP) numbers(gam->child("map")->text, am_maps[k]);
         } else if (desorb_type[k] == MFG_DES_ANGLEMAP) {
             desorb_type[k] = MFG_DES_NONE;
@@ -354,8 +365,13 @@ bool XmlModel::load(const std::string& path, std::string& err, const char* catal
     // phiWidth x (lowerRes + higherRes) counts
     for (int k = 0; k < nf; ++k) {
         if (desorb_type[k] != MFG_DES_ANGLEMAP) continue;
-        const size_t n = size_t(std::max(am_phi_width[k], 0)) * size_t(std::max(am_lower[k] + am_higher[k], 0));
-        for (size_t i = 0; i < n; ++i) desorb_anglemap.push_back(i < am_maps[k].size() ? uint64_t(am_maps[k][i]) : 0ull);
+        const int64_t n = int64_t(std::max(am_phi_width[k], 0)) * std::max<int64_t>(int64_t(am_lower[k]) + am_higher[k], 0);
+        if (n > int64_t(INT32_MAX)) {
+            err = "facet " + std::to_string(k + 1) + ": angle map of more than 2^31-1 cells";
+            return false;
+        }
+        for (int64_t i = 0; i < n; ++i)
+            desorb_anglemap.push_back(size_t(i) < am_maps[k].size() ? to_u64(am_maps[k][size_t(i)]) : 0ull);
     }
     bool any_og = false;
     for (int k = 0; k < nf; ++k)
@@ -395,16 +411,16 @@ bool XmlModel::load(const std::string& path, std::string& err, const char* catal
         const XNode* gas = sims->child("Gas");
         desc.gas_mass = fa(gas, "mass", 28.0);
         if (const XNode* sc = kid(gas, "Scattering")) {   // LoaderXML.cpp:106-116 (rho is not in the file)
-            desc.scatter_enabled = int32_t(ia(sc, "enabled"));
+            desc.scatter_enabled = ia32(sc, "enabled");
             desc.scatter_mass_ratio = fa(sc, "massRatio", 1.0);
             desc.scatter_mean_free_path_cm = fa(sc, "meanFreePath_cm", 1e30);
             if (const XNode* co = sc->child("LowSpeedCutoff")) {
-                desc.scatter_cutoff_enabled = int32_t(ia(co, "enabled"));
+                desc.scatter_cutoff_enabled = ia32(co, "enabled");
                 desc.scatter_cutoff_speed = fa(co, "speed");
             }
         }
         if (const XNode* mo = sims->child("Motion")) {   // LoaderXML.cpp:144-160
-            desc.motion_type = int32_t(ia(mo, "type"));
+            desc.motion_type = ia32(mo, "type");
             if (desc.motion_type == 1) {
                 const XNode* v = mo->child("VelocityVector");
                 desc.motion_vector2[0] = fa(v, "vx"); desc.motion_vector2[1] = fa(v, "vy"); desc.motion_vector2[2] = fa(v, "vz");
@@ -415,22 +431,22 @@ bool XmlModel::load(const std::string& path, std::string& err, const char* catal
                 desc.motion_vector2[0] = fa(rv, "x"); desc.motion_vector2[1] = fa(rv, "y"); desc.motion_vector2[2] = fa(rv, "z");
             }
         }
-        desc.enable_decay = int32_t(ia(gas, "enableDecay"));
+        desc.enable_decay = ia32(gas, "enableDecay");
         desc.half_life = fa(gas, "halfLife", 1.0);
         if (const XNode* fm = sims->child("MeasureForces")) {   // LoaderXML.cpp:163-177
-            desc.enable_force_measurement = int32_t(ia(fm, "enabled"));
+            desc.enable_force_measurement = ia32(fm, "enabled");
             if (const XNode* rp = kid(fm->child("Torque"), "refPoint")) {
                 desc.torque_ref_point[0] = fa(rp, "x"); desc.torque_ref_point[1] = fa(rp, "y"); desc.torque_ref_point[2] = fa(rp, "z");
             }
         }
         const XNode* lf = sims->child("LowFluxMode");
-        desc.low_flux_mode = int32_t(ia(lf, "enabled"));
+        desc.low_flux_mode = ia32(lf, "enabled");
         desc.low_flux_cutoff = fa(lf, "cutoff", 1e-7);
         desc.global_histogram = hist_params(sims->child("Global_histograms"));
         const XNode* ts = sims->child("TimeSettings");
         desc.time_window = fa(ts, "timeWindow", 1e-10);
-        desc.use_maxwell = int32_t(ia(ts, "useMaxwellDistr", 1));
-        desc.constant_flow = int32_t(ia(ts, "calcConstFlow", 1));
+        desc.use_maxwell = ia32(ts, "useMaxwellDistr", 1);
+        desc.constant_flow = ia32(ts, "calcConstFlow", 1);
         user_moments(kid(ts, "UserMoments"), mt, mw);
     }
     {   // moments sorted by time (stable)
@@ -524,7 +540,7 @@ int read_results(const XNode* r, const mfg::HostModel& h, mfg_state_view* v, std
             if (v->facet_counts && hh) {
                 v->facet_counts[fo * MFG_FC_N + MFG_FC_NBMCHIT] = uint64_t(ia(hh, "nbHit"));
                 v->facet_counts[fo * MFG_FC_N + MFG_FC_NBDESORBED] = uint64_t(ia(hh, "nbDes"));
-                v->facet_counts[fo * MFG_FC_N + MFG_FC_NBABSORBED] = uint64_t(std::nearbyint(fa(hh, "nbAbsEquiv")));
+                v->facet_counts[fo * MFG_FC_N + MFG_FC_NBABSORBED] = to_u64(std::nearbyint(fa(hh, "nbAbsEquiv")));
             }
             if (v->facet_sums && hh) {
                 double* s = v->facet_sums + fo * MFG_FS_N;
@@ -555,7 +571,8 @@ int read_results(const XNode* r, const mfg::HostModel& h, mfg_state_view* v, std
                     if (!c) continue;
                     std::vector<double> vals;
                     numbers(c->text, vals);
-                    if (fw <= 0 || fh <= 0 || int64_t(vals.size()) < fw * fh) continue;
+                    const int64_t nv = int64_t(vals.size());
+                    if (fw <= 0 || fh <= 0 || fw > nv || fh > nv / fw) continue;   // fewer than fw*fh numbers
                     double* t = v->texture + (int64_t(mi) * L.texture_cells + h.tex_off[size_t(k)]) * 3;
                     for (int64_t y = 0; y < std::min(hgt, fh); ++y)
                         for (int64_t x = 0; x < std::min(w, fw); ++x) t[(y * w + x) * 3 + field] = vals[size_t(y * fw + x)];
@@ -603,7 +620,7 @@ int read_results(const XNode* r, const mfg::HostModel& h, mfg_state_view* v, std
             numbers(am->child("map")->text, vals);
             const int64_t o = h.ang_off[k];
             const int64_t n = std::min<int64_t>(int64_t(vals.size()), L.n_anglemap - o);
-            for (int64_t i = 0; i < n; ++i) v->anglemap[o + i] = uint64_t(vals[size_t(i)]);
+            for (int64_t i = 0; i < n; ++i) v->anglemap[o + i] = to_u64(vals[size_t(i)]);
         }
     }
     return MFG_OK;

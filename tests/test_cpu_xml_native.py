@@ -362,3 +362,79 @@ def test_native_reader_xml_syntax(tmp_path):
     bad.write_text("<A><B x=1/></A>")
     with pytest.raises(MfgError, match="unquoted"):
         _open(L, str(bad))
+
+
+def test_native_reader_extreme_values(tmp_path):
+    """Out-of-range numbers in a file: counts that are not a number or negative read as 0, a stored
+    texture whose declared size overflows is skipped, and a structure count past the limit is
+    refused with MFG_ERR_LIMIT, not attempted."""
+    L = _lib()
+    m, _, _ = golden_util.load("B02-lr10_pipe_tex")
+    st, _ = Oracle(m).run(3000, seed=5)
+    gm = GpuModel(m)
+    path = tmp_path / "b02.xml"
+    xmlwriter.save(str(path), m, st, gm.outgassing(), gm.facet_geometry()[1])
+    text = path.read_text()
+    text = text.replace('nbAbsEquiv="', 'nbAbsEquiv="nan', 1)   # "nan<number>": not a number
+    i = text.index("<MolflowResults")
+    j = text.index('<Texture width="', i) + len('<Texture width="')
+    text = text[:j] + "9.2e18" + text[text.index('"', j):]
+    bad = tmp_path / "extreme.xml"
+    bad.write_text(text)
+
+    def read(p):
+        h = _open(L, str(p))
+        try:
+            cd = L.mfg_xml_desc(h).contents
+            mh = C.c_void_p()
+            assert L.mfg_model_create(C.byref(cd), C.byref(mh)) == A.MFG_OK
+            try:
+                got = SimuState(m)
+                v = got.view()
+                assert L.mfg_xml_read_state(h, mh, C.byref(v)) == A.MFG_OK
+                return got
+            finally:
+                L.mfg_model_destroy(mh)
+        finally:
+            L.mfg_xml_close(h)
+    good, got = read(path), read(bad)
+    fc_good = good.facet_counts.reshape(-1, A.FC_N)
+    fc_got = got.facet_counts.reshape(-1, A.FC_N)
+    changed = np.flatnonzero(fc_good[:, A.FC_NBABSORBED] != fc_got[:, A.FC_NBABSORBED])
+    assert len(changed) == 1 and fc_got[changed[0], A.FC_NBABSORBED] == 0 and fc_good[changed[0], A.FC_NBABSORBED] > 0
+    # the texture with the overflowing declared size is left empty, the others are read
+    assert good.texture.any() and got.texture.sum() < good.texture.sum() and got.texture.any()
+    many = tmp_path / "structures.xml"
+    many.write_text(path.read_text().replace('<Structures nb="1"', '<Structures nb="2147483647"', 1))
+    h = _open(L, str(many))
+    try:
+        cd = L.mfg_xml_desc(h).contents
+        assert cd.n_structures == 2147483647
+        mh = C.c_void_p()
+        assert L.mfg_model_create(C.byref(cd), C.byref(mh)) == A.MFG_ERR_LIMIT
+    finally:
+        L.mfg_xml_close(h)
+
+
+def test_model_size_limits():
+    """Sizes past the device's 32-bit cell offsets and histogram settings that define no bins are
+    refused before anything is allocated for them."""
+    def code(m):
+        with pytest.raises(MfgError) as e:
+            GpuModel(m)
+        return e.value.code
+    m, _, _ = golden_util.load("B02-lr10_pipe_tex")
+    k = int(np.flatnonzero(m.tex_width * m.tex_height > 0)[0])
+    m.tex_width[k] = m.tex_height[k] = 50000.0   # 2.5e9 cells
+    assert code(m) == A.MFG_ERR_LIMIT
+    m, _, _ = golden_util.load("B02-lr10_pipe_tex")
+    m.tex_width[0] = float("nan")
+    assert code(m) == A.MFG_ERR_INVALID_MODEL
+    m, _, _ = golden_util.load("B02-lr10_pipe_tex")
+    m.n_structures = A.MFG_MAX_STRUCTURES + 1
+    assert code(m) == A.MFG_ERR_LIMIT
+    m, _, _ = golden_util.load("B02-lr10_pipe_tex")
+    m.hist_record[0] = A.HIST_DISTANCE
+    m.hist_distance_binsize[0] = 0.0
+    m.hist_distance_max[0] = 10.0
+    assert code(m) == A.MFG_ERR_INVALID_MODEL
