@@ -382,7 +382,9 @@ int build_host_model(const mfg_model_desc* d, HostModel& m, std::string& err, in
     const int32_t* fs = d->facet_vertex_start;
     if (fs[0] != 0) { err = "facet_vertex_start[0] must be 0"; return MFG_ERR_INVALID_MODEL; }
     for (int i = 0; i < nf; ++i)
-        if (fs[i + 1] - fs[i] < 3) { err = "facet " + std::to_string(i + 1) + " has fewer than 3 vertices"; return MFG_ERR_INVALID_MODEL; }
+        if (int64_t(fs[i + 1]) - fs[i] < 3) { err = "facet " + std::to_string(i + 1) + " has fewer than 3 vertices"; return MFG_ERR_INVALID_MODEL; }
+    for (int64_t k = 0; k < 3 * int64_t(d->n_vertices); ++k)
+        if (!std::isfinite(d->vertices[k])) { err = "vertex " + std::to_string(k / 3 + 1) + " is not a finite point"; return MFG_ERR_INVALID_MODEL; }
     m.v2.assign(2 * size_t(fs[nf]), 0.0);
     for (int i = 0; i < nf; ++i) {
         HostFacet& F = m.facets[i];

@@ -438,3 +438,11 @@ def test_model_size_limits():
     m.hist_distance_binsize[0] = 0.0
     m.hist_distance_max[0] = 10.0
     assert code(m) == A.MFG_ERR_INVALID_MODEL
+
+
+def test_model_rejects_non_finite_vertex():
+    m, _, _ = golden_util.load("B02-lr10_pipe_tex")
+    m.vertices[3, 1] = float("inf")
+    with pytest.raises(MfgError, match="not a finite point") as e:
+        GpuModel(m)
+    assert e.value.code == A.MFG_ERR_INVALID_MODEL
