@@ -36,6 +36,13 @@ template <class T, typename std::enable_if<std::is_integral<T>::value, int>::typ
 std::string num(T x) {
     return std::to_string(x);
 }
+// a count held as a double, written as an integer: not a number -> 0, clamped to the 64-bit range
+std::string count(double x) {
+    if (!(x == x)) return "0";
+    if (x >= 9.2e18) return num(9200000000000000000LL);
+    if (x <= -9.2e18) return num(-9200000000000000000LL);
+    return num((long long)x);
+}
 
 std::string esc(const std::string& s) {
     std::string o;
@@ -113,7 +120,7 @@ void hist_results(W& w, const mfg_histogram_params& p, const int32_t sizes[3], c
         if (!(p.record & rec[t]) || n <= 0) continue;
         w.open(tags[t], {{"size", num(n)}, {"binSize", bss[t]}, {"max", mxs[t]}});
         for (int32_t k = 0; k < n; ++k)
-            w.leaf("Bin", {{"start", k == n - 1 ? std::string("overRange") : (t == 0 ? num((long long)(k * (long long)p.bounce_binsize)) : num(k * bs[t]))},
+            w.leaf("Bin", {{"start", k == n - 1 ? std::string("overRange") : (t == 0 ? num(uint64_t(k) * p.bounce_binsize) : num(k * bs[t]))},
                            {"count", num(v[o + size_t(k)])}});
         w.close(tags[t]);
         o += size_t(n);
@@ -123,7 +130,10 @@ void hist_results(W& w, const mfg_histogram_params& p, const int32_t sizes[3], c
 bool write_stored_zip(const std::string& path, const std::string& inner, const std::string& data, std::string& err) {
     // one stored entry: local header, data, central directory, end record (PKWARE APPNOTE)
     const uint32_t crc = crc32(reinterpret_cast<const uint8_t*>(data.data()), data.size());
-    if (data.size() >= 0xffffffffull) { err = "the document is too large for a ZIP entry without ZIP64"; return false; }
+    if (data.size() + 2 * inner.size() + 128 >= 0xffffffffull || inner.size() > 0xffff) {   // offsets and sizes are 32-bit
+        err = "the document is too large for a ZIP archive without ZIP64";
+        return false;
+    }
     std::string z;
     auto u16 = [&](uint32_t v) { z += char(v & 0xff); z += char((v >> 8) & 0xff); };
     auto u32 = [&](uint32_t v) { u16(v & 0xffff); u16(v >> 16); };
@@ -316,10 +326,10 @@ bool write_file(const std::string& path, const mfg_model_desc& d, const mfg::Hos
                 const double* g = st->global;
                 auto gv = [&](int k) { return g ? g[k] : 0.0; };
                 w.open("Global", {});
-                w.leaf("Hits", {{"totalHit", num((long long)gv(MFG_G_NBMCHIT))}, {"totalHitEquiv", num(gv(MFG_G_NBHITEQUIV))},
-                                {"totalDes", num((long long)gv(MFG_G_NBDESORBED))}, {"totalAbsEquiv", num(gv(MFG_G_NBABSEQUIV))},
+                w.leaf("Hits", {{"totalHit", count(gv(MFG_G_NBMCHIT))}, {"totalHitEquiv", num(gv(MFG_G_NBHITEQUIV))},
+                                {"totalDes", count(gv(MFG_G_NBDESORBED))}, {"totalAbsEquiv", num(gv(MFG_G_NBABSEQUIV))},
                                 {"totalDist_total", num(gv(MFG_G_DIST_TOTAL))}, {"totalDist_fullHitsOnly", num(gv(MFG_G_DIST_FULLHITS))},
-                                {"totalLeak", num((long long)gv(MFG_G_NBLEAK))}, {"maxDesorption", "0"}});
+                                {"totalLeak", count(gv(MFG_G_NBLEAK))}, {"maxDesorption", "0"}});
                 w.leaf("Hit_Cache", {{"nb", "0"}});
                 w.leaf("Leak_Cache", {{"nb", "0"}});
                 w.close("Global");
@@ -388,7 +398,7 @@ bool write_file(const std::string& path, const mfg_model_desc& d, const mfg::Hos
                         rows += "\n";
                     }
                     w.text("vel.vectors", rows);
-                    w.text("count", grid(tw, th, [&](int64_t k) { return num((long long)dv[k * 4 + 3]); }));
+                    w.text("count", grid(tw, th, [&](int64_t k) { return count(dv[k * 4 + 3]); }));
                     w.close("Directions");
                 }
                 if (st->histogram && !h.fhist.empty() && h.fhist[size_t(i)].off >= 0 && d.facet_histogram) {

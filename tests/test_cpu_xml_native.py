@@ -446,3 +446,24 @@ def test_model_rejects_non_finite_vertex():
     with pytest.raises(MfgError, match="not a finite point") as e:
         GpuModel(m)
     assert e.value.code == A.MFG_ERR_INVALID_MODEL
+
+
+def test_native_writer_counts_out_of_range(tmp_path):
+    """Counts held as doubles that are not a number or past the 64-bit range are written as 0 and
+    as the clamped value, not converted with undefined results."""
+    L = _lib()
+    L.mfg_xml_save.argtypes = [C.c_char_p, C.POINTER(A.ModelDesc), C.c_void_p, C.POINTER(A.StateView),
+                               C.POINTER(C.c_char_p)]
+    m, _, _ = golden_util.load("B02-lr10_pipe_tex")
+    st, _ = Oracle(m).run(3000, seed=5)
+    gm = GpuModel(m)
+    st.global_[A.G_NBMCHIT] = float("nan")
+    st.global_[A.G_NBDESORBED] = -1e300
+    st.global_[A.G_NBLEAK] = 1e300
+    path = str(tmp_path / "counts.xml")
+    v = st.view()
+    assert L.mfg_xml_save(path.encode(), C.byref(gm._desc), gm.h, C.byref(v), None) == A.MFG_OK
+    _, st2, _ = xmlio.load(path)
+    assert st2.global_[A.G_NBMCHIT] == 0
+    assert st2.global_[A.G_NBDESORBED] == -9.2e18
+    assert st2.global_[A.G_NBLEAK] == 9.2e18
