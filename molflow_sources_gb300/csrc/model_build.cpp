@@ -2,6 +2,7 @@
 #include "model_build.h"
 
 #include <algorithm>
+#include <climits>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -1172,8 +1173,23 @@ int merge_host_models(const std::vector<const HostModel*>& parts, HostModel& out
     out.nstruct = 0;
     out.bvh_depth = 0;
     out.scene_scale = 0;
+    int inst = 0;
     for (const HostModel* pp : parts) {
         const HostModel& p = *pp;
+        ++inst;
+        // the merged arrays are addressed with 32-bit offsets on the device
+        auto fits = [](int64_t have, int64_t add) { return have + add <= int64_t(INT32_MAX); };
+        if (!fits(out.nf, p.nf) || !fits(out.nstruct, p.nstruct) || !fits(out.layout.texture_cells, p.layout.texture_cells) ||
+            !fits(out.layout.direction_cells, p.layout.direction_cells) || !fits(out.layout.anglemap_cells, p.layout.anglemap_cells) ||
+            !fits(out.layout.profile_facets, p.layout.profile_facets) || !fits(int64_t(out.nodes_d.size()), int64_t(p.nodes_d.size())) ||
+            !fits(int64_t(out.nodes_c.size()), int64_t(p.nodes_c.size())) || !fits(int64_t(out.prims.size()), int64_t(p.prims.size())) ||
+            !fits(int64_t(out.prims_c.size()), int64_t(p.prims_c.size())) || !fits(int64_t(out.v2_d.size()), int64_t(p.v2_d.size())) ||
+            !fits(int64_t(out.src_facet.size()), int64_t(p.src_facet.size())) || !fits(int64_t(out.id_t.size()), int64_t(p.id_t.size())) ||
+            !fits(int64_t(out.par_t.size()), int64_t(p.par_t.size()))) {
+            err = "the merged model passes 2^31-1 facets, structures, cells, BVH nodes or table entries at instance " +
+                  std::to_string(inst);
+            return MFG_ERR_LIMIT;
+        }
         HostModel::Instance in = p.instances[0];
         in.facet_base = out.nf;
         in.struct_base = out.nstruct;
