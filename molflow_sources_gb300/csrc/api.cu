@@ -1100,8 +1100,10 @@ int mfg_update_sticking(mfg_sim* s, int32_t n, const int32_t* facets, const doub
 
 int mfg_sens_setup(mfg_sim* s, int32_t n_params, const int32_t* param_facets, int32_t n_gauges, const int32_t* gauge_facets,
                    int32_t n_pumps, const int32_t* pump_facets) {
-    if (!s || n_params < 0 || n_gauges < 0 || n_gauges > MFG_SENS_NOUT - 1 || n_pumps < 0)
+    if (!s || n_params < 0 || n_gauges < 0 || n_gauges > MFG_SENS_NOUT - 1 || n_pumps < 0 || (n_params && !param_facets) ||
+        (n_gauges && !gauge_facets) || (n_pumps && !pump_facets))
         return fail(MFG_ERR_INVALID_ARGUMENT, "bad argument (at most 8 gauges)");
+    if (n_params >= (1 << 20) - 1) return fail(MFG_ERR_INVALID_ARGUMENT, "at most 2^20 - 2 parameters");
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->running) return fail(MFG_ERR_BUSY, "run in flight");
     const mfg::HostModel& h = s->model->h;
@@ -1131,11 +1133,13 @@ int mfg_sens_setup(mfg_sim* s, int32_t n_params, const int32_t* param_facets, in
         if (f < 0 || f >= h.nf) return fail(MFG_ERR_INVALID_ARGUMENT, "bad pump facet");
         pump[f] = 1;
     }
+    s->js.clear();   // a Jacobian of the previous setup has other sizes
+    s->jq.clear();
+    s->jy.clear();
     s->sens_src.clear();
     for (size_t k = 0; k < h.src_facet.size(); ++k) { sof[h.src_facet[k]] = int32_t(k); s->sens_src.push_back(h.src_facet[k]); }
     s->sens_params.assign(param_facets, param_facets + n_params);
     const size_t P = size_t(std::max(n_params, 1)), S = std::max<size_t>(s->sens_src.size(), 1), nf = size_t(h.nf);
-    if (n_params >= (1 << 20) - 1) return fail(MFG_ERR_INVALID_ARGUMENT, "at most 2^20 - 2 parameters");
     std::vector<int32_t> code(h.nf, 0);   // packed: parameter + 1 (bits 0-19), gauge + 1 (20-23), pump (24)
     for (int f = 0; f < h.nf; ++f)
         code[f] = (pof[f] + 1) | ((gof[f] + 1) << 20) | (int32_t(pump[f]) << 24);
@@ -1145,6 +1149,7 @@ int mfg_sens_setup(mfg_sim* s, int32_t n_params, const int32_t* param_facets, in
     const size_t off_C = off_B + 8 * P * MFG_SENS_NOUT, off_Y = off_C + 8 * S * MFG_SENS_NOUT;
     const size_t off_cnt = off_Y + 8 * MFG_SENS_NOUT, off_ovf = off_cnt + 8 * S, total = off_ovf + 8;
     CK(cudaSetDevice(s->device));
+    s->sens_ready = false;   // until the new block is filled
     if (s->sens_block) { cudaFree(s->sens_block); s->sens_block = nullptr; }
     CK(cudaMalloc(&s->sens_block, total));
     char* b = static_cast<char*>(s->sens_block);
@@ -1218,7 +1223,7 @@ int mfg_sens_forward(mfg_sim* s, uint64_t n, const mfg_run_options* opt, double*
 }
 
 int mfg_sens_jacobian(mfg_sim* s, double* d_sticking, double* d_outgassing, int32_t* source_facets) {
-    if (!s || s->js.empty() && !s->sens_params.empty()) return fail(MFG_ERR_INVALID_ARGUMENT, "no forward pass yet");
+    if (!s || s->jy.empty()) return fail(MFG_ERR_INVALID_ARGUMENT, "no forward pass yet");
     if (d_sticking) std::copy(s->js.begin(), s->js.end(), d_sticking);
     if (d_outgassing) std::copy(s->jq.begin(), s->jq.end(), d_outgassing);
     if (source_facets) std::copy(s->sens_src.begin(), s->sens_src.end(), source_facets);

@@ -247,3 +247,25 @@ def test_gradients_after_autotune(setup):
     y_plain = sf.forward(n, precision=A.PREC_FP32R, seed=SEED, block_size=256, blocks_per_sm=2)
     # the same particles; FP64 output sums added in another order
     np.testing.assert_allclose(y_tuned, y_plain, rtol=1e-9, atol=0)
+
+
+def test_new_setup_drops_the_previous_jacobian():
+    """A new mfg_sens_setup (other parameters) drops the Jacobian of the previous one: backward and
+    jacobian refuse until the next forward pass, instead of reading the old, smaller matrices."""
+    from molflow_sources_gb300.simulation import MfgError
+    m = config5_neg_tube()
+    sim = GpuSimulation(m)
+    try:
+        sf = SensitivityFunction(sim, m.neg[:10], m.gauges, m.neg)
+        sf.forward(20000, precision=A.PREC_FP32R, seed=SEED)
+        sf.backward(np.ones(9))
+        sf2 = SensitivityFunction(sim, m.neg, m.gauges, m.neg)
+        for call in (lambda: sf2.backward(np.ones(9)), sf2.jacobian):
+            with pytest.raises(MfgError) as e:
+                call()
+            assert e.value.code == A.MFG_ERR_INVALID_ARGUMENT
+        sf2.forward(20000, precision=A.PREC_FP32R, seed=SEED)
+        js, jq, src = sf2.jacobian()
+        assert js.shape == (len(m.neg), 9) and np.isfinite(js).all()
+    finally:
+        sim.close()
