@@ -467,3 +467,69 @@ def test_native_writer_counts_out_of_range(tmp_path):
     assert st2.global_[A.G_NBMCHIT] == 0
     assert st2.global_[A.G_NBDESORBED] == -9.2e18
     assert st2.global_[A.G_NBLEAK] == 9.2e18
+
+
+def test_native_reader_survives_mutated_files(tmp_path):
+    """Seeded attribute mutations of a written file (extreme numbers, not a number, empty values):
+    the C++ reader, the model build, the results read and the writer either succeed or return an
+    error code; none of them crashes.  (The same mutations ran at scale under sanitizers.)"""
+    import random
+    L = _lib()
+    L.mfg_xml_save.argtypes = [C.c_char_p, C.POINTER(A.ModelDesc), C.c_void_p, C.POINTER(A.StateView),
+                               C.POINTER(C.c_char_p)]
+    m, _, _ = golden_util.load("01-quick_pipe_profiles_textures_2sided")
+    st, _ = Oracle(m).run(3000, seed=5)
+    gm = GpuModel(m)
+    base = str(tmp_path / "base.xml")
+    xmlwriter.save(base, m, st, gm.outgassing(), gm.facet_geometry()[1])
+    text = open(base).read()
+    values = ["-1", "0", "2147483647", "-2147483648", "1e300", "-1e300", "nan", "inf", "", "x", "4294967296",
+              "65536", "3", "-5", "0.5", "1e-300", "9223372036854775807"]
+    r = random.Random(20261205)
+    outcomes = {"read": 0, "model": 0, "results": 0, "refused": 0}
+    for it in range(400):
+        t = text
+        for _ in range(1 + r.randrange(6)):
+            q = t.find('="', r.randrange(len(t)))
+            if q < 0:
+                continue
+            e = t.find('"', q + 2)
+            t = t[:q + 2] + r.choice(values) + t[e:]
+        p = str(tmp_path / "m.xml")
+        open(p, "w").write(t)
+        h = C.c_void_p()
+        if L.mfg_xml_open(p.encode(), C.byref(h)) != A.MFG_OK:
+            outcomes["refused"] += 1
+            continue
+        outcomes["read"] += 1
+        try:
+            cd = L.mfg_xml_desc(h).contents
+            mh = C.c_void_p()
+            if L.mfg_model_create(C.byref(cd), C.byref(mh)) != A.MFG_OK:
+                continue
+            outcomes["model"] += 1
+            try:
+                lay = A.StateLayout()
+                assert L.mfg_state_layout_of(mh, C.byref(lay)) == A.MFG_OK
+                if max(lay.n_texture, lay.n_facet_counts, lay.n_histogram, lay.n_direction, lay.n_profile) > 10 ** 7:
+                    continue
+                arrays = {f: np.zeros(max(1, getattr(lay, "n_" + f)), np.uint64 if f in ("facet_counts", "anglemap")
+                                      else np.float64)
+                          for f in ("global", "facet_counts", "facet_sums", "texture", "profile", "direction",
+                                    "anglemap", "histogram", "force")}
+                v = A.StateView(*[arrays[f].ctypes.data_as(C.POINTER(C.c_uint64 if arrays[f].dtype == np.uint64
+                                                                      else C.c_double)) for f in
+                                  ("global", "facet_counts", "facet_sums", "texture", "profile", "direction",
+                                   "anglemap", "histogram", "force")])
+                if L.mfg_xml_read_state(h, mh, C.byref(v)) == A.MFG_OK:
+                    outcomes["results"] += 1
+                    out = str(tmp_path / "w.zip")
+                    if L.mfg_xml_save(out.encode(), C.byref(cd), mh, C.byref(v), None) == A.MFG_OK:
+                        h2 = C.c_void_p()
+                        assert L.mfg_xml_open(out.encode(), C.byref(h2)) == A.MFG_OK
+                        L.mfg_xml_close(h2)
+            finally:
+                L.mfg_model_destroy(mh)
+        finally:
+            L.mfg_xml_close(h)
+    assert outcomes["results"] > 10 and outcomes["model"] < outcomes["read"]
