@@ -21,7 +21,7 @@ import numpy as np
 
 from . import _abi as A
 from .model import Model
-from .simulation import GpuSimulation, _check, load_library
+from .simulation import GpuSimulation, _check, _count, load_library
 
 N_OUT = 9   # 8 gauges + pumped flux
 
@@ -77,7 +77,7 @@ class SensitivityFunction:
         out = np.zeros(N_OUT)
         st = A.RunStats()
         o = A.RunOptions(precision=precision, seed=seed, block_size=block_size, blocks_per_sm=blocks_per_sm)
-        _check(load_library().mfg_sens_forward(self.sim.h, int(n), C.byref(o), A.ptr(out, C.c_double), C.byref(st)))
+        _check(load_library().mfg_sens_forward(self.sim.h, _count(n, "n"), C.byref(o), A.ptr(out, C.c_double), C.byref(st)))
         self.last_stats = {f: getattr(st, f) for f, _ in A.RunStats._fields_}
         return out
 

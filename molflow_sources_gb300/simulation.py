@@ -115,6 +115,15 @@ def _check(rc):
     return rc
 
 
+def _count(n, what="count"):
+    """A particle count or id for an unsigned 64-bit argument of the C ABI (ctypes would wrap a
+    negative number)."""
+    n = int(n)
+    if n < 0 or n >= 1 << 64:
+        raise ValueError("%s must be in [0, 2^64), got %d" % (what, n))
+    return n
+
+
 class GpuModel:
     """Device-independent prepared model (facet basis, BVH, tables) — mfg_model."""
 
@@ -203,7 +212,7 @@ class GpuSimulation:
                     L["n_direction"] + L["n_anglemap"])
 
     def set_particle_offset(self, first_particle):
-        _check(load_library().mfg_set_particle_offset(self.h, int(first_particle)))
+        _check(load_library().mfg_set_particle_offset(self.h, _count(first_particle, "first_particle")))
 
     def particle_offset(self):
         return int(load_library().mfg_particle_offset(self.h))
@@ -219,7 +228,7 @@ class GpuSimulation:
                          time_limit_s=time_limit_s, max_steps_per_particle=max_steps, use_graph=int(use_graph),
                          smem_bvh_levels=smem_bvh_levels, particles_per_request=particles_per_request)
         st = A.RunStats()
-        rc = load_library().mfg_run(self.h, int(n_desorptions), C.byref(o), C.byref(st))
+        rc = load_library().mfg_run(self.h, _count(n_desorptions, "n_desorptions"), C.byref(o), C.byref(st))
         self.last_stats = {f: getattr(st, f) for f, _ in A.RunStats._fields_}
         if rc == A.MFG_ERR_NO_SOURCE:
             return MCStepResult.DesorptionError
@@ -235,13 +244,13 @@ class GpuSimulation:
     def autotune(self, n_trial, precision=A.PREC_FP32R, seed=0x4D6F6C66):
         """Pick the fastest launch shape for this model (clears tallies); returns it as a dict."""
         o = A.RunOptions()
-        _check(load_library().mfg_autotune(self.h, int(n_trial), precision, seed, C.byref(o)))
+        _check(load_library().mfg_autotune(self.h, _count(n_trial, "n_trial"), precision, seed, C.byref(o)))
         return {"block_size": o.block_size, "blocks_per_sm": o.blocks_per_sm, "smem_bvh_levels": o.smem_bvh_levels,
                 "particles_per_request": o.particles_per_request}
 
     def run_async(self, n_desorptions, precision=A.PREC_FP64, seed=0x4D6F6C66, time_limit_s=0.0):
         o = A.RunOptions(precision=precision, seed=seed, time_limit_s=time_limit_s)
-        _check(load_library().mfg_run_async(self.h, int(n_desorptions), C.byref(o)))
+        _check(load_library().mfg_run_async(self.h, _count(n_desorptions, "n_desorptions"), C.byref(o)))
 
     def poll(self):
         return load_library().mfg_poll(self.h)
@@ -340,7 +349,7 @@ class GpuBatch:
         """counts: particles per instance (int applies to all)."""
         if np.isscalar(counts):
             counts = [int(counts)] * len(self.models)
-        c = np.ascontiguousarray(counts, dtype=np.uint64)
+        c = np.ascontiguousarray([_count(k, "counts") for k in counts], dtype=np.uint64)
         if not time_limit_s:
             time_limit_s = float(os.environ.get("MFG_TIME_LIMIT_S", "0"))
         o = A.RunOptions(precision=precision, seed=seed, block_size=block_size, blocks_per_sm=blocks_per_sm,
@@ -355,7 +364,7 @@ class GpuBatch:
     def autotune(self, n_trial, precision=A.PREC_FP32R, seed=0x4D6F6C66):
         """Fastest launch shape for the batch (n_trial particles per instance per trial); clears tallies."""
         o = A.RunOptions()
-        _check(load_library().mfg_autotune(self.h, int(n_trial), precision, seed, C.byref(o)))
+        _check(load_library().mfg_autotune(self.h, _count(n_trial, "n_trial"), precision, seed, C.byref(o)))
         return {"block_size": o.block_size, "blocks_per_sm": o.blocks_per_sm, "smem_bvh_levels": o.smem_bvh_levels,
                 "particles_per_request": o.particles_per_request}
 
@@ -369,7 +378,7 @@ class GpuBatch:
         _check(load_library().mfg_reset(self.h))
 
     def set_particle_offset(self, first_particle):
-        _check(load_library().mfg_set_particle_offset(self.h, int(first_particle)))
+        _check(load_library().mfg_set_particle_offset(self.h, _count(first_particle, "first_particle")))
 
     def close(self):
         L = load_library()

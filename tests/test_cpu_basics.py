@@ -208,3 +208,13 @@ def test_sim_create_without_device_fails_cleanly():
     with pytest.raises(MfgError) as e:
         GpuSimulation(config1_tube())
     assert e.value.code == A.MFG_ERR_NO_DEVICE
+
+
+def test_counts_for_unsigned_arguments():
+    """Particle counts and ids go to unsigned 64-bit C arguments: a negative number is refused
+    instead of wrapping to 2^64 - n."""
+    from molflow_sources_gb300.simulation import _count
+    assert _count(0) == 0 and _count(2 ** 64 - 1) == 2 ** 64 - 1
+    for bad in (-1, 2 ** 64):
+        with pytest.raises(ValueError):
+            _count(bad)
